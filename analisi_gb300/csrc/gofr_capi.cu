@@ -1,0 +1,927 @@
+// C ABI of the GB300 Gofrt engine (declared in include/gofr_gb300.h).
+//
+// Host-side responsibilities:
+//   * frame residency: the reference's internal FP64 buffers are copied once
+//     into HBM and converted there to FP32 {x,y,z,type} records;
+//   * calc_init semantics (lib/src/gofrt.cpp:41-93): leff, the trajectory
+//     length check, origins/lags grid, incr;
+//   * exact bin thresholds in d2 space (gofr_bin_thresholds) and the certified
+//     FP32 error bound that turns them into FP32 windows (certify());
+//   * kernel selection, launches, counts back to the caller;
+//   * the reference's double result buffer from counts, including its exact
+//     per-thread fold (gofr_counts_to_buffer).
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/gofr_gb300.h"
+#include "gofr_internal.h"
+
+using namespace gofr;
+
+namespace {
+
+struct BoxStats {
+    double Lmin[3], Lmax[3];   // full edges 2*lh over all frames
+    double eL[3];              // max |fl32(L) - L|
+    double tmax[3];            // max |tilt| {xy, xz, yz}
+    double eT[3];              // max |fl32(tilt) - tilt|
+    double lh_min;             // min half edge over frames and axes
+};
+
+struct TrajDev {
+    size_t T = 0, N = 0;
+    unsigned ntypes = 0;
+    int tric = 0;
+    double *pos64 = nullptr;
+    float4 *pos32 = nullptr;
+    double *box64 = nullptr;
+    Box32 *box32 = nullptr;
+    int *types = nullptr;
+    std::vector<double> h_box;  // [T][9]
+    double shift[3] = {0, 0, 0};
+    double M[3] = {0, 0, 0};    // bound on |fl64(x - shift)| per axis
+    BoxStats bs{};
+    gofr_params params{};       // batch parameters
+    size_t out_offset = 0, out_count = 0;
+};
+
+}  // namespace
+
+struct gofr_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    std::vector<TrajDev> trajs;
+    unsigned long long *d_counts = nullptr;
+    size_t cap_counts = 0;
+    float2 *d_win = nullptr;
+    size_t cap_win = 0;
+    unsigned short *d_chtab = nullptr;
+    size_t cap_chtab = 0;
+    unsigned *d_err = nullptr;
+    unsigned long long *d_stats = nullptr;
+    double *d_minmax = nullptr;
+    unsigned *d_nonfinite = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    gofr_stats stats{};
+    size_t batch_total = 0;
+};
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+namespace {
+
+int fail(gofr_ctx *ctx, int code, const char *fmt, ...)
+{
+    if (ctx) {
+        char buf[1024];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        ctx->err = buf;
+    }
+    return code;
+}
+
+#define CK(call)                                                                             \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return fail(ctx, e_ == cudaErrorMemoryAllocation ? GOFR_ERR_NOMEM : GOFR_ERR_CUDA, \
+                        "%s failed: %s", #call, cudaGetErrorString(e_));                     \
+    } while (0)
+
+struct DevGuard {
+    int prev = -1;
+    explicit DevGuard(int d)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != d) cudaSetDevice(d);
+    }
+    ~DevGuard()
+    {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+template <typename T>
+int ensure(gofr_ctx *ctx, T *&p, size_t &cap, size_t n)
+{
+    if (n <= cap && p) return GOFR_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+    CK(cudaMalloc(reinterpret_cast<void **>(&p), bytes));
+    cap = n;
+    return GOFR_OK;
+}
+
+void free_traj(TrajDev &t)
+{
+    cudaFree(t.pos64);
+    cudaFree(t.pos32);
+    cudaFree(t.box64);
+    cudaFree(t.box32);
+    cudaFree(t.types);
+    t.pos64 = nullptr; t.pos32 = nullptr; t.box64 = nullptr; t.box32 = nullptr; t.types = nullptr;
+}
+
+inline uint64_t dbits(double x) { uint64_t u; std::memcpy(&u, &x, 8); return u; }
+inline double bitsd(uint64_t u) { double x; std::memcpy(&x, &u, 8); return x; }
+
+// Smallest float >= x / largest float <= x / largest float < x.
+inline float f_up(double x)
+{
+    float f = (float)x;
+    if ((double)f < x) f = std::nextafter(f, INFINITY);
+    return f;
+}
+inline float f_down(double x)
+{
+    float f = (float)x;
+    if ((double)f > x) f = std::nextafter(f, -INFINITY);
+    return f;
+}
+inline float f_below(double x)
+{
+    float f = f_down(x);
+    if ((double)f >= x) f = std::nextafter(f, -INFINITY);
+    return f;
+}
+
+// ---------------------------------------------------------------------------
+// Reference binning on the host (lib/src/gofrt.cpp:104,114-118).  Compiled
+// without FMA contraction (the build passes -fmad=false / -ffp-contract=off);
+// the expressions below contain no multiply-add anyway.
+// ---------------------------------------------------------------------------
+struct BinMap {
+    double rmin, rmax, dr, rmin2, rmax2;
+    unsigned nbin;
+    explicit BinMap(double rmin_, double rmax_, unsigned nbin_)
+        : rmin(rmin_), rmax(rmax_), nbin(nbin_)
+    {
+        dr = (rmax - rmin) / nbin;
+        rmax2 = rmax * rmax;
+        rmin2 = rmin * rmin;
+    }
+    // floorf((float)((sqrt(d2)-rmin)/dr)) as a float: monotone non-decreasing in d2 >= 0
+    float raw(double d2) const
+    {
+        double d = std::sqrt(d2);
+        return std::floor((float)((d - rmin) / dr));
+    }
+};
+
+// smallest non-negative double in [lo, hi] with pred true (pred monotone
+// false..true over the ordered doubles), or hi+ when none.
+template <typename P>
+double first_true(double lo, double hi, P pred)
+{
+    uint64_t a = dbits(lo), b = dbits(hi);
+    if (!pred(hi)) return std::nextafter(hi, INFINITY);
+    while (a < b) {
+        uint64_t m = a + (b - a) / 2;
+        if (pred(bitsd(m))) b = m;
+        else a = m + 1;
+    }
+    return bitsd(a);
+}
+
+bool regular_bins(double rmin, double rmax, unsigned nbin)
+{
+    if (!std::isfinite(rmin) || !std::isfinite(rmax) || !(rmax > rmin) || nbin == 0) return false;
+    if (nbin >= (1u << 24)) return false;
+    double dr = (rmax - rmin) / nbin;
+    if (!(dr > 0.0) || !std::isfinite(dr)) return false;
+    if (!std::isfinite(rmax * rmax) || !std::isfinite(rmin * rmin)) return false;
+    return true;
+}
+
+// th[0..nbin]; returns false when the accepted window is empty.
+bool thresholds(const BinMap &bm, double *th)
+{
+    const double top = bitsd(0x7FEFFFFFFFFFFFFFull);
+    double P = first_true(0.0, top, [&](double x) { return bm.raw(x) >= 0.0f; });
+    double Q = first_true(0.0, top, [&](double x) { return bm.raw(x) >= (float)bm.nbin; });
+    double A = std::max(bm.rmin2, P);
+    double B = std::min(bm.rmax2, std::nextafter(Q, -INFINITY));
+    if (!(A <= B)) {
+        for (unsigned b = 0; b <= bm.nbin; ++b) th[b] = 0.0;
+        return false;
+    }
+    th[0] = A;
+    double Bp = std::nextafter(B, INFINITY);
+    for (unsigned b = 1; b < bm.nbin; ++b)
+        th[b] = first_true(A, B, [&](double x) { return bm.raw(x) >= (float)b; });
+    for (unsigned b = 1; b < bm.nbin; ++b)
+        if (th[b] > Bp) th[b] = Bp;
+    th[bm.nbin] = Bp;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Certified FP32 error bound.
+//
+// The FP32 kernel computes, per axis, d = fl32(a_i - a_j) from coordinates
+// a = fl32(fl64(x - shift)), wraps it with k = rint(d/L) and an FMA
+// d - k*fl32(L) (triclinic: the z and y wraps also subtract k*fl32(tilt)),
+// and forms d2 = fma(z,z, fma(y,y, x*x)).  For every pair whose wrap counts k
+// equal the reference's, each final component differs from the reference's
+// by at most e_k + 2^-24 |x_k|, where e_k collects (all bounds are maxima
+// over frames):
+//   2 eps_k                 quantisation of both coordinates, eps = 2^-24 M
+//   2^-24 (D_k + 2 eps_k)   rounding of the FP32 difference, D = 2 M
+//   2^-53 D_k               rounding of the reference's FP64 difference
+//   k_max (|fl32(L)-L| + 2^-53 (D+L))    FP32 box edge, reference's k roundings
+//   (triclinic) the same for the tilt terms, plus 2^-24 of each intermediate.
+// Summing squares with Cauchy-Schwarz gives, with e = ||e_k||_2 and s the
+// reference d2:
+//   |d2_f32 - d2_ref| <= E(s) = (2 sqrt(s) e + 2 e^2 + 5.01 * 2^-24 s) (1 + 2^-20)
+// (the last term covers 2^-23 s from the relative component error, three FP32
+// roundings of the sum and four FP64 roundings of the reference).  E and
+// s - E(s) are both increasing in s, which is what the window construction
+// in certify() uses.
+// ---------------------------------------------------------------------------
+struct Bound {
+    double e[3];       // per-axis absolute component error
+    double enorm;      // ||e||_2
+    double eta;        // max error of a wrap quotient d/L (for the wrap check)
+    double kmax[3];
+};
+
+Bound error_bound(const TrajDev &t)
+{
+    Bound b{};
+    const double u24 = std::ldexp(1.0, -24), u53 = std::ldexp(1.0, -53);
+    double eps[3], D[3], eraw[3];
+    for (int k = 0; k < 3; ++k) {
+        eps[k] = t.M[k] * u24 * (1.0 + std::ldexp(1.0, -20)) + t.M[k] * std::ldexp(1.0, -52);
+        D[k] = 2.0 * t.M[k] * (1.0 + std::ldexp(1.0, -40)) + 2.0 * eps[k];
+        eraw[k] = 2.0 * eps[k] + u24 * (D[k] + 2.0 * eps[k]) + u53 * D[k];
+    }
+    const BoxStats &s = t.bs;
+    auto kmax_of = [](double Dk, double Lmin) { return std::floor(Dk / Lmin + 0.5) + 1.0; };
+    if (!t.tric) {
+        for (int k = 0; k < 3; ++k) {
+            b.kmax[k] = kmax_of(D[k], s.Lmin[k]);
+            b.e[k] = eraw[k] + b.kmax[k] * (s.eL[k] + u53 * (D[k] + s.Lmax[k]));
+        }
+    } else {
+        // z
+        b.kmax[2] = kmax_of(D[2], s.Lmin[2]);
+        b.e[2] = eraw[2] + b.kmax[2] * (s.eL[2] + u53 * (D[2] + s.Lmax[2]));
+        // y after the z wrap (tilt yz = tilt index 2)
+        double Dy = D[1] + b.kmax[2] * s.tmax[2];
+        double ey1 = eraw[1] + b.kmax[2] * (s.eT[2] + u53 * Dy) + u24 * Dy;
+        b.kmax[1] = kmax_of(Dy, s.Lmin[1]);
+        b.e[1] = ey1 + b.kmax[1] * (s.eL[1] + u53 * (Dy + s.Lmax[1]));
+        // x after the z (xz = tilt 1) and y (xy = tilt 0) wraps
+        double Dx = D[0] + b.kmax[2] * s.tmax[1] + b.kmax[1] * s.tmax[0];
+        double ex2 = eraw[0] + b.kmax[2] * (s.eT[1] + u53 * Dx) + u24 * Dx +
+                     b.kmax[1] * (s.eT[0] + u53 * Dx) + u24 * Dx;
+        b.kmax[0] = kmax_of(Dx, s.Lmin[0]);
+        b.e[0] = ex2 + b.kmax[0] * (s.eL[0] + u53 * (Dx + s.Lmax[0]));
+        D[1] = Dy;
+        D[0] = Dx;
+    }
+    b.enorm = std::sqrt(b.e[0] * b.e[0] + b.e[1] * b.e[1] + b.e[2] * b.e[2]);
+    b.eta = 0.0;
+    for (int k = 0; k < 3; ++k) {
+        double eq = b.e[k] / s.Lmin[k] + (D[k] / s.Lmin[k] + 1.0) * std::ldexp(1.0, -22);
+        b.eta = std::max(b.eta, eq);
+    }
+    return b;
+}
+
+inline double Efun(const Bound &b, double s)
+{
+    if (s < 0) s = 0;
+    double E = (2.0 * std::sqrt(s) * b.enorm + 2.0 * b.enorm * b.enorm +
+                5.01 * std::ldexp(1.0, -24) * s) * (1.0 + std::ldexp(1.0, -20));
+    // slack for the double arithmetic of the window construction itself
+    return E * 1.01 + std::ldexp(1.0, -50) * s + 1e-300;
+}
+
+struct Windows {
+    std::vector<float2> win;
+    float hi_f, lo_f;
+    double E_rmax;
+};
+
+void certify(const Bound &b, const double *th, unsigned nbin, Windows &w)
+{
+    w.win.resize(nbin);
+    for (unsigned k = 0; k < nbin; ++k) {
+        float lo = th[k] <= 0.0 ? -INFINITY : f_up(th[k] + Efun(b, th[k]));
+        float hi = f_below(th[k + 1] - Efun(b, th[k + 1]));
+        w.win[k] = make_float2(lo, hi);
+    }
+    w.hi_f = f_up(th[nbin] + Efun(b, th[nbin]));
+    w.lo_f = th[0] <= 0.0 ? -INFINITY : f_down(th[0] - Efun(b, th[0]));
+    w.E_rmax = Efun(b, th[nbin]);
+}
+
+struct RunShape {
+    unsigned leff = 0, ntimesteps = 0, skip = 1, every = 1, nch = 0;
+    unsigned n_lags = 0, n_orig = 0;
+    size_t data_length = 0;
+};
+
+int shape_of(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, RunShape &rs)
+{
+    if (p.nbin == 0) return fail(ctx, GOFR_ERR_ARG, "nbin must be > 0");
+    rs.skip = p.skip ? p.skip : 1;
+    rs.every = p.every ? p.every : 1;
+    rs.ntimesteps = p.ntimesteps;
+    rs.leff = (p.ntimesteps < p.tmax || p.tmax == 0) ? p.ntimesteps : p.tmax;
+    rs.nch = t.ntypes * (t.ntypes + 1);
+    rs.data_length = (size_t)rs.leff * rs.nch * p.nbin;
+    rs.n_lags = (rs.leff + rs.every - 1) / rs.every;
+    rs.n_orig = (rs.ntimesteps + rs.skip - 1) / rs.skip;
+    if ((unsigned long long)rs.leff + rs.ntimesteps + p.primo > (unsigned long long)t.T + 1)
+        return fail(ctx, GOFR_ERR_RANGE,
+                    "trajectory is too short for this kind of calculation. Select a different "
+                    "starting timestep or lower the size of the average or the lenght of the "
+                    "time lag");
+    return GOFR_OK;
+}
+
+// Upload one trajectory into t (device buffers owned by t).
+int upload_traj(gofr_ctx *ctx, TrajDev &t, const double *positions, const double *boxes,
+                int box_kind, const int *type_ids, unsigned ntypes, size_t natoms, size_t nframes)
+{
+    if (!positions || !boxes || !type_ids)
+        return fail(ctx, GOFR_ERR_ARG, "null positions, boxes or type ids");
+    if (natoms == 0 || nframes == 0) return fail(ctx, GOFR_ERR_ARG, "empty trajectory");
+    if (natoms > (size_t)INT32_MAX / 2) return fail(ctx, GOFR_ERR_ARG, "too many atoms");
+    if (box_kind != GOFR_BOX_ORTHO && box_kind != GOFR_BOX_TRICLINIC)
+        return fail(ctx, GOFR_ERR_ARG, "invalid box kind %d", box_kind);
+    if (ntypes == 0 || ntypes > 255) return fail(ctx, GOFR_ERR_ARG, "ntypes must be in 1..255");
+    for (size_t a = 0; a < natoms; ++a)
+        if (type_ids[a] < 0 || (unsigned)type_ids[a] >= ntypes)
+            return fail(ctx, GOFR_ERR_ARG, "type id %d of atom %zu outside 0..%u", type_ids[a], a,
+                        ntypes - 1);
+    t.T = nframes;
+    t.N = natoms;
+    t.ntypes = ntypes;
+    t.tric = box_kind == GOFR_BOX_TRICLINIC;
+    const size_t stride = t.tric ? 9 : 6;
+    t.h_box.assign(nframes * 9, 0.0);
+    BoxStats &s = t.bs;
+    for (int k = 0; k < 3; ++k) {
+        s.Lmin[k] = INFINITY; s.Lmax[k] = 0; s.eL[k] = 0; s.tmax[k] = 0; s.eT[k] = 0;
+    }
+    s.lh_min = INFINITY;
+    std::vector<Box32> b32(nframes);
+    for (size_t f = 0; f < nframes; ++f) {
+        const double *src = boxes + f * stride;
+        double *dst = &t.h_box[f * 9];
+        for (size_t q = 0; q < stride; ++q) {
+            if (!std::isfinite(src[q]))
+                return fail(ctx, GOFR_ERR_ARG, "non-finite box value in frame %zu", f);
+            dst[q] = src[q];
+        }
+        Box32 &bb = b32[f];
+        std::memset(&bb, 0, sizeof bb);
+        for (int k = 0; k < 3; ++k) {
+            double lh = dst[3 + k];
+            if (!(lh > 0.0))
+                return fail(ctx, GOFR_ERR_ARG,
+                            "box half edge %d of frame %zu is not positive (%g)", k, f, lh);
+            double L = lh * 2.0;
+            s.Lmin[k] = std::min(s.Lmin[k], L);
+            s.Lmax[k] = std::max(s.Lmax[k], L);
+            s.lh_min = std::min(s.lh_min, lh);
+            bb.L[k] = (float)L;
+            bb.invL[k] = (float)(1.0 / L);
+            s.eL[k] = std::max(s.eL[k], std::fabs((double)bb.L[k] - L));
+            double tl = dst[6 + k];
+            bb.tilt[k] = (float)tl;
+            s.tmax[k] = std::max(s.tmax[k], std::fabs(tl));
+            s.eT[k] = std::max(s.eT[k], std::fabs((double)bb.tilt[k] - tl));
+        }
+    }
+    free_traj(t);
+    const size_t n3 = nframes * natoms * 3;
+    CK(cudaMalloc(&t.pos64, n3 * sizeof(double)));
+    CK(cudaMalloc(&t.pos32, nframes * natoms * sizeof(float4)));
+    CK(cudaMalloc(&t.box64, nframes * 9 * sizeof(double)));
+    CK(cudaMalloc(&t.box32, nframes * sizeof(Box32)));
+    CK(cudaMalloc(&t.types, natoms * sizeof(int)));
+    CK(cudaMemcpyAsync(t.pos64, positions, n3 * sizeof(double), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(t.box64, t.h_box.data(), nframes * 9 * sizeof(double),
+                       cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(t.box32, b32.data(), nframes * sizeof(Box32), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(t.types, type_ids, natoms * sizeof(int), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_nonfinite, 0, sizeof(unsigned), ctx->stream));
+    if (launch_minmax(t.pos64, nframes * natoms, ctx->d_minmax, ctx->d_nonfinite, ctx->stream))
+        return fail(ctx, GOFR_ERR_CUDA, "min/max kernel launch failed: %s",
+                    cudaGetErrorString(cudaGetLastError()));
+    std::vector<double> mm(256 * 6);
+    unsigned nonfinite = 0;
+    CK(cudaMemcpyAsync(mm.data(), ctx->d_minmax, mm.size() * sizeof(double),
+                       cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(&nonfinite, ctx->d_nonfinite, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (nonfinite)
+        return fail(ctx, GOFR_ERR_ARG,
+                    "%u non-finite coordinates: the reference's minimum image would not "
+                    "terminate on them", nonfinite);
+    for (int k = 0; k < 3; ++k) {
+        double mn = INFINITY, mx = -INFINITY;
+        for (int b = 0; b < 256; ++b) {
+            mn = std::min(mn, mm[b * 6 + k]);
+            mx = std::max(mx, mm[b * 6 + 3 + k]);
+        }
+        t.shift[k] = 0.5 * mn + 0.5 * mx;
+        double m = std::max(std::fabs(mx - t.shift[k]), std::fabs(t.shift[k] - mn));
+        t.M[k] = m * (1.0 + std::ldexp(1.0, -40)) + 1e-300;
+    }
+    if (launch_convert(t.pos64, t.types, nframes, natoms, t.shift[0], t.shift[1], t.shift[2],
+                       t.pos32, ctx->stream))
+        return fail(ctx, GOFR_ERR_CUDA, "convert kernel launch failed: %s",
+                    cudaGetErrorString(cudaGetLastError()));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return GOFR_OK;
+}
+
+std::vector<unsigned short> channel_table(unsigned ntypes)
+{
+    // lib/include/gofrt.h:86-104
+    std::vector<unsigned short> tab(ntypes * ntypes);
+    for (unsigned a = 0; a < ntypes; ++a)
+        for (unsigned c = 0; c < ntypes; ++c) {
+            unsigned t1 = std::min(a, c), t2 = std::max(a, c);
+            tab[a * ntypes + c] =
+                (unsigned short)(ntypes * (ntypes + 1) / 2 - (t2 + 1) * (t2 + 2) / 2 + t1);
+        }
+    return tab;
+}
+
+struct Plan {
+    int kind = 1;              // 0 = FP32+recheck, 1 = FP64
+    bool wrapcheck = false;
+    bool empty = false;        // accepted window empty: nothing can be counted
+    Windows w;
+    Bound b{};
+    std::vector<double> th;
+};
+
+int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
+{
+    const int req = p.kernel;
+    if (req != GOFR_KERNEL_AUTO && req != GOFR_KERNEL_F32_RECHECK && req != GOFR_KERNEL_F64 &&
+        req != GOFR_KERNEL_CELL)
+        return fail(ctx, GOFR_ERR_ARG, "unknown kernel %d", req);
+    const bool reg = regular_bins(p.rmin, p.rmax, p.nbin);
+    if (reg) {
+        pl.th.resize(p.nbin + 1);
+        BinMap bm(p.rmin, p.rmax, p.nbin);
+        pl.empty = !thresholds(bm, pl.th.data());
+    }
+    if (req == GOFR_KERNEL_F64 || (!reg && req == GOFR_KERNEL_AUTO)) {
+        pl.kind = 1;
+        return GOFR_OK;
+    }
+    if (!reg)
+        return fail(ctx, GOFR_ERR_UNSUPPORTED,
+                    "the FP32 kernel needs finite rmin < rmax and nbin < 2^24");
+    pl.b = error_bound(t);
+    certify(pl.b, pl.th.data(), p.nbin, pl.w);
+    const double emax = std::max(pl.b.e[0], std::max(pl.b.e[1], pl.b.e[2]));
+    const double reach = std::sqrt((double)pl.w.hi_f) * (1.0 + std::ldexp(1.0, -20)) +
+                         2.0 * emax + 1e-9;
+    pl.kind = 0;
+    pl.wrapcheck = !(t.bs.lh_min > reach);
+    if (pl.wrapcheck && !(0.5 - pl.b.eta > 0.25)) {
+        if (req == GOFR_KERNEL_AUTO) { pl.kind = 1; return GOFR_OK; }
+        return fail(ctx, GOFR_ERR_UNSUPPORTED,
+                    "coordinates too far outside the box for a certified FP32 wrap");
+    }
+    return GOFR_OK;
+}
+
+int check_device_error(gofr_ctx *ctx)
+{
+    unsigned e = 0;
+    CK(cudaMemcpyAsync(&e, ctx->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (e)
+        return fail(ctx, GOFR_ERR_DEVICE, "kernel reported error word 0x%x (%s%s%s)", e,
+                    (e & ERRW_WAIT_TIMEOUT) ? "bounded wait ran out " : "",
+                    (e & ERRW_WRAP_LOOP) ? "minimum-image iteration cap " : "",
+                    (e & ERRW_QUEUE) ? "work queue overflow" : "");
+    return GOFR_OK;
+}
+
+// Queue every launch of one trajectory's calculate on the stream; counts is
+// a device pointer to data_length*(nparts>1?nparts:1) zeroed counts.
+int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const RunShape &rs,
+                const Plan &pl, unsigned long long *counts, unsigned long long *pairs_out)
+{
+    *pairs_out = 0;
+    if (pl.empty || rs.n_lags == 0 || rs.n_orig == 0 || t.N == 0) return GOFR_OK;
+    std::vector<unsigned short> tab = channel_table(t.ntypes);
+    int rc = ensure(ctx, ctx->d_chtab, ctx->cap_chtab, tab.size());
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->d_chtab, tab.data(), tab.size() * sizeof(unsigned short),
+                       cudaMemcpyHostToDevice, ctx->stream));
+    if (pl.kind == 0) {
+        rc = ensure(ctx, ctx->d_win, ctx->cap_win, pl.w.win.size());
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(ctx->d_win, pl.w.win.data(), pl.w.win.size() * sizeof(float2),
+                           cudaMemcpyHostToDevice, ctx->stream));
+    }
+    const int smem = pairs_smem_bytes(pl.kind, (int)rs.nch, (int)p.nbin, (int)t.ntypes);
+    int max_smem = 0;
+    CK(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    if (smem > max_smem)
+        return fail(ctx, GOFR_ERR_UNSUPPORTED,
+                    "histogram of %u channels x %u bins needs %d B of shared memory (max %d)",
+                    rs.nch, p.nbin, smem, max_smem);
+    PairLaunch L{};
+    L.pos32 = t.pos32;
+    L.pos64 = t.pos64;
+    L.box64 = t.box64;
+    L.box32 = t.box32;
+    L.win = ctx->d_win;
+    L.chtab = ctx->d_chtab;
+    L.err = ctx->d_err;
+    L.stats = ctx->d_stats;
+    L.N = (int)t.N;
+    L.nbin = (int)p.nbin;
+    L.nch = (int)rs.nch;
+    L.ntypes = (int)t.ntypes;
+    L.n_lags = (int)rs.n_lags;
+    L.every = (int)rs.every;
+    L.n_orig = (int)rs.n_orig;
+    L.skip = (int)rs.skip;
+    L.primo = (long long)p.primo;
+    L.tric = t.tric;
+    BinMap bm(p.rmin, p.rmax, p.nbin);
+    L.rmin = bm.rmin; L.rmax = bm.rmax; L.dr = bm.dr; L.rmin2 = bm.rmin2; L.rmax2 = bm.rmax2;
+    if (pl.kind == 0) {
+        L.hi_f = pl.w.hi_f;
+        L.lo_f = pl.w.lo_f;
+        L.rmin_f = (float)p.rmin;
+        L.inv_dr_f = (float)(1.0 / bm.dr);
+        L.wlim = (float)(0.5 - pl.b.eta);
+    }
+    const unsigned nparts = p.nparts > 1 ? p.nparts : 1;
+    const int TI = pl.kind == 0 ? 512 : 512;
+    const size_t per = t.N / nparts;
+    for (unsigned q = 0; q < nparts; ++q) {
+        size_t a0 = q * per, a1 = (q == nparts - 1) ? t.N : (q + 1) * per;
+        if (a1 <= a0) continue;
+        L.a0 = (int)a0;
+        L.a1 = (int)a1;
+        L.n_itiles = (int)((a1 - a0 + TI - 1) / TI);
+        L.n_items = (long long)L.n_lags * L.n_itiles * L.n_orig;
+        L.counts = counts + (size_t)q * rs.data_length;
+        if (launch_pairs(L, pl.kind, pl.wrapcheck, ctx->num_sms, ctx->stream, nullptr))
+            return fail(ctx, GOFR_ERR_CUDA, "pair kernel launch failed: %s",
+                        cudaGetErrorString(cudaGetLastError()));
+    }
+    *pairs_out = (unsigned long long)rs.n_lags * rs.n_orig * t.N * t.N;
+    return GOFR_OK;
+}
+
+int run_common(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_dev,
+               unsigned long long *counts_host)
+{
+    if (!ctx) return GOFR_ERR_ARG;
+    if (!p) return fail(ctx, GOFR_ERR_ARG, "null params");
+    if (ctx->trajs.size() != 1) return fail(ctx, GOFR_ERR_STATE, "no frames uploaded");
+    const TrajDev &t = ctx->trajs[0];
+    RunShape rs;
+    int rc = shape_of(ctx, t, *p, rs);
+    if (rc) return rc;
+    Plan pl;
+    rc = make_plan(ctx, t, *p, pl);
+    if (rc) return rc;
+    const unsigned nparts = p->nparts > 1 ? p->nparts : 1;
+    const size_t n_out = rs.data_length * nparts;
+    unsigned long long *out = counts_dev;
+    if (!out) {
+        rc = ensure(ctx, ctx->d_counts, ctx->cap_counts, n_out);
+        if (rc) return rc;
+        out = ctx->d_counts;
+    }
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_stats, 0, ST_COUNT * sizeof(unsigned long long), ctx->stream));
+    if (n_out) CK(cudaMemsetAsync(out, 0, n_out * sizeof(unsigned long long), ctx->stream));
+    CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+    unsigned long long pairs = 0;
+    rc = enqueue_run(ctx, t, *p, rs, pl, out, &pairs);
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+    if (counts_host && n_out)
+        CK(cudaMemcpyAsync(counts_host, out, n_out * sizeof(unsigned long long),
+                           cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+    std::memset(&ctx->stats, 0, sizeof ctx->stats);
+    ctx->stats.pairs = pairs;
+    ctx->stats.evaluated = pairs;
+    ctx->stats.kernel_used = pl.kind == 0 ? GOFR_KERNEL_F32_RECHECK : GOFR_KERNEL_F64;
+    ctx->stats.wrap_checked = pl.wrapcheck ? 1 : 0;
+    ctx->stats.err_bound_d2 = pl.kind == 0 ? pl.w.E_rmax : 0.0;
+    if (counts_host) return gofr_sync(ctx);
+    return GOFR_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// exported entry points
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int gofr_ctx_create(gofr_ctx **out, int device)
+{
+    if (!out) return GOFR_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GOFR_ERR_CUDA;
+    if (device < 0 || device >= ndev) return GOFR_ERR_ARG;
+    gofr_ctx *ctx = new (std::nothrow) gofr_ctx();
+    if (!ctx) return GOFR_ERR_NOMEM;
+    ctx->device = device;
+    DevGuard g(device);
+    int rc = GOFR_OK;
+    do {
+        if (cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device) !=
+                cudaSuccess ||
+            cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            rc = GOFR_ERR_CUDA;
+            break;
+        }
+        bool ok = true;
+        for (auto &e : ctx->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+        ok = ok && cudaMalloc(&ctx->d_err, sizeof(unsigned)) == cudaSuccess;
+        ok = ok && cudaMalloc(&ctx->d_stats, ST_COUNT * sizeof(unsigned long long)) == cudaSuccess;
+        ok = ok && cudaMalloc(&ctx->d_minmax, 256 * 6 * sizeof(double)) == cudaSuccess;
+        ok = ok && cudaMalloc(&ctx->d_nonfinite, sizeof(unsigned)) == cudaSuccess;
+        if (!ok) rc = GOFR_ERR_CUDA;
+    } while (0);
+    if (rc) {
+        gofr_ctx_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return GOFR_OK;
+}
+
+void gofr_ctx_destroy(gofr_ctx *ctx)
+{
+    if (!ctx) return;
+    {
+        DevGuard g(ctx->device);
+        if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+        for (auto &t : ctx->trajs) free_traj(t);
+        cudaFree(ctx->d_counts);
+        cudaFree(ctx->d_win);
+        cudaFree(ctx->d_chtab);
+        cudaFree(ctx->d_err);
+        cudaFree(ctx->d_stats);
+        cudaFree(ctx->d_minmax);
+        cudaFree(ctx->d_nonfinite);
+        for (auto &e : ctx->ev)
+            if (e) cudaEventDestroy(e);
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    }
+    delete ctx;
+}
+
+const char *gofr_last_error(const gofr_ctx *ctx)
+{
+    if (!ctx) return "no context (gofr_ctx_create failed or was not called)";
+    return ctx->err.c_str();
+}
+
+int gofr_set_frames(gofr_ctx *ctx, const double *positions, const double *boxes, int box_kind,
+                    const int *type_ids, unsigned ntypes, size_t natoms, size_t nframes)
+{
+    if (!ctx) return GOFR_ERR_ARG;
+    DevGuard g(ctx->device);
+    for (auto &t : ctx->trajs) free_traj(t);
+    ctx->trajs.clear();
+    ctx->trajs.emplace_back();
+    int rc = upload_traj(ctx, ctx->trajs[0], positions, boxes, box_kind, type_ids, ntypes, natoms,
+                         nframes);
+    if (rc) {
+        free_traj(ctx->trajs[0]);
+        ctx->trajs.clear();
+    }
+    return rc;
+}
+
+int gofr_output_size(const gofr_ctx *ctx_c, const gofr_params *p, size_t *n_counts)
+{
+    gofr_ctx *ctx = const_cast<gofr_ctx *>(ctx_c);
+    if (!ctx || !p || !n_counts) return GOFR_ERR_ARG;
+    if (ctx->trajs.size() != 1) return fail(ctx, GOFR_ERR_STATE, "no frames uploaded");
+    const TrajDev &t = ctx->trajs[0];
+    unsigned leff = (p->ntimesteps < p->tmax || p->tmax == 0) ? p->ntimesteps : p->tmax;
+    size_t n = (size_t)leff * t.ntypes * (t.ntypes + 1) * p->nbin;
+    *n_counts = n * (p->nparts > 1 ? p->nparts : 1);
+    return GOFR_OK;
+}
+
+int gofr_run(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_host)
+{
+    if (!ctx) return GOFR_ERR_ARG;
+    if (!counts_host) return fail(ctx, GOFR_ERR_ARG, "null output buffer");
+    DevGuard g(ctx->device);
+    return run_common(ctx, p, nullptr, counts_host);
+}
+
+int gofr_run_device(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_device)
+{
+    if (!ctx) return GOFR_ERR_ARG;
+    if (!counts_device) return fail(ctx, GOFR_ERR_ARG, "null output buffer");
+    DevGuard g(ctx->device);
+    return run_common(ctx, p, counts_device, nullptr);
+}
+
+int gofr_sync(gofr_ctx *ctx)
+{
+    if (!ctx) return GOFR_ERR_ARG;
+    DevGuard g(ctx->device);
+    CK(cudaStreamSynchronize(ctx->stream));
+    int rc = check_device_error(ctx);
+    if (rc) return rc;
+    unsigned long long st[ST_COUNT];
+    CK(cudaMemcpy(st, ctx->d_stats, sizeof st, cudaMemcpyDeviceToHost));
+    ctx->stats.candidates = st[ST_CANDIDATES];
+    ctx->stats.rechecks = st[ST_RECHECKS];
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]) == cudaSuccess) ctx->stats.kernel_ms = ms;
+    if (cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[3]) == cudaSuccess) ctx->stats.total_ms = ms;
+    return GOFR_OK;
+}
+
+int gofr_get_stats(const gofr_ctx *ctx, gofr_stats *out)
+{
+    if (!ctx || !out) return GOFR_ERR_ARG;
+    *out = ctx->stats;
+    return GOFR_OK;
+}
+
+int gofr_bin_thresholds(double rmin, double rmax, unsigned nbin, double *th)
+{
+    if (!th) return GOFR_ERR_ARG;
+    if (!regular_bins(rmin, rmax, nbin)) return GOFR_ERR_UNSUPPORTED;
+    BinMap bm(rmin, rmax, nbin);
+    thresholds(bm, th);
+    return GOFR_OK;
+}
+
+// incr added k times in sequence (lib/src/gofrt.cpp:118), in O(number of
+// binades): within one binade of the running sum the rounded step is the
+// same for every addition until the sum reaches the binade's upper end, so
+// those additions are taken in one exact multiplication.  Exact ties (the
+// step is half an ulp) are taken one at a time; they end in a fixed point.
+static double repeated_sum(unsigned long long k, double incr)
+{
+    double s = 0.0;
+    while (k > 0) {
+        double n1 = s + incr;
+        if (n1 == s) return s;  // the sum no longer moves
+        if (s == 0.0 || !std::isfinite(n1)) { s = n1; --k; continue; }
+        int e;
+        std::frexp(s, &e);                     // s in [2^(e-1), 2^e)
+        double top = std::ldexp(1.0, e);       // upper end of the binade
+        double u = std::ldexp(1.0, e - 53);    // ulp in the binade
+        double r = incr / u;                   // exact (power-of-two scaling)
+        double fr = r - std::floor(r);
+        if (fr == 0.5 || !(top - s > incr)) { s = n1; --k; continue; }
+        double delta = n1 - s;                 // exact: same binade, Sterbenz
+        // additions from s + j*delta stay exact steps while s + j*delta + incr <= top
+        double jm = std::floor((top - s - incr) / delta) - 2.0;
+        if (jm < 1.0) { s = n1; --k; continue; }
+        unsigned long long j = jm >= (double)k ? k : (unsigned long long)jm;
+        s = s + (double)j * delta;
+        k -= j;
+    }
+    return s;
+}
+
+int gofr_counts_to_buffer(const unsigned long long *counts, size_t n, unsigned nparts,
+                          unsigned ntimesteps, unsigned skip, double *out)
+{
+    if ((!counts || !out) && n) return GOFR_ERR_ARG;
+    if (skip == 0) skip = 1;
+    const double incr = (ntimesteps / skip > 0) ? 1.0 / (int)(ntimesteps / skip) : 1.0;
+    if (nparts <= 1) {
+        for (size_t i = 0; i < n; ++i) out[i] = (double)counts[i] * incr;
+        return GOFR_OK;
+    }
+    for (size_t i = 0; i < n; ++i) {
+        double acc = repeated_sum(counts[i], incr);
+        for (unsigned q = 1; q < nparts; ++q) acc += repeated_sum(counts[(size_t)q * n + i], incr);
+        out[i] = acc;
+    }
+    return GOFR_OK;
+}
+
+// ---- batch: v1 runs the trajectories one launch each (see gofr_batch_run) --
+int gofr_batch_set(gofr_ctx *ctx, const gofr_traj_desc *trajs, unsigned ntraj)
+{
+    if (!ctx) return GOFR_ERR_ARG;
+    if (!trajs || ntraj == 0) return fail(ctx, GOFR_ERR_ARG, "empty batch");
+    DevGuard g(ctx->device);
+    for (auto &t : ctx->trajs) free_traj(t);
+    ctx->trajs.clear();
+    ctx->trajs.resize(ntraj);
+    size_t off = 0;
+    for (unsigned k = 0; k < ntraj; ++k) {
+        const gofr_traj_desc &d = trajs[k];
+        int rc = upload_traj(ctx, ctx->trajs[k], d.positions, d.boxes, d.box_kind, d.type_ids,
+                             d.ntypes, d.natoms, d.nframes);
+        if (rc == GOFR_OK) {
+            ctx->trajs[k].params = d.params;
+            RunShape rs;
+            rc = shape_of(ctx, ctx->trajs[k], d.params, rs);
+            ctx->trajs[k].out_offset = off;
+            ctx->trajs[k].out_count = rs.data_length;
+            off += rs.data_length;
+        }
+        if (rc) {
+            std::string m = ctx->err;
+            for (auto &t : ctx->trajs) free_traj(t);
+            ctx->trajs.clear();
+            return fail(ctx, rc, "trajectory %u: %s", k, m.c_str());
+        }
+    }
+    ctx->batch_total = off;
+    return GOFR_OK;
+}
+
+int gofr_batch_output_layout(const gofr_ctx *ctx, unsigned k, size_t *offset, size_t *n_counts)
+{
+    if (!ctx || !offset || !n_counts || k >= ctx->trajs.size()) return GOFR_ERR_ARG;
+    *offset = ctx->trajs[k].out_offset;
+    *n_counts = ctx->trajs[k].out_count;
+    return GOFR_OK;
+}
+
+int gofr_batch_run(gofr_ctx *ctx, int use_graph, unsigned long long *counts_host)
+{
+    (void)use_graph;
+    if (!ctx) return GOFR_ERR_ARG;
+    if (!counts_host) return fail(ctx, GOFR_ERR_ARG, "null output buffer");
+    if (ctx->trajs.empty()) return fail(ctx, GOFR_ERR_STATE, "no batch uploaded");
+    DevGuard g(ctx->device);
+    int rc = ensure(ctx, ctx->d_counts, ctx->cap_counts, ctx->batch_total);
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_stats, 0, ST_COUNT * sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_counts, 0, std::max<size_t>(ctx->batch_total, 1) * 8, ctx->stream));
+    CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+    unsigned long long pairs_total = 0;
+    for (auto &t : ctx->trajs) {
+        gofr_params p = t.params;
+        p.kernel = GOFR_KERNEL_AUTO;
+        p.nparts = 1;
+        RunShape rs;
+        rc = shape_of(ctx, t, p, rs);
+        if (rc) return rc;
+        Plan pl;
+        rc = make_plan(ctx, t, p, pl);
+        if (rc) return rc;
+        unsigned long long pairs = 0;
+        rc = enqueue_run(ctx, t, p, rs, pl, ctx->d_counts + t.out_offset, &pairs);
+        if (rc) return rc;
+        pairs_total += pairs;
+    }
+    CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+    CK(cudaMemcpyAsync(counts_host, ctx->d_counts, ctx->batch_total * 8, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+    std::memset(&ctx->stats, 0, sizeof ctx->stats);
+    ctx->stats.pairs = pairs_total;
+    ctx->stats.evaluated = pairs_total;
+    ctx->stats.kernel_used = GOFR_KERNEL_AUTO;
+    return gofr_sync(ctx);
+}
+
+}  // extern "C"

@@ -1,0 +1,67 @@
+// Internal declarations shared by the host side (gofr_capi.cu) and the
+// kernels (gofr_kernels.cu).  Not part of the C ABI.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gofr {
+
+// Bits of the device error word.
+enum : unsigned {
+    ERRW_WAIT_TIMEOUT = 1u,   // a bounded mbarrier wait ran out
+    ERRW_WRAP_LOOP = 2u,      // the FP64 iterative minimum image exceeded its iteration cap
+    ERRW_QUEUE = 4u           // a work queue overflowed its capacity
+};
+
+// Stats slots (unsigned long long) on the device.
+enum : int { ST_CANDIDATES = 0, ST_RECHECKS = 1, ST_EVALUATED = 2, ST_COUNT = 4 };
+
+// Per-frame FP32 box parameters for the FP32 kernels (12 floats, 48 B).
+//   L[3]    full edges 2*lh rounded to float
+//   invL[3] 1/(2*lh) rounded to float
+//   tilt[3] {xy, xz, yz} rounded to float
+struct Box32 {
+    float L[3];
+    float invL[3];
+    float tilt[3];
+    float pad[3];
+};
+
+// One launch of an all-pairs kernel over (lag, i-tile, origin) items.
+struct PairLaunch {
+    const float4 *pos32;      // [T][N] {x-cx, y-cy, z-cz, type id bits}
+    const double *pos64;      // [T][N][3] internal FP64 positions (reference values)
+    const double *box64;      // [T][9] internal boxes (tilts zero when orthorhombic)
+    const Box32 *box32;       // [T]
+    const float2 *win;        // [nbin] certified FP32 window {lo, hi} of each bin
+    const unsigned short *chtab; // [ntypes*ntypes] channel of a type pair
+    unsigned long long *counts;  // [leff][nch][nbin]
+    unsigned *err;
+    unsigned long long *stats;
+    int N, nbin, nch, ntypes;
+    int a0, a1;               // first-atom range [a0, a1) (one reference thread partition)
+    int n_lags, every;        // lags t = l*every, l < n_lags
+    int n_orig, skip;         // origins primo + k*skip, k < n_orig
+    long long primo;
+    int n_itiles;             // tiles of the first-atom range
+    long long n_items;        // n_lags * n_itiles * n_orig
+    float hi_f, lo_f;         // certain reject above hi_f / below lo_f
+    float rmin_f, inv_dr_f;   // bin guess
+    float wlim;               // wrap check: |frac| > wlim flags a recheck
+    double rmin, rmax, dr, rmin2, rmax2;  // reference binning constants
+    int tric;
+};
+
+// Launch configuration helpers implemented in gofr_kernels.cu.
+int launch_minmax(const double *pos64, size_t n3, double *d_out6, unsigned *d_nonfinite,
+                  cudaStream_t s);
+int launch_convert(const double *pos64, const int *types, size_t T, size_t N, double cx,
+                   double cy, double cz, float4 *pos32, cudaStream_t s);
+// kind: 0 = FP32+recheck, 1 = FP64.  wrapcheck only for kind 0.
+int launch_pairs(const PairLaunch &P, int kind, bool wrapcheck, int num_sms, cudaStream_t s,
+                 size_t *smem_bytes_out);
+int pairs_smem_bytes(int kind, int nch, int nbin, int ntypes);
+int launch_zero_u64(unsigned long long *p, size_t n, cudaStream_t s);
+
+}  // namespace gofr

@@ -1,0 +1,273 @@
+"""ctypes binding of the C ABI in include/gofr_gb300.h.
+
+This is the thinnest possible host front: it loads the in-tree
+libgofr_gb300.so (built by analisi_gb300.build) and fails loudly when it is
+missing -- there is no CPU path behind it.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgofr_gb300.so")
+
+GOFR_OK = 0
+STATUS = {
+    -1: "GOFR_ERR_ARG", -2: "GOFR_ERR_RANGE", -3: "GOFR_ERR_CUDA", -4: "GOFR_ERR_NOMEM",
+    -5: "GOFR_ERR_STATE", -6: "GOFR_ERR_DEVICE", -7: "GOFR_ERR_UNSUPPORTED",
+}
+BOX_ORTHO, BOX_TRICLINIC = 0, 1
+KERNELS = {"auto": 0, "f32": 1, "f64": 2, "cell": 3}
+
+# every symbol the header declares (checked by the CPU tests)
+EXPORTED = [
+    "gofr_ctx_create", "gofr_ctx_destroy", "gofr_last_error", "gofr_set_frames",
+    "gofr_output_size", "gofr_run", "gofr_run_device", "gofr_sync", "gofr_get_stats",
+    "gofr_counts_to_buffer", "gofr_bin_thresholds", "gofr_batch_set",
+    "gofr_batch_output_layout", "gofr_batch_run",
+]
+
+
+class GofrError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class TrajectoryTooShort(GofrError):
+    pass
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("rmin", ctypes.c_double), ("rmax", ctypes.c_double), ("nbin", ctypes.c_uint),
+                ("tmax", ctypes.c_uint), ("skip", ctypes.c_uint), ("every", ctypes.c_uint),
+                ("ntimesteps", ctypes.c_uint), ("primo", ctypes.c_ulonglong),
+                ("kernel", ctypes.c_int), ("nparts", ctypes.c_uint)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("pairs", ctypes.c_ulonglong), ("evaluated", ctypes.c_ulonglong),
+                ("candidates", ctypes.c_ulonglong), ("rechecks", ctypes.c_ulonglong),
+                ("kernel_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
+                ("kernel_used", ctypes.c_int), ("wrap_checked", ctypes.c_int),
+                ("err_bound_d2", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class TrajDesc(ctypes.Structure):
+    _fields_ = [("positions", ctypes.POINTER(ctypes.c_double)),
+                ("boxes", ctypes.POINTER(ctypes.c_double)), ("box_kind", ctypes.c_int),
+                ("type_ids", ctypes.POINTER(ctypes.c_int)), ("ntypes", ctypes.c_uint),
+                ("natoms", ctypes.c_size_t), ("nframes", ctypes.c_size_t),
+                ("params", Params)]
+
+
+_lib = None
+
+
+def load_library(path=None):
+    """Load libgofr_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise ImportError(f"{p} not built: run `python -m analisi_gb300.build` "
+                          "(the GPU engine has no CPU fallback)")
+    L = ctypes.CDLL(p)
+    vp = ctypes.c_void_p
+    dp = ctypes.POINTER(ctypes.c_double)
+    ip = ctypes.POINTER(ctypes.c_int)
+    up = ctypes.POINTER(ctypes.c_ulonglong)
+    L.gofr_ctx_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int]
+    L.gofr_ctx_destroy.argtypes = [vp]
+    L.gofr_ctx_destroy.restype = None
+    L.gofr_last_error.argtypes = [vp]
+    L.gofr_last_error.restype = ctypes.c_char_p
+    L.gofr_set_frames.argtypes = [vp, dp, dp, ctypes.c_int, ip, ctypes.c_uint, ctypes.c_size_t,
+                                  ctypes.c_size_t]
+    L.gofr_output_size.argtypes = [vp, ctypes.POINTER(Params), ctypes.POINTER(ctypes.c_size_t)]
+    L.gofr_run.argtypes = [vp, ctypes.POINTER(Params), up]
+    L.gofr_run_device.argtypes = [vp, ctypes.POINTER(Params), vp]
+    L.gofr_sync.argtypes = [vp]
+    L.gofr_get_stats.argtypes = [vp, ctypes.POINTER(Stats)]
+    L.gofr_counts_to_buffer.argtypes = [up, ctypes.c_size_t, ctypes.c_uint, ctypes.c_uint,
+                                        ctypes.c_uint, dp]
+    L.gofr_bin_thresholds.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_uint, dp]
+    L.gofr_batch_set.argtypes = [vp, ctypes.POINTER(TrajDesc), ctypes.c_uint]
+    L.gofr_batch_output_layout.argtypes = [vp, ctypes.c_uint, ctypes.POINTER(ctypes.c_size_t),
+                                           ctypes.POINTER(ctypes.c_size_t)]
+    L.gofr_batch_run.argtypes = [vp, ctypes.c_int, up]
+    for name in ("gofr_ctx_create", "gofr_set_frames", "gofr_output_size", "gofr_run",
+                 "gofr_run_device", "gofr_sync", "gofr_get_stats", "gofr_counts_to_buffer",
+                 "gofr_bin_thresholds", "gofr_batch_set", "gofr_batch_output_layout",
+                 "gofr_batch_run"):
+        getattr(L, name).restype = ctypes.c_int
+    if path is None:
+        _lib = L
+    return L
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def make_params(rmin, rmax, nbin, tmax=0, skip=1, every=1, ntimesteps=0, primo=0,
+                kernel="auto", nparts=1):
+    return Params(float(rmin), float(rmax), int(nbin), int(tmax), int(skip), int(every),
+                  int(ntimesteps), int(primo), KERNELS[kernel] if isinstance(kernel, str)
+                  else int(kernel), int(nparts))
+
+
+def bin_thresholds(rmin, rmax, nbin):
+    """Exact d2 thresholds th[0..nbin] of the reference's bin map (host code)."""
+    L = load_library()
+    th = np.zeros(int(nbin) + 1)
+    rc = L.gofr_bin_thresholds(float(rmin), float(rmax), int(nbin), _dp(th))
+    if rc != GOFR_OK:
+        raise GofrError(rc, "bin map not monotone for these parameters")
+    return th
+
+
+def counts_to_buffer(counts, ntimesteps, skip, nparts=1):
+    """The reference's double result buffer from counts (host code).  With
+    nparts > 1, counts is [nparts][...] and the result is the exact thread fold."""
+    L = load_library()
+    c = np.ascontiguousarray(counts, dtype=np.uint64)
+    shape = c.shape[1:] if nparts > 1 else c.shape
+    n = int(np.prod(shape))
+    out = np.zeros(shape, dtype=np.float64)
+    rc = L.gofr_counts_to_buffer(c.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)), n,
+                                 int(nparts), int(ntimesteps), int(skip), _dp(out))
+    if rc != GOFR_OK:
+        raise GofrError(rc, "counts_to_buffer failed")
+    return out
+
+
+class Engine:
+    """One gofr_ctx: resident frames on one GPU and runs on them."""
+
+    def __init__(self, device=0):
+        self.L = load_library()
+        self._ctx = ctypes.c_void_p()
+        rc = self.L.gofr_ctx_create(ctypes.byref(self._ctx), int(device))
+        if rc != GOFR_OK:
+            raise GofrError(rc, self.L.gofr_last_error(None).decode())
+        self.ntypes = 0
+        self.natoms = 0
+        self.nframes = 0
+        self._batch = None
+
+    def close(self):
+        if self._ctx:
+            self.L.gofr_ctx_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != GOFR_OK:
+            msg = self.L.gofr_last_error(self._ctx).decode()
+            cls = TrajectoryTooShort if rc == -2 else GofrError
+            raise cls(rc, msg)
+
+    def set_frames(self, positions, boxes, type_ids, ntypes=None, triclinic=None):
+        """positions [T][N][3] f64 internal, boxes [T][6|9] f64 internal, type_ids [N]."""
+        pos = np.ascontiguousarray(positions, dtype=np.float64)
+        bx = np.ascontiguousarray(boxes, dtype=np.float64)
+        ty = np.ascontiguousarray(type_ids, dtype=np.int32)
+        if triclinic is None:
+            triclinic = bx.shape[1] == 9
+        if ntypes is None:
+            ntypes = int(ty.max()) + 1 if ty.size else 1
+        T, N = pos.shape[0], pos.shape[1]
+        self._check(self.L.gofr_set_frames(
+            self._ctx, _dp(pos), _dp(bx), BOX_TRICLINIC if triclinic else BOX_ORTHO,
+            ty.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), int(ntypes), N, T))
+        self.ntypes, self.natoms, self.nframes = int(ntypes), N, T
+
+    def output_size(self, params):
+        n = ctypes.c_size_t()
+        self._check(self.L.gofr_output_size(self._ctx, ctypes.byref(params), ctypes.byref(n)))
+        return n.value
+
+    def run(self, rmin, rmax, nbin, tmax=0, skip=1, every=1, ntimesteps=0, primo=0,
+            kernel="auto", nparts=1, out=None):
+        """Exact counts [leff][nch][nbin] (or [nparts][...]) as uint64."""
+        p = make_params(rmin, rmax, nbin, tmax, skip, every, ntimesteps, primo, kernel, nparts)
+        n = self.output_size(p)
+        leff = ntimesteps if (ntimesteps < tmax or tmax == 0) else tmax
+        nch = self.ntypes * (self.ntypes + 1)
+        shape = (leff, nch, int(nbin)) if nparts <= 1 else (int(nparts), leff, nch, int(nbin))
+        if out is None:
+            out = np.zeros(max(n, 1), dtype=np.uint64)
+        self._check(self.L.gofr_run(self._ctx, ctypes.byref(p),
+                                    out.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong))))
+        return out[:n].reshape(shape)
+
+    def run_params(self, p, out):
+        """gofr_run with prepared Params and a preallocated uint64 output (hot loop form)."""
+        self._check(self.L.gofr_run(self._ctx, ctypes.byref(p),
+                                    out.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong))))
+        return out
+
+    def run_device(self, p, dev_ptr):
+        self._check(self.L.gofr_run_device(self._ctx, ctypes.byref(p), ctypes.c_void_p(dev_ptr)))
+
+    def sync(self):
+        self._check(self.L.gofr_sync(self._ctx))
+
+    def stats(self):
+        s = Stats()
+        self._check(self.L.gofr_get_stats(self._ctx, ctypes.byref(s)))
+        return s.as_dict()
+
+    # ---- batches ---------------------------------------------------------
+    def batch_set(self, trajs):
+        """trajs: list of dicts with positions, boxes, type_ids, ntypes, params (Params)."""
+        keep = []
+        descs = (TrajDesc * len(trajs))()
+        for k, t in enumerate(trajs):
+            pos = np.ascontiguousarray(t["positions"], dtype=np.float64)
+            bx = np.ascontiguousarray(t["boxes"], dtype=np.float64)
+            ty = np.ascontiguousarray(t["type_ids"], dtype=np.int32)
+            keep += [pos, bx, ty]
+            descs[k] = TrajDesc(_dp(pos), _dp(bx),
+                                BOX_TRICLINIC if bx.shape[1] == 9 else BOX_ORTHO,
+                                ty.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                int(t["ntypes"]), pos.shape[1], pos.shape[0], t["params"])
+        self._check(self.L.gofr_batch_set(self._ctx, descs, len(trajs)))
+        layout = []
+        total = 0
+        for k, t in enumerate(trajs):
+            off, n = ctypes.c_size_t(), ctypes.c_size_t()
+            self._check(self.L.gofr_batch_output_layout(self._ctx, k, ctypes.byref(off),
+                                                        ctypes.byref(n)))
+            p = t["params"]
+            leff = p.ntimesteps if (p.ntimesteps < p.tmax or p.tmax == 0) else p.tmax
+            nch = int(t["ntypes"]) * (int(t["ntypes"]) + 1)
+            layout.append((off.value, n.value, (leff, nch, p.nbin)))
+            total = max(total, off.value + n.value)
+        self._batch = (layout, total)
+        return layout
+
+    def batch_run(self, use_graph=True, out=None):
+        layout, total = self._batch
+        if out is None:
+            out = np.zeros(max(total, 1), dtype=np.uint64)
+        self._check(self.L.gofr_batch_run(self._ctx, int(bool(use_graph)),
+                                          out.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong))))
+        return [out[o:o + n].reshape(s) for (o, n, s) in layout]

@@ -1,0 +1,186 @@
+/*
+ * gofr_gb300.h -- C ABI of the GB300 (sm_103a) van Hove g(r,t) engine.
+ *
+ * This is the drop-in boundary for analisi's Gofrt calculation
+ * (lib/include/gofrt.h, lib/src/gofrt.cpp).  The C++ Gofrt class of
+ * analisi_gb300/host/gofrt.h and its Python binding call only these entry
+ * points; any other language binds them with a plain FFI (ctypes, cgo, JNI).
+ *
+ * Conventions
+ *   - Every entry point returns an int status: GOFR_OK (0) or a negative
+ *     gofr_status.  No C++ exception ever crosses this boundary.
+ *   - gofr_last_error(ctx) returns the message of the last failure on ctx.
+ *   - One context owns one CUDA stream and the device-resident frames of one
+ *     trajectory.  A context is thread-compatible, not thread-safe, like one
+ *     reference Gofrt object (nothing in the reference is re-entrant).
+ *   - Positions and boxes are the reference's INTERNAL buffers, i.e. what
+ *     Trajectory_numpy / Trajectory hold after their preprocessing
+ *     (lib/src/trajectory_numpy.cpp:7-199): positions [nframes][natoms][3]
+ *     FP64, boxes [nframes][6 or 9] FP64 in the internal format
+ *     {xlo, ylo, zlo, lx/2, ly/2, lz/2, xy, xz, yz}
+ *     (lib/include/basetrajectory.h:21-43,94-105), dense type ids 0..ntypes-1
+ *     (lib/src/basetrajectory.cpp:52-89).
+ *   - Histogram counts are exact unsigned 64-bit integers laid out as the
+ *     reference's result buffer: [leff][ntypes*(ntypes+1)][nbin]
+ *     (lib/src/gofrt.cpp:65-71); lags not on the `every` grid stay 0.  The
+ *     reference's double value of a bin is count * incr
+ *     (incr = 1/int(ntimesteps/skip), lib/src/gofrt.cpp:91-92), or its exact
+ *     thread-fold when per-partition counts are requested (nparts > 1).
+ */
+#ifndef GOFR_GB300_H
+#define GOFR_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gofr_ctx gofr_ctx;
+
+enum gofr_status {
+    GOFR_OK = 0,
+    GOFR_ERR_ARG = -1,      /* invalid argument (shape, null pointer, value) */
+    GOFR_ERR_RANGE = -2,    /* leff+ntimesteps+primo > nframes+1 (reference: runtime_error, gofrt.cpp:81-83) */
+    GOFR_ERR_CUDA = -3,     /* a CUDA runtime call failed */
+    GOFR_ERR_NOMEM = -4,    /* device or host allocation failed */
+    GOFR_ERR_STATE = -5,    /* no frames uploaded yet */
+    GOFR_ERR_DEVICE = -6,   /* a kernel reported an error word (bounded wait ran out, wrap loop cap) */
+    GOFR_ERR_UNSUPPORTED = -7
+};
+
+enum gofr_box_kind {
+    GOFR_BOX_ORTHO = 0,     /* box stride 6 (lib/include/basetrajectory.h:38-43) */
+    GOFR_BOX_TRICLINIC = 1  /* box stride 9 (lib/include/basetrajectory.h:32-37) */
+};
+
+enum gofr_kernel {
+    GOFR_KERNEL_AUTO = 0,        /* FP32 bulk + FP64 edge recheck when certifiable, else FP64 */
+    GOFR_KERNEL_F32_RECHECK = 1, /* force the FP32 + recheck kernel (error if not certifiable) */
+    GOFR_KERNEL_F64 = 2,         /* plain FP64 kernel: reference arithmetic for every pair */
+    GOFR_KERNEL_CELL = 3         /* cell-list FP32 + recheck kernel (large N) */
+};
+
+/* Parameters of one Gofrt::calculate (lib/include/gofrt.h:37-45 constructor
+ * arguments, reset(n) and calculate(primo)). */
+typedef struct gofr_params {
+    double rmin;            /* Gofrt(..., rmin, ...) */
+    double rmax;            /* Gofrt(..., rmax, ...) */
+    unsigned nbin;          /* Gofrt(..., nbin, ...) */
+    unsigned tmax;          /* Gofrt(..., tmax): maximum lag; 0 = ntimesteps */
+    unsigned skip;          /* origin stride; 0 means 1 (calculatemultithread.h:44) */
+    unsigned every;         /* lag stride; 0 means 1 (calculatemultithread.h:45) */
+    unsigned ntimesteps;    /* reset(ntimesteps) */
+    unsigned long long primo; /* calculate(primo) */
+    int kernel;             /* enum gofr_kernel */
+    unsigned nparts;        /* >1: counts per reference thread partition
+                               (calculatemultithread.h:50-78), output is
+                               [nparts][leff][nch][nbin]; 0/1: totals */
+} gofr_params;
+
+/* Statistics of the last run on a context. */
+typedef struct gofr_stats {
+    unsigned long long pairs;        /* ordered pairs of the reference loop (N^2 per lag/origin) */
+    unsigned long long evaluated;    /* pairs whose distance was computed on the GPU */
+    unsigned long long candidates;   /* FP32 pairs inside the accept window (+ its error bound) */
+    unsigned long long rechecks;     /* pairs recomputed in FP64 */
+    double kernel_ms;                /* device time of the pair kernel(s), CUDA events */
+    double total_ms;                 /* device time of the whole run incl. copies */
+    int kernel_used;                 /* enum gofr_kernel actually launched */
+    int wrap_checked;                /* 1 if the per-pair wrap-decision check was on */
+    double err_bound_d2;             /* FP32 error bound on d2 at rmax (A^2) */
+} gofr_stats;
+
+/* Creates a context on CUDA device `device` (replaces the construction of a
+ * Gofrt object, lib/src/gofrt.cpp:22-31, whose work is per-call here). */
+int gofr_ctx_create(gofr_ctx **out, int device);
+
+/* Releases the context, its stream and all its device memory. */
+void gofr_ctx_destroy(gofr_ctx *ctx);
+
+/* Message of the last error on ctx ("" if none); ctx may be NULL for
+ * failures of gofr_ctx_create. */
+const char *gofr_last_error(const gofr_ctx *ctx);
+
+/* Copies one trajectory into HBM, where it stays resident for every later
+ * run (replaces the per-pair host reads of Trajectory_numpy::positions/box,
+ * lib/include/trajectory_numpy.h:19-23, and BaseTrajectory::get_type,
+ * lib/include/basetrajectory.h:71-77).  The host buffers may be freed after
+ * the call returns.  Pinned host memory makes the copy asynchronous-capable
+ * and faster; pageable memory works too. */
+int gofr_set_frames(gofr_ctx *ctx, const double *positions, const double *boxes,
+                    int box_kind, const int *type_ids, unsigned ntypes,
+                    size_t natoms, size_t nframes);
+
+/* Number of unsigned 64-bit counts gofr_run writes for these parameters
+ * (leff * ntypes*(ntypes+1) * nbin, times nparts when nparts > 1). */
+int gofr_output_size(const gofr_ctx *ctx, const gofr_params *p, size_t *n_counts);
+
+/* One Gofrt::calculate(primo) on the resident frames (replaces
+ * CalculateMultiThread::calculate, lib/include/calculatemultithread.h:106-162,
+ * Gofrt::calc_init/calc_single_th/calc_end, lib/src/gofrt.cpp:74-155).
+ * Writes exact counts into the caller's host buffer and returns when done. */
+int gofr_run(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_host);
+
+/* Same as gofr_run, asynchronous: counts go to a caller-owned device buffer
+ * of gofr_output_size elements, work is queued on the context's stream.
+ * Call gofr_sync before reading the counts. */
+int gofr_run_device(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_device);
+
+/* Waits for the context's stream and reports device-side errors. */
+int gofr_sync(gofr_ctx *ctx);
+
+/* Statistics of the last completed run. */
+int gofr_get_stats(const gofr_ctx *ctx, gofr_stats *out);
+
+/* Converts counts to the reference's double result buffer: out[i] =
+ * counts[i] * incr, with incr = 1/int(ntimesteps/skip) (gofrt.cpp:91-92).
+ * When nparts > 1 the counts are per partition and the result is the
+ * reference's exact thread fold (gofrt.cpp:118,128-132): each partition's
+ * value is incr added count times in sequence, partitions summed in order.
+ * n is the number of doubles (leff*nch*nbin). */
+int gofr_counts_to_buffer(const unsigned long long *counts, size_t n, unsigned nparts,
+                          unsigned ntimesteps, unsigned skip, double *out);
+
+/* Exact squared-distance bin thresholds used by the kernels: th[b] is the
+ * smallest double d2 whose reference bin is >= b inside the accepted window,
+ * th[0] the smallest accepted d2, th[nbin] the successor of the largest
+ * accepted d2 (lib/src/gofrt.cpp:104,114-118).  th has nbin+1 doubles.
+ * Returns GOFR_ERR_UNSUPPORTED when the bin map is not monotone
+ * (rmax <= rmin, non-finite values). */
+int gofr_bin_thresholds(double rmin, double rmax, unsigned nbin, double *th);
+
+/* ---- batched trajectories (one persistent launch) --------------------- */
+
+/* Description of one trajectory of a batch.  Pointers are host buffers in
+ * the same internal format as gofr_set_frames. */
+typedef struct gofr_traj_desc {
+    const double *positions;
+    const double *boxes;
+    int box_kind;
+    const int *type_ids;
+    unsigned ntypes;
+    size_t natoms;
+    size_t nframes;
+    gofr_params params;      /* per-trajectory parameters (kernel and nparts ignored) */
+} gofr_traj_desc;
+
+/* Uploads a batch of trajectories to a context (replacing any frames). */
+int gofr_batch_set(gofr_ctx *ctx, const gofr_traj_desc *trajs, unsigned ntraj);
+
+/* Number of counts of trajectory k of the current batch, and its offset in
+ * the concatenated output of gofr_batch_run. */
+int gofr_batch_output_layout(const gofr_ctx *ctx, unsigned k, size_t *offset, size_t *n_counts);
+
+/* Runs every trajectory of the batch in one persistent launch that pulls
+ * (trajectory, origin, lag, tile) items from a device work queue.  With
+ * use_graph != 0 the launch sequence is captured once into a CUDA graph and
+ * replayed.  counts_host receives the concatenation of every trajectory's
+ * [leff][nch][nbin] counts (gofr_batch_output_layout gives the offsets). */
+int gofr_batch_run(gofr_ctx *ctx, int use_graph, unsigned long long *counts_host);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GOFR_GB300_H */

@@ -1,0 +1,160 @@
+"""ctypes front of the C restatement in oracle/gofr_oracle.c -- TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, always as the checker (or the timed CPU baseline), never as a product
+path.  build() compiles the C file with -ffp-contract=off so that the FP64
+arithmetic matches the reference's separate multiply/add
+(lib/include/basetrajectory.h:215-217) on every host, x86-64 or aarch64.
+"""
+import ctypes
+import os
+import subprocess
+import sysconfig
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libgofr_oracle.so")
+SRC = os.path.join(HERE, "gofr_oracle.c")
+
+_lib = None
+
+
+def build(force=False):
+    """Compile oracle/gofr_oracle.c into oracle/_build/libgofr_oracle.so."""
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if (not force and os.path.exists(LIB_PATH)
+            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC)):
+        return LIB_PATH
+    cc = os.environ.get("CC", "gcc")
+    cmd = [cc, "-O3", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+           "-pthread", SRC, "-o", LIB_PATH + ".tmp", "-lm"]
+    subprocess.check_call(cmd)
+    os.replace(LIB_PATH + ".tmp", LIB_PATH)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        dp = ctypes.POINTER(ctypes.c_double)
+        ip = ctypes.POINTER(ctypes.c_int)
+        up = ctypes.POINTER(ctypes.c_uint64)
+        L.oracle_d2.argtypes = [dp, dp, dp, ctypes.c_int]
+        L.oracle_d2.restype = ctypes.c_double
+        L.oracle_bin.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_uint]
+        L.oracle_bin.restype = ctypes.c_int
+        L.oracle_channel.argtypes = [ctypes.c_uint] * 3
+        L.oracle_channel.restype = ctypes.c_uint
+        L.oracle_lammps_to_internal.argtypes = [dp]
+        L.oracle_lammps_to_internal.restype = None
+        L.oracle_pbc_wrap.argtypes = [dp, dp, ctypes.c_size_t, ctypes.c_int, ctypes.c_size_t,
+                                      ctypes.c_size_t]
+        L.oracle_pbc_wrap.restype = None
+        L.oracle_gofrt_counts.argtypes = [dp, dp, ctypes.c_size_t, ctypes.c_int, ip, ctypes.c_uint,
+                                          ctypes.c_size_t, ctypes.c_size_t, ctypes.c_double,
+                                          ctypes.c_double, ctypes.c_uint, ctypes.c_uint,
+                                          ctypes.c_uint, ctypes.c_uint, ctypes.c_uint,
+                                          ctypes.c_uint, ctypes.c_size_t, up]
+        L.oracle_gofrt_counts.restype = ctypes.c_int
+        L.oracle_incr.argtypes = [ctypes.c_uint, ctypes.c_uint]
+        L.oracle_incr.restype = ctypes.c_double
+        L.oracle_fold_buffer.argtypes = [up, ctypes.c_size_t, ctypes.c_uint, ctypes.c_double, dp]
+        L.oracle_fold_buffer.restype = None
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def d2(xi, xj, box, tric):
+    xi = np.ascontiguousarray(xi, dtype=np.float64)
+    xj = np.ascontiguousarray(xj, dtype=np.float64)
+    b = np.zeros(9)
+    b[:len(box)] = box
+    return lib().oracle_d2(_dp(xi), _dp(xj), _dp(b), int(bool(tric)))
+
+
+def bin_of(d2v, rmin, rmax, nbin):
+    return lib().oracle_bin(float(d2v), float(rmin), float(rmax), int(nbin))
+
+
+def lammps_to_internal(box_rows):
+    """Row-wise copy of lib/include/basetrajectory.h:94-105."""
+    b = np.array(box_rows, dtype=np.float64, copy=True, order="C")
+    for r in range(b.shape[0]):
+        lib().oracle_lammps_to_internal(_dp(b[r]))
+    return b
+
+
+def pbc_wrap(pos, boxes, tric):
+    """Returns a wrapped copy of pos [T][N][3] (basetrajectory.h:145-161)."""
+    p = np.array(pos, dtype=np.float64, copy=True, order="C")
+    bx = np.ascontiguousarray(boxes, dtype=np.float64)
+    T, N = p.shape[0], p.shape[1]
+    for f in range(T):
+        lib().oracle_pbc_wrap(_dp(p), _dp(bx), bx.shape[1], int(bool(tric)), N, f)
+    return p
+
+
+def gofrt_counts(pos, boxes, type_ids, ntypes, rmin, rmax, nbin, tmax, nthreads, skip, every,
+                 ntimesteps, primo, tric=None, per_thread=False):
+    """Integer counts [leff][nch][nbin] (summed over thread partitions unless
+    per_thread) of the reference Gofrt on internal buffers."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    boxes = np.ascontiguousarray(boxes, dtype=np.float64)
+    type_ids = np.ascontiguousarray(type_ids, dtype=np.int32)
+    T, N = pos.shape[0], pos.shape[1]
+    stride = boxes.shape[1]
+    if tric is None:
+        tric = stride == 9
+    nthreads = max(1, int(nthreads))
+    leff = ntimesteps if (ntimesteps < tmax or tmax == 0) else tmax
+    nch = ntypes * (ntypes + 1)
+    out = np.zeros((nthreads, leff, nch, nbin), dtype=np.uint64)
+    rc = lib().oracle_gofrt_counts(
+        _dp(pos), _dp(boxes), stride, int(bool(tric)),
+        type_ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), ntypes, N, T,
+        float(rmin), float(rmax), int(nbin), int(tmax), nthreads, int(skip), int(every),
+        int(ntimesteps), int(primo), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+    if rc == -1:
+        raise RuntimeError("trajectory is too short for this kind of calculation. Select a "
+                           "different starting timestep or lower the size of the average or "
+                           "the lenght of the time lag")
+    if rc != 0:
+        raise MemoryError("oracle allocation failed")
+    return out if per_thread else out.sum(axis=0)
+
+
+def incr(ntimesteps, skip):
+    return lib().oracle_incr(int(ntimesteps), int(skip))
+
+
+def fold_buffer(per_thread_counts, incr_value):
+    c = np.ascontiguousarray(per_thread_counts, dtype=np.uint64)
+    nth = c.shape[0]
+    dl = int(np.prod(c.shape[1:]))
+    out = np.zeros(c.shape[1:], dtype=np.float64)
+    lib().oracle_fold_buffer(c.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)), dl, nth,
+                             float(incr_value), _dp(out))
+    return out
+
+
+def host_info():
+    """CPU model and core count of this host (for the CPU-baseline record)."""
+    model = "unknown"
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                low = line.lower()
+                if low.startswith("model name") or low.startswith("cpu part"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    return {"cpu": model, "cores": os.cpu_count(), "arch": sysconfig.get_platform()}

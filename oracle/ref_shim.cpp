@@ -1,0 +1,62 @@
+// Reduced Python binding of the reference's own Gofrt path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is compiled together with the
+// reference's unmodified sources lib/src/gofrt.cpp, lib/src/basetrajectory.cpp
+// and lib/src/trajectory_numpy.cpp (see oracle/build_ref.sh) into
+// oracle/_ref/pyanalisi_ref*.so.  It exposes exactly the three classes the
+// Gofrt path needs, with the constructor and method signatures of the full
+// reference binding (pyanalisi/src/pyanalisi.cpp:67-82 for Gofrt,
+// :487-527 for Trajectory, :528-532 for BoxFormat), so that fixtures can be
+// generated by the reference itself and the C restatement in
+// oracle/gofr_oracle.c can be pinned against it.
+#include <pybind11/pybind11.h>
+#include <pybind11/numpy.h>
+#include "trajectory_numpy.h"
+#include "gofrt.h"
+
+namespace py = pybind11;
+
+PYBIND11_MODULE(pyanalisi_ref, m) {
+    using G = Gofrt<double, Trajectory_numpy>;
+    py::class_<Trajectory_numpy>(m, "Trajectory")
+        .def(py::init<py::buffer, py::buffer, py::buffer, py::buffer,
+                      Trajectory_numpy::BoxFormat, bool, bool>(),
+             py::keep_alive<1, 2>(), py::keep_alive<1, 3>(),
+             py::keep_alive<1, 4>(), py::keep_alive<1, 5>())
+        .def("get_ntypes", &Trajectory_numpy::get_ntypes)
+        .def("get_natoms", &Trajectory_numpy::get_natoms)
+        .def("get_ntimesteps", &Trajectory_numpy::get_ntimesteps)
+        .def("is_triclinic", &Trajectory_numpy::is_triclinic)
+        // internal (post-preprocessing) buffers: what the hot path reads
+        .def("internal_positions", [](Trajectory_numpy &t) {
+            size_t nt = t.get_ntimesteps(), na = t.get_natoms();
+            return py::array_t<double>({nt, na, (size_t)3}, t.positions_data());
+        })
+        .def("internal_boxes", [](Trajectory_numpy &t) {
+            size_t nt = t.get_ntimesteps(), st = t.get_box_stride();
+            return py::array_t<double>({nt, st}, t.box<false>(0));
+        })
+        .def("internal_type_ids", [](Trajectory_numpy &t) {
+            size_t na = t.get_natoms();
+            py::array_t<int> a(na);
+            for (size_t i = 0; i < na; ++i) a.mutable_data()[i] = t.get_type(i);
+            return a;
+        });
+    py::enum_<Trajectory_numpy::BoxFormat>(m, "BoxFormat", py::arithmetic())
+        .value("Invalid", Trajectory_numpy::BoxFormat::Invalid)
+        .value("CellVectors", Trajectory_numpy::BoxFormat::Cell_vectors)
+        .value("LammpsOrtho", Trajectory_numpy::BoxFormat::Lammps_ortho)
+        .value("LammpsTriclinic", Trajectory_numpy::BoxFormat::Lammps_triclinic);
+    py::class_<G>(m, "Gofrt", py::buffer_protocol())
+        .def(py::init<Trajectory_numpy *, double, double, unsigned int, unsigned int,
+                      unsigned int, unsigned int, unsigned int, bool>())
+        .def("reset", &G::reset)
+        .def("getNumberOfExtraTimestepsNeeded", &G::nExtraTimesteps)
+        .def("calculate", &G::calculate)
+        .def("get_columns_description", &G::get_columns_description)
+        .def_buffer([](G &g) -> py::buffer_info {
+            return py::buffer_info(g.access_vdata(), sizeof(double),
+                                   py::format_descriptor<double>::format(),
+                                   g.get_shape().size(), g.get_shape(), g.get_stride());
+        });
+}
