@@ -75,6 +75,7 @@ struct gofr_ctx {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     gofr_stats stats{};
     size_t batch_total = 0;
+    unsigned long long launches = 0;  // kernels launched on this context
 };
 
 // ---------------------------------------------------------------------------
@@ -430,6 +431,7 @@ int upload_traj(gofr_ctx *ctx, TrajDev &t, const double *positions, const double
     CK(cudaMemcpyAsync(t.types, type_ids, natoms * sizeof(int), cudaMemcpyHostToDevice,
                        ctx->stream));
     CK(cudaMemsetAsync(ctx->d_nonfinite, 0, sizeof(unsigned), ctx->stream));
+    ++ctx->launches;
     if (launch_minmax(t.pos64, nframes * natoms, ctx->d_minmax, ctx->d_nonfinite, ctx->stream))
         return fail(ctx, GOFR_ERR_CUDA, "min/max kernel launch failed: %s",
                     cudaGetErrorString(cudaGetLastError()));
@@ -454,6 +456,7 @@ int upload_traj(gofr_ctx *ctx, TrajDev &t, const double *positions, const double
         double m = std::max(std::fabs(mx - t.shift[k]), std::fabs(t.shift[k] - mn));
         t.M[k] = m * (1.0 + std::ldexp(1.0, -40)) + 1e-300;
     }
+    ++ctx->launches;
     if (launch_convert(t.pos64, t.types, nframes, natoms, t.shift[0], t.shift[1], t.shift[2],
                        t.pos32, ctx->stream))
         return fail(ctx, GOFR_ERR_CUDA, "convert kernel launch failed: %s",
@@ -595,6 +598,7 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
         L.n_itiles = (int)((a1 - a0 + TI - 1) / TI);
         L.n_items = (long long)L.n_lags * L.n_itiles * L.n_orig;
         L.counts = counts + (size_t)q * rs.data_length;
+        ++ctx->launches;
         if (launch_pairs(L, pl.kind, pl.wrapcheck, ctx->num_sms, ctx->stream, nullptr))
             return fail(ctx, GOFR_ERR_CUDA, "pair kernel launch failed: %s",
                         cudaGetErrorString(cudaGetLastError()));
@@ -782,6 +786,7 @@ int gofr_get_stats(const gofr_ctx *ctx, gofr_stats *out)
 {
     if (!ctx || !out) return GOFR_ERR_ARG;
     *out = ctx->stats;
+    out->launches = ctx->launches;
     return GOFR_OK;
 }
 

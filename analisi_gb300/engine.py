@@ -25,7 +25,7 @@ EXPORTED = [
     "gofr_ctx_create", "gofr_ctx_destroy", "gofr_last_error", "gofr_set_frames",
     "gofr_output_size", "gofr_run", "gofr_run_device", "gofr_sync", "gofr_get_stats",
     "gofr_counts_to_buffer", "gofr_bin_thresholds", "gofr_batch_set",
-    "gofr_batch_output_layout", "gofr_batch_run",
+    "gofr_batch_output_layout", "gofr_batch_run", "gofr_measure_peaks",
 ]
 
 
@@ -51,7 +51,7 @@ class Stats(ctypes.Structure):
                 ("candidates", ctypes.c_ulonglong), ("rechecks", ctypes.c_ulonglong),
                 ("kernel_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
                 ("kernel_used", ctypes.c_int), ("wrap_checked", ctypes.c_int),
-                ("err_bound_d2", ctypes.c_double)]
+                ("err_bound_d2", ctypes.c_double), ("launches", ctypes.c_ulonglong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -101,10 +101,11 @@ def load_library(path=None):
     L.gofr_batch_output_layout.argtypes = [vp, ctypes.c_uint, ctypes.POINTER(ctypes.c_size_t),
                                            ctypes.POINTER(ctypes.c_size_t)]
     L.gofr_batch_run.argtypes = [vp, ctypes.c_int, up]
+    L.gofr_measure_peaks.argtypes = [ctypes.c_int, dp, dp]
     for name in ("gofr_ctx_create", "gofr_set_frames", "gofr_output_size", "gofr_run",
                  "gofr_run_device", "gofr_sync", "gofr_get_stats", "gofr_counts_to_buffer",
                  "gofr_bin_thresholds", "gofr_batch_set", "gofr_batch_output_layout",
-                 "gofr_batch_run"):
+                 "gofr_batch_run", "gofr_measure_peaks"):
         getattr(L, name).restype = ctypes.c_int
     if path is None:
         _lib = L
@@ -120,6 +121,16 @@ def make_params(rmin, rmax, nbin, tmax=0, skip=1, every=1, ntimesteps=0, primo=0
     return Params(float(rmin), float(rmax), int(nbin), int(tmax), int(skip), int(every),
                   int(ntimesteps), int(primo), KERNELS[kernel] if isinstance(kernel, str)
                   else int(kernel), int(nparts))
+
+
+def measure_peaks(device=0):
+    """(FP32 lane operations/s, shared-memory u32 atomics/s) measured on the GPU."""
+    L = load_library()
+    a, b = ctypes.c_double(), ctypes.c_double()
+    rc = L.gofr_measure_peaks(int(device), ctypes.byref(a), ctypes.byref(b))
+    if rc != GOFR_OK:
+        raise GofrError(rc, "peak measurement failed")
+    return a.value, b.value
 
 
 def bin_thresholds(rmin, rmax, nbin):

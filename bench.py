@@ -1,0 +1,388 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 Gofrt engine on the 16k-atom workload.
+
+Workload (the reference's headline configuration for this path): N=16384
+atoms in 3 types (16352/16/16), cubic box at density 0.1 (L=54.72 A),
+Gaussian random walk sigma=0.08 A, T=2000 frames; Gofrt(rmin=0, rmax=12,
+nbin=400, tmax=200, skip=4), reset(1800), i.e. 450 origins x 200 lags x N^2
+ordered pairs = 2.42e13 pair evaluations.  Seeded synthetic data
+(analisi_gb300.workloads.c2), no dataset.
+
+One step = one Gofrt::calculate over a window of 25 consecutive origins
+(reset(100), calculate(primo)) x all 200 lags: step s uses primo=100*(s mod 18),
+so 18 steps are exactly the full reset(1800) calculation, split the way the
+reference's block-average driver splits a trajectory.
+
+  value   pair throughput with the frames resident in HBM (device-timed with
+          CUDA events on the engine's stream, L2 flushed between steps)
+  e2e     the same metric through the C ABI with host buffers: every step
+          uploads its 300-frame window from pinned host memory
+          (gofr_set_frames) and reads the counts back (gofr_run)
+  roofline  FP32-issue bound: 16 FP32 lane operations per ordered pair
+          (orthorhombic), against the FP32 lane-op peak measured on this GPU
+          by gofr_measure_peaks
+  cpu_baseline  the C restatement of the reference (oracle/gofr_oracle.c,
+          same fork/join thread split as the reference) on this host's cores,
+          on a bounded sample of the same workload
+
+--impl reference times that CPU implementation alone (the reference's own
+algorithm on the host cores), with the same metric and configuration.
+"""
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "g(r,t) Gpairs/s on 1 GB300: FP32+FP64-edge-recheck vs plain FP64, exact counts"
+UNIT = "Gpairs/s"
+ORIGINS_PER_STEP = 25
+OPS_PER_PAIR = 16  # orthorhombic FP32 pair: 3 sub + 3x(ffma, fadd, ffma) + fmul + 2 ffma + cmp
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-f64", action="store_true")
+    ap.add_argument("--lags", type=int, default=200,
+                    help="tmax of every step (200 = the workload; smaller only for ncu captures)")
+    return ap.parse_args()
+
+
+def dist_info():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def step_window(s, rank=0):
+    """primo of step s: 18 windows of 100 origins-frames cover reset(1800)."""
+    return 100 * ((s + rank * 7) % 18)
+
+
+def workload_config(extra=None):
+    cfg = {"workload": "c2_n16384_t2000_ortho", "natoms": 16384, "types": [16352, 16, 16],
+           "box": "cubic L=54.72 (density 0.1)", "frames": 2000, "sigma": 0.08,
+           "rmin": 0.0, "rmax": 12.0, "nbin": 400, "tmax": 200, "skip": 4, "every": 1,
+           "reset": 1800, "step": "calculate over 25 origins (reset(100), primo=100*(s%18)) "
+                                   "x 200 lags; 18 steps = the full reset(1800)",
+           "l2": "flushed between timed steps (256 MiB write); per-step inputs ~60 MB < L2"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+# ---------------------------------------------------------------------------
+# CPU leg: the oracle port with the reference's thread split
+# ---------------------------------------------------------------------------
+def cpu_sample(w, seconds=15.0, threads=None):
+    """Times the C restatement on a bounded sample of the workload.
+    Returns (Gpairs/s, threads, description)."""
+    from oracle import oracle
+    oracle.build()
+    threads = threads or os.cpu_count() or 1
+    N = w["positions"].shape[1]
+    p = w["params"]
+    pos, boxes, tids = w["positions"], w["boxes"], w["type_ids"]
+
+    def run(n_lags):
+        # 1 origin, lags 0..n_lags-1: reset(n) with tmax=n and skip=n
+        t0 = time.perf_counter()
+        oracle.gofrt_counts(pos, boxes, tids, w["ntypes"], p["rmin"], p["rmax"], p["nbin"],
+                            n_lags, threads, n_lags, 1, n_lags, 0)
+        return time.perf_counter() - t0
+
+    dt = run(1)
+    n_lags = max(1, min(200, int(seconds / max(dt, 1e-3))))
+    dt = run(n_lags)
+    pairs = n_lags * N * N
+    desc = (f"1 origin x {n_lags} lags of the workload ({pairs:.3g} ordered pairs), "
+            f"{threads} threads forked/joined per (lag, origin) as the reference does")
+    return pairs / dt / 1e9, threads, desc, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    from analisi_gb300 import workloads
+    w = workloads.c2()
+    from oracle import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    N = 16384
+    p = w["params"]
+    n_lags = None
+    times = []
+    for s in range(args.warmup + args.steps):
+        if n_lags is None:
+            t0 = time.perf_counter()
+            oracle.gofrt_counts(w["positions"], w["boxes"], w["type_ids"], w["ntypes"],
+                                p["rmin"], p["rmax"], p["nbin"], 1, threads, 1, 1, 1, 0)
+            dt1 = time.perf_counter() - t0
+            n_lags = max(1, min(200, int(6.0 / max(dt1, 1e-3))))
+        primo = step_window(s)
+        t0 = time.perf_counter()
+        oracle.gofrt_counts(w["positions"], w["boxes"], w["type_ids"], w["ntypes"], p["rmin"],
+                            p["rmax"], p["nbin"], n_lags, threads, n_lags, 1, n_lags, primo)
+        dt = time.perf_counter() - t0
+        if s >= args.warmup:
+            times.append(dt)
+    pairs = n_lags * N * N
+    val = pairs * len(times) / sum(times) / 1e9
+    from oracle.oracle import host_info
+    hi = host_info()
+    sample = (f"each step: 1 origin (primo=100*(s%18)) x {n_lags} lags = {pairs:.3g} pairs "
+              f"on {threads} threads of {hi['cpu']} ({hi['arch']})")
+    out = {"metric": METRIC, "value": round(val, 4), "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(1e3 * sum(times) / len(times), 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "impl": "reference",
+           "config": workload_config({"reference_kind": "port of lib/src/gofrt.cpp "
+                                      "(oracle/gofr_oracle.c): the reference's sources need "
+                                      "its tree, absent on this host"}),
+           "cpu_baseline": {"value": round(val, 4), "unit": UNIT, "cores": threads,
+                            "kind": "port", "sample": sample},
+           "e2e": {"value": round(val, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+class Clocks:
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self, gpu_index):
+        try:
+            rows = [l.split(",") for l in open(self.path) if l.strip()]
+        except OSError:
+            return None
+        rows = [[c.strip() for c in r] for r in rows if len(r) >= 9]
+        rows = [r for r in rows if r[0] == str(gpu_index)] or rows
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if re.match(r"^[\d.]+$", r[1])]
+        mx = [float(r[2]) for r in rows if re.match(r"^[\d.]+$", r[2])]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, n in enumerate(names):
+                if r[5 + k].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def traffic_from_profiles():
+    """dram bytes per launch of the FP32 pair kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "k_pairs_f32_c2_n16384.md")
+    try:
+        for line in open(path):
+            m = re.search(r"traffic_bytes_per_launch:\s*([\d.eE+]+)", line)
+            if m:
+                return float(m.group(1))
+    except OSError:
+        pass
+    return None
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    from analisi_gb300 import engine, workloads
+    w = workloads.c2()
+    p = w["params"]
+    N = w["positions"].shape[1]
+    eng = engine.Engine(local)
+    eng.set_frames(w["positions"], w["boxes"], w["type_ids"], w["ntypes"])
+    step_n = ORIGINS_PER_STEP * p["skip"]
+    lags = min(args.lags, p["tmax"])
+    prm = [engine.make_params(p["rmin"], p["rmax"], p["nbin"], lags, p["skip"], p["every"],
+                              step_n, step_window(s, rank)) for s in range(18)]
+    nout = eng.output_size(prm[0])
+    out = np.zeros(nout, dtype=np.uint64)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # warm-up
+    for s in range(args.warmup):
+        eng.run_params(prm[s % 18], out)
+    st0 = eng.stats()
+    launches0 = st0["launches"]
+    kernel_ms, total_ms, cands, rech, pairs = [], [], 0, 0, 0
+    barrier()
+    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+    with Clocks(os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv")) as clk:
+        for s in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            eng.run_params(prm[(args.warmup + s) % 18], out)
+            st = eng.stats()
+            kernel_ms.append(st["kernel_ms"])
+            total_ms.append(st["total_ms"])
+            cands += st["candidates"]
+            rech += st["rechecks"]
+            pairs += st["pairs"]
+    barrier()
+    launches = eng.stats()["launches"] - launches0
+    dev_s = sum(total_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([dev_s], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_s = float(t[0])
+    value = pairs * world / dev_s / 1e9
+    kernel_avg_s = sum(kernel_ms) / len(kernel_ms) / 1e3
+    pairs_per_launch = pairs / args.steps
+
+    # e2e through the C ABI with host buffers (pinned), copies in the timed region
+    e2e = None
+    if not args.no_e2e:
+        win_frames = step_n + p["tmax"]
+        pinned_pos = torch.empty((win_frames, N, 3), dtype=torch.float64).pin_memory()
+        pinned_box = torch.empty((win_frames, 6), dtype=torch.float64).pin_memory()
+        pp, pb = pinned_pos.numpy(), pinned_box.numpy()
+        e2 = engine.Engine(local)
+        pe = [engine.make_params(p["rmin"], p["rmax"], p["nbin"], lags, p["skip"],
+                                 p["every"], step_n, 0) for _ in range(1)]
+        times = []
+        h2d = win_frames * N * 24 + win_frames * 48 + N * 4
+        for s in range(args.warmup + args.steps):
+            primo = step_window(s, rank)
+            pp[...] = w["positions"][primo:primo + win_frames]
+            pb[...] = w["boxes"][primo:primo + win_frames]
+            flush.zero_()
+            barrier()
+            t0 = time.perf_counter()
+            e2.set_frames(pp, pb, w["type_ids"], w["ntypes"])
+            e2.run_params(pe[0], out)
+            dt = time.perf_counter() - t0
+            if s >= args.warmup:
+                times.append(dt)
+        e2_launch = e2.stats()["launches"]
+        e2.close()
+        e2e_s = sum(times)
+        if world > 1:
+            t = torch.tensor([e2e_s], dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e_s = float(t[0])
+        e2e = {"value": round(pairs * world / e2e_s / 1e9, 3), "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(nout * 8),
+               "timing": "host wall clock around gofr_set_frames + gofr_run (synchronous)",
+               "launches": int(e2_launch)}
+
+    # FP64 comparison kernel on a sample (1 origin x 10 lags), same engine
+    f64 = None
+    if rank == 0 and not args.no_f64:
+        pf = engine.make_params(p["rmin"], p["rmax"], p["nbin"], 10, p["skip"], p["every"],
+                                4, 0, kernel="f64")
+        o64 = np.zeros(eng.output_size(pf), dtype=np.uint64)
+        eng.run_params(pf, o64)
+        st = eng.stats()
+        pf32 = engine.make_params(p["rmin"], p["rmax"], p["nbin"], 10, p["skip"], p["every"],
+                                  4, 0, kernel="f32")
+        o32 = np.zeros_like(o64)
+        eng.run_params(pf32, o32)
+        st32 = eng.stats()
+        f64 = {"gpairs_per_s_f64": round(st["pairs"] / st["kernel_ms"] / 1e6, 3),
+               "gpairs_per_s_f32_same_sample": round(st32["pairs"] / st32["kernel_ms"] / 1e6, 3),
+               "counts_identical": bool(np.array_equal(o64, o32)),
+               "sample": "1 origin x 10 lags (1.07e9 pairs)"}
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+        return 0
+
+    fp32_peak, satom_peak = engine.measure_peaks(local)
+    achieved = pairs_per_launch * OPS_PER_PAIR / kernel_avg_s / 1e12
+    peak = fp32_peak / 1e12
+    traffic = traffic_from_profiles()
+    roof = {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(peak, 3),
+            "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
+            "traffic": traffic,
+            "notes": "FP32 lane operations (one FADD/FMUL/FFMA = 1) at 16 per ordered pair; "
+                     "peak = FFMA issue rate measured on this GPU (gofr_measure_peaks, burst); "
+                     "traffic = ncu dram bytes per launch (profiles/)",
+            "smem_atomic_peak_per_s": satom_peak,
+            "atomics_needed_per_s": round(cands / (sum(kernel_ms) / 1e3), 1)}
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, thr, desc, dt = cpu_sample(w, seconds=15.0)
+        cpu = {"value": round(v, 4), "unit": UNIT, "cores": thr, "kind": "port",
+               "sample": desc, "seconds": round(dt, 2)}
+    clocks = clk.summary(local)
+    res = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(1e3 * dev_s / args.steps, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64-recheck (u64 counts)",
+           "data": "synthetic (seeded random walk, analisi_gb300.workloads.c2)",
+           "config": workload_config({"pairs_per_step": int(pairs_per_launch), "lags": lags,
+                                      "candidates_frac": round(cands / pairs, 6),
+                                      "recheck_frac": rech / pairs}),
+           "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
+           "clocks": clocks, "fp64_kernel": f64,
+           "kernel_ms_per_step": round(1e3 * kernel_avg_s, 3)}
+    print(json.dumps(res))
+    if world > 1:
+        torch.distributed.barrier()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

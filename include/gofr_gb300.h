@@ -89,6 +89,7 @@ typedef struct gofr_stats {
     int kernel_used;                 /* enum gofr_kernel actually launched */
     int wrap_checked;                /* 1 if the per-pair wrap-decision check was on */
     double err_bound_d2;             /* FP32 error bound on d2 at rmax (A^2) */
+    unsigned long long launches;     /* kernels launched on this context since its creation */
 } gofr_stats;
 
 /* Creates a context on CUDA device `device` (replaces the construction of a
@@ -149,6 +150,12 @@ int gofr_counts_to_buffer(const unsigned long long *counts, size_t n, unsigned n
  * Returns GOFR_ERR_UNSUPPORTED when the bin map is not monotone
  * (rmax <= rmin, non-finite values). */
 int gofr_bin_thresholds(double rmin, double rmax, unsigned nbin, double *th);
+
+/* Measures, on `device`, the two peaks that bound the FP32 pair kernel: the
+ * FP32 lane-operation rate (one FFMA = one operation, the unit of the kernel's
+ * 16/19 operations per pair) and the shared-memory u32 atomic rate.  No
+ * reference counterpart: the reference has no GPU path. */
+int gofr_measure_peaks(int device, double *fp32_lane_ops_per_s, double *smem_atomics_per_s);
 
 /* ---- batched trajectories (one persistent launch) --------------------- */
 
