@@ -42,7 +42,8 @@ struct TrajDev {
     unsigned ntypes = 0;
     int tric = 0;
     double *pos64 = nullptr;
-    float4 *pos32 = nullptr;
+    float *pos32 = nullptr;          // [T][3][NP]
+    unsigned char *types8 = nullptr; // [NP]
     double *box64 = nullptr;
     Box32 *box32 = nullptr;
     int *types = nullptr;
@@ -137,7 +138,9 @@ void free_traj(TrajDev &t)
     cudaFree(t.box64);
     cudaFree(t.box32);
     cudaFree(t.types);
+    cudaFree(t.types8);
     t.pos64 = nullptr; t.pos32 = nullptr; t.box64 = nullptr; t.box32 = nullptr; t.types = nullptr;
+    t.types8 = nullptr;
 }
 
 inline uint64_t dbits(double x) { uint64_t u; std::memcpy(&u, &x, 8); return u; }
@@ -418,7 +421,9 @@ int upload_traj(gofr_ctx *ctx, TrajDev &t, const double *positions, const double
     free_traj(t);
     const size_t n3 = nframes * natoms * 3;
     CK(cudaMalloc(&t.pos64, n3 * sizeof(double)));
-    CK(cudaMalloc(&t.pos32, nframes * natoms * sizeof(float4)));
+    const size_t NP = padded_natoms(natoms);
+    CK(cudaMalloc(&t.pos32, nframes * 3 * NP * sizeof(float)));
+    CK(cudaMalloc(&t.types8, NP));
     CK(cudaMalloc(&t.box64, nframes * 9 * sizeof(double)));
     CK(cudaMalloc(&t.box32, nframes * sizeof(Box32)));
     CK(cudaMalloc(&t.types, natoms * sizeof(int)));
@@ -458,7 +463,7 @@ int upload_traj(gofr_ctx *ctx, TrajDev &t, const double *positions, const double
     }
     ++ctx->launches;
     if (launch_convert(t.pos64, t.types, nframes, natoms, t.shift[0], t.shift[1], t.shift[2],
-                       t.pos32, ctx->stream))
+                       t.pos32, t.types8, ctx->stream))
         return fail(ctx, GOFR_ERR_CUDA, "convert kernel launch failed: %s",
                     cudaGetErrorString(cudaGetLastError()));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -561,6 +566,7 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
                     rs.nch, p.nbin, smem, max_smem);
     PairLaunch L{};
     L.pos32 = t.pos32;
+    L.types8 = t.types8;
     L.pos64 = t.pos64;
     L.box64 = t.box64;
     L.box32 = t.box32;
@@ -569,6 +575,7 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
     L.err = ctx->d_err;
     L.stats = ctx->d_stats;
     L.N = (int)t.N;
+    L.NP = (int)padded_natoms(t.N);
     L.nbin = (int)p.nbin;
     L.nch = (int)rs.nch;
     L.ntypes = (int)t.ntypes;
@@ -588,7 +595,7 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
         L.wlim = (float)(0.5 - pl.b.eta);
     }
     const unsigned nparts = p.nparts > 1 ? p.nparts : 1;
-    const int TI = pl.kind == 0 ? 512 : 512;
+    const int TI = pairs_tile_atoms(pl.kind);
     const size_t per = t.N / nparts;
     for (unsigned q = 0; q < nparts; ++q) {
         size_t a0 = q * per, a1 = (q == nparts - 1) ? t.N : (q + 1) * per;

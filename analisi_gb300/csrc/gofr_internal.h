@@ -30,7 +30,8 @@ struct Box32 {
 
 // One launch of an all-pairs kernel over (lag, i-tile, origin) items.
 struct PairLaunch {
-    const float4 *pos32;      // [T][N] {x-cx, y-cy, z-cz, type id bits}
+    const float *pos32;       // [T][3][NP] SoA {x-cx | y-cy | z-cz}, padding NaN
+    const unsigned char *types8; // [NP] dense type ids (padding 0)
     const double *pos64;      // [T][N][3] internal FP64 positions (reference values)
     const double *box64;      // [T][9] internal boxes (tilts zero when orthorhombic)
     const Box32 *box32;       // [T]
@@ -39,7 +40,7 @@ struct PairLaunch {
     unsigned long long *counts;  // [leff][nch][nbin]
     unsigned *err;
     unsigned long long *stats;
-    int N, nbin, nch, ntypes;
+    int N, NP, nbin, nch, ntypes;
     int a0, a1;               // first-atom range [a0, a1) (one reference thread partition)
     int n_lags, every;        // lags t = l*every, l < n_lags
     int n_orig, skip;         // origins primo + k*skip, k < n_orig
@@ -56,12 +57,15 @@ struct PairLaunch {
 // Launch configuration helpers implemented in gofr_kernels.cu.
 int launch_minmax(const double *pos64, size_t n3, double *d_out6, unsigned *d_nonfinite,
                   cudaStream_t s);
+// Padded per-frame stride of the FP32 SoA frames.
+inline size_t padded_natoms(size_t N) { return (N + 15) / 16 * 16; }
 int launch_convert(const double *pos64, const int *types, size_t T, size_t N, double cx,
-                   double cy, double cz, float4 *pos32, cudaStream_t s);
+                   double cy, double cz, float *pos32, unsigned char *types8, cudaStream_t s);
 // kind: 0 = FP32+recheck, 1 = FP64.  wrapcheck only for kind 0.
 int launch_pairs(const PairLaunch &P, int kind, bool wrapcheck, int num_sms, cudaStream_t s,
                  size_t *smem_bytes_out);
 int pairs_smem_bytes(int kind, int nch, int nbin, int ntypes);
+int pairs_tile_atoms(int kind);
 int launch_zero_u64(unsigned long long *p, size_t n, cudaStream_t s);
 
 }  // namespace gofr

@@ -9,11 +9,18 @@
 // item of a Gofrt::calculate.  A persistent grid of CTAs takes contiguous,
 // lag-major ranges of items, so consecutive items of a CTA share the lag and
 // its shared-memory histogram [nch][nbin] is flushed to the global u64 counts
-// only when the lag changes (or before a u32 bin could overflow).  Inside an
-// item, each thread holds R first atoms (frame `origin`) in registers and the
-// CTA streams the second atoms (frame `origin+lag`) through shared memory in
-// tiles of TJ atoms, double buffered with 1-D TMA bulk copies completed on
-// mbarriers.
+// only when the lag changes (or before a u32 bin could overflow).
+//
+// FP32 kernel, per item: each thread holds R first atoms (frame `origin`)
+// in registers, duplicated into f32x2 pairs; the CTA streams the second atoms
+// (frame `origin+lag`, SoA x|y|z blocks plus u8 types) through shared memory
+// in tiles of TJ atoms, double buffered with 1-D TMA bulk copies completed on
+// mbarriers.  Distances are computed two second-atoms per packed f32x2
+// instruction.  The rare pairs that land inside the accept window (plus its
+// error bound) are appended to per-thread slots in shared memory and binned
+// later by the whole warp, so the hot loop never diverges; pairs whose FP32
+// bin cannot be certified go to a per-CTA queue recomputed in FP64 by all
+// threads together at the end of the item.
 #include <cstdint>
 #include <cstdio>
 #include <cuda_runtime.h>
@@ -23,10 +30,12 @@
 
 namespace gofr {
 
-constexpr int NT = 256;      // threads per CTA
-constexpr int R32 = 2;       // first atoms per thread, FP32 kernel
+constexpr int NT = 256;       // threads per CTA
+constexpr int R32 = 4;        // first atoms per thread, FP32 kernel
 constexpr int TI32 = NT * R32;
-constexpr int TJ32 = 1024;   // second atoms per shared-memory tile (16 KB of float4)
+constexpr int TJ32 = 1024;    // second atoms per shared-memory tile
+constexpr int SLOTS = 16;     // candidate slots per thread
+constexpr int QCAP = 1024;    // FP64 recheck queue entries per CTA
 constexpr int R64 = 2;
 constexpr int TI64 = NT * R64;
 constexpr int TJ64 = 512;
@@ -77,11 +86,12 @@ __device__ __forceinline__ void add_stats(unsigned long long *stats, unsigned lo
 
 // Exact FP64 re-evaluation of one pair, exactly as the reference computes it.
 template <bool TRI>
-__device__ __noinline__ void recheck_pair(const double *__restrict__ pos64,
-                                          const double *__restrict__ box64, long long N,
-                                          long long fo, long long fl, int ia, int ja,
-                                          unsigned *hist, int ch, int nbin, double rmin,
-                                          double dr, double rmin2, double rmax2, unsigned *err)
+__device__ __forceinline__ void recheck_pair(const double *__restrict__ pos64,
+                                             const double *__restrict__ box64, long long N,
+                                             long long fo, long long fl, int ia, int ja,
+                                             unsigned *hist, int ch, int nbin, double rmin,
+                                             double dr, double rmin2, double rmax2,
+                                             unsigned *err)
 {
     const double *xi = pos64 + (fo * N + ia) * 3;
     const double *xj = pos64 + (fl * N + ja) * 3;
@@ -92,27 +102,172 @@ __device__ __noinline__ void recheck_pair(const double *__restrict__ pos64,
 }
 
 // ---------------------------------------------------------------------------
+// packed f32x2 arithmetic (PTX ISA add/sub/mul/fma .f32x2, sm_100+)
+// ---------------------------------------------------------------------------
+typedef unsigned long long f2;
+
+__device__ __forceinline__ f2 f2pk(float a, float b)
+{
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2up(f2 v, float &a, float &b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2 f2add(f2 a, f2 b)
+{
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2sub(f2 a, f2 b)
+{
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2mul(f2 a, f2 b)
+{
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2fma(f2 a, f2 b, f2 c)
+{
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// Box constants of one origin frame, duplicated into both f32x2 lanes.
+struct Box2 {
+    f2 invL[3], negL[3];
+    f2 negT[3];   // -{xy, xz, yz}
+};
+
+// Minimum-image d2 of (i, j0) and (i, j1) in one f32x2 lane pair.
+// WCHK: also reports, per lane, whether some wrap quotient lay within the
+// certified bound of a half-integer (bits 0 and 1 of *wflag).
+template <bool TRI, bool WCHK>
+__device__ __forceinline__ f2 pair2(f2 xi, f2 yi, f2 zi, f2 xj, f2 yj, f2 zj, const Box2 &b,
+                                    float wlim, unsigned *wflag)
+{
+    const f2 MAG = f2pk(12582912.0f, 12582912.0f);  // 1.5*2^23: rounds to integer
+    f2 dx = f2sub(xi, xj), dy = f2sub(yi, yj), dz = f2sub(zi, zj);
+    if (TRI) {
+        f2 kz;
+        if (WCHK) {
+            f2 q = f2mul(dz, b.invL[2]);
+            kz = f2sub(f2add(q, MAG), MAG);
+            float a0, a1;
+            f2up(f2sub(q, kz), a0, a1);
+            *wflag |= (fabsf(a0) > wlim ? 1u : 0u) | (fabsf(a1) > wlim ? 2u : 0u);
+        } else {
+            kz = f2sub(f2fma(dz, b.invL[2], MAG), MAG);
+        }
+        dz = f2fma(kz, b.negL[2], dz);
+        dy = f2fma(kz, b.negT[2], dy);
+        dx = f2fma(kz, b.negT[1], dx);
+        f2 ky;
+        if (WCHK) {
+            f2 q = f2mul(dy, b.invL[1]);
+            ky = f2sub(f2add(q, MAG), MAG);
+            float a0, a1;
+            f2up(f2sub(q, ky), a0, a1);
+            *wflag |= (fabsf(a0) > wlim ? 1u : 0u) | (fabsf(a1) > wlim ? 2u : 0u);
+        } else {
+            ky = f2sub(f2fma(dy, b.invL[1], MAG), MAG);
+        }
+        dy = f2fma(ky, b.negL[1], dy);
+        dx = f2fma(ky, b.negT[0], dx);
+        f2 kx;
+        if (WCHK) {
+            f2 q = f2mul(dx, b.invL[0]);
+            kx = f2sub(f2add(q, MAG), MAG);
+            float a0, a1;
+            f2up(f2sub(q, kx), a0, a1);
+            *wflag |= (fabsf(a0) > wlim ? 1u : 0u) | (fabsf(a1) > wlim ? 2u : 0u);
+        } else {
+            kx = f2sub(f2fma(dx, b.invL[0], MAG), MAG);
+        }
+        dx = f2fma(kx, b.negL[0], dx);
+    } else {
+        f2 kx, ky, kz;
+        if (WCHK) {
+            f2 qx = f2mul(dx, b.invL[0]), qy = f2mul(dy, b.invL[1]), qz = f2mul(dz, b.invL[2]);
+            kx = f2sub(f2add(qx, MAG), MAG);
+            ky = f2sub(f2add(qy, MAG), MAG);
+            kz = f2sub(f2add(qz, MAG), MAG);
+            float a0, a1, c0, c1, e0, e1;
+            f2up(f2sub(qx, kx), a0, a1);
+            f2up(f2sub(qy, ky), c0, c1);
+            f2up(f2sub(qz, kz), e0, e1);
+            bool w0 = fabsf(a0) > wlim || fabsf(c0) > wlim || fabsf(e0) > wlim;
+            bool w1 = fabsf(a1) > wlim || fabsf(c1) > wlim || fabsf(e1) > wlim;
+            *wflag |= (w0 ? 1u : 0u) | (w1 ? 2u : 0u);
+        } else {
+            kx = f2sub(f2fma(dx, b.invL[0], MAG), MAG);
+            ky = f2sub(f2fma(dy, b.invL[1], MAG), MAG);
+            kz = f2sub(f2fma(dz, b.invL[2], MAG), MAG);
+        }
+        dx = f2fma(kx, b.negL[0], dx);
+        dy = f2fma(ky, b.negL[1], dy);
+        dz = f2fma(kz, b.negL[2], dz);
+    }
+    f2 d2 = f2mul(dx, dx);
+    d2 = f2fma(dy, dy, d2);
+    d2 = f2fma(dz, dz, d2);
+    return d2;
+}
+
+// Shared-memory layout of the FP32 kernel (byte offsets).
+struct F32Smem {
+    int jx, jt, bars, flag, rqn, win, hist, chtab, slots, rq, total;
+    __host__ __device__ F32Smem(int nbin, int nch, int ntypes)
+    {
+        int o = 0;
+        jx = o;    o += 2 * 3 * TJ32 * 4;        // [2][3][TJ] floats
+        jt = o;    o += 2 * TJ32;                // [2][TJ] u8 types
+        bars = o;  o += 16;                      // 2 mbarriers
+        flag = o;  o += 8;
+        rqn = o;   o += 8;
+        slots = o; o += SLOTS * NT * 8;          // [SLOTS][NT] uint2
+        rq = o;    o += QCAP * 16;               // [QCAP] uint4
+        win = o;   o += nbin * 8;                // [nbin] float2
+        hist = o;  o += nch * nbin * 4;          // [nch][nbin] u32
+        chtab = o; o += ntypes * ntypes * 2;     // [ntypes][ntypes] u16
+        total = (o + 127) / 128 * 128;
+    }
+};
+
+// ---------------------------------------------------------------------------
 // FP32 bulk + FP64 edge recheck
 // ---------------------------------------------------------------------------
 //
-// Per pair (orthorhombic): 3 FADD for the raw difference, per axis an FFMA
-// with a 1.5*2^23 offset and an FADD that round d/L to the nearest integer k,
-// an FFMA d - k*L (L rounded to FP32; its rounding is part of the bound),
-// then d2 by FMUL + 2 FFMA and one compare against hi_f.
-// The bound behind hi_f, lo_f and the per-bin windows is derived on the host
-// (gofr_capi.cu, certify()): a pair whose FP32 d2 falls outside its bin's
-// window, or (WCHK) whose wrap quotient lies within the error bound of a
-// half-integer, is recomputed in FP64 by recheck_pair.
+// Per pair (orthorhombic): FP32 difference, per axis an FMA with a 1.5*2^23
+// offset and a subtraction that round d/L to the nearest integer k, an FMA
+// d - k*L (L rounded to FP32; its rounding is part of the bound), then d2 by
+// one multiply and two FMAs -- 15 FP32 operations issued as f32x2 for two
+// second atoms at once -- and one compare against hi_f.  The bound behind
+// hi_f, lo_f and the per-bin windows is derived on the host (gofr_capi.cu,
+// certify()).
 template <bool TRI, bool WCHK>
 __global__ void __launch_bounds__(NT, 2) k_pairs_f32(const PairLaunch P)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    float4 *jbuf = reinterpret_cast<float4 *>(smem);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + 2 * TJ32 * sizeof(float4));
-    int *sflag = reinterpret_cast<int *>(bars + 2);
-    float2 *win = reinterpret_cast<float2 *>(smem + 2 * TJ32 * sizeof(float4) + 32);
-    unsigned *hist = reinterpret_cast<unsigned *>(win + P.nbin);
-    unsigned short *chtab = reinterpret_cast<unsigned short *>(hist + P.nch * P.nbin);
+    const F32Smem L(P.nbin, P.nch, P.ntypes);
+    float *jx = reinterpret_cast<float *>(smem + L.jx);
+    unsigned char *jt = smem + L.jt;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.bars);
+    int *sflag = reinterpret_cast<int *>(smem + L.flag);
+    int *rqn = reinterpret_cast<int *>(smem + L.rqn);
+    uint2 *slots = reinterpret_cast<uint2 *>(smem + L.slots);
+    uint4 *rq = reinterpret_cast<uint4 *>(smem + L.rq);
+    float2 *win = reinterpret_cast<float2 *>(smem + L.win);
+    unsigned *hist = reinterpret_cast<unsigned *>(smem + L.hist);
+    unsigned short *chtab = reinterpret_cast<unsigned short *>(smem + L.chtab);
 
     const int tid = threadIdx.x;
     const int hlen = P.nch * P.nbin;
@@ -124,6 +279,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f32(const PairLaunch P)
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         *sflag = 0;
+        *rqn = 0;
         fence_mbar_init();
     }
     __syncthreads();
@@ -131,16 +287,17 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f32(const PairLaunch P)
     const long long per = (P.n_items + gridDim.x - 1) / gridDim.x;
     const long long it0 = (long long)blockIdx.x * per;
     const long long it1 = min(it0 + per, P.n_items);
-    const long long N = P.N;
+    const long long N = P.N, NP = P.NP;
     const int nchunks = (P.N + TJ32 - 1) / TJ32;
     const long long flush_every = items_per_flush(TI32, P.N);
-    const float MAGIC = 12582912.0f;  // 1.5 * 2^23
+    const float hi_f = P.hi_f;
 
     unsigned phase0 = 0u, phase1 = 0u;
     int cur_lag = -1;
     long long since_flush = 0;
     unsigned long long n_cand = 0, n_rech = 0;
     bool failed = false;
+    uint2 *const my_slots = slots + tid;
 
     for (long long item = it0; item < it1 && !failed; ++item) {
         int lag_idx, itile, k;
@@ -154,96 +311,93 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f32(const PairLaunch P)
         ++since_flush;
         const long long fo = P.primo + (long long)k * P.skip;
         const long long fl = fo + (long long)lag_idx * P.every;
-        const Box32 bx = P.box32[fo];
-
-        float xi[R32], yi[R32], zi[R32];
-        int ti[R32], ia[R32];
+        Box2 bx;
+        {
+            const Box32 b = P.box32[fo];
 #pragma unroll
-        for (int r = 0; r < R32; ++r) {
-            ia[r] = P.a0 + itile * TI32 + r * NT + tid;
-            if (ia[r] < P.a1) {
-                float4 p = P.pos32[fo * N + ia[r]];
-                xi[r] = p.x; yi[r] = p.y; zi[r] = p.z;
-                ti[r] = __float_as_int(p.w);
-            } else {
-                // no atom: NaN coordinates never pass d2 <= hi_f
-                xi[r] = yi[r] = zi[r] = __int_as_float(0x7fc00000);
-                ti[r] = 0;
+            for (int a = 0; a < 3; ++a) {
+                bx.invL[a] = f2pk(b.invL[a], b.invL[a]);
+                bx.negL[a] = f2pk(-b.L[a], -b.L[a]);
+                bx.negT[a] = f2pk(-b.tilt[a], -b.tilt[a]);
             }
         }
+        // first atoms of this item
+        const int ia0 = P.a0 + itile * TI32 + tid;
+        f2 xi[R32], yi[R32], zi[R32];
+        int ti[R32];
+        const float *fi = P.pos32 + fo * 3 * NP;
+#pragma unroll
+        for (int r = 0; r < R32; ++r) {
+            const int ia = ia0 + r * NT;
+            float x, y, z;
+            if (ia < P.a1) {
+                x = fi[ia]; y = fi[NP + ia]; z = fi[2 * NP + ia];
+                ti[r] = P.types8[ia];
+            } else {
+                // no atom: NaN never passes d2 <= hi_f nor the wrap check
+                x = y = z = __int_as_float(0x7fc00000);
+                ti[r] = 0;
+            }
+            xi[r] = f2pk(x, x); yi[r] = f2pk(y, y); zi[r] = f2pk(z, z);
+        }
 
-        const float4 *jsrc = P.pos32 + fl * N;
+        const float *fj = P.pos32 + fl * 3 * NP;
+        int cnt = 0;
         __syncthreads();  // previous item done with both buffers
         if (tid == 0) {
-            unsigned bytes = (unsigned)(min(TJ32, P.N) * sizeof(float4));
-            mbar_arrive_expect_tx(&bars[0], bytes);
-            bulk_g2s(jbuf, jsrc, bytes, &bars[0]);
+            const int tj = min(TJ32, P.N);
+            const unsigned fb = (unsigned)(((tj + 3) & ~3) * 4), tb = (unsigned)((tj + 15) & ~15);
+            mbar_arrive_expect_tx(&bars[0], 3 * fb + tb);
+            bulk_g2s(jx, fj, fb, &bars[0]);
+            bulk_g2s(jx + TJ32, fj + NP, fb, &bars[0]);
+            bulk_g2s(jx + 2 * TJ32, fj + 2 * NP, fb, &bars[0]);
+            bulk_g2s(jt, P.types8, tb, &bars[0]);
         }
         for (int c = 0; c < nchunks; ++c) {
             const int b = c & 1;
+            const int jbase = c * TJ32;
             if (tid == 0 && c + 1 < nchunks) {
-                int nxt = min(TJ32, P.N - (c + 1) * TJ32);
-                unsigned bytes = (unsigned)(nxt * sizeof(float4));
-                mbar_arrive_expect_tx(&bars[b ^ 1], bytes);
-                bulk_g2s(jbuf + (b ^ 1) * TJ32, jsrc + (long long)(c + 1) * TJ32, bytes,
-                         &bars[b ^ 1]);
+                const int nb = jbase + TJ32;
+                const int tj = min(TJ32, P.N - nb);
+                const unsigned fb = (unsigned)(((tj + 3) & ~3) * 4);
+                const unsigned tb = (unsigned)((tj + 15) & ~15);
+                float *dst = jx + (b ^ 1) * 3 * TJ32;
+                mbar_arrive_expect_tx(&bars[b ^ 1], 3 * fb + tb);
+                bulk_g2s(dst, fj + nb, fb, &bars[b ^ 1]);
+                bulk_g2s(dst + TJ32, fj + NP + nb, fb, &bars[b ^ 1]);
+                bulk_g2s(dst + 2 * TJ32, fj + 2 * NP + nb, fb, &bars[b ^ 1]);
+                bulk_g2s(jt + (b ^ 1) * TJ32, P.types8 + nb, tb, &bars[b ^ 1]);
             }
-            bool ok = mbar_wait_bounded(&bars[b], b ? phase1 : phase0);
+            const bool ok = mbar_wait_bounded(&bars[b], b ? phase1 : phase0);
             if (ok) { if (b) phase1 ^= 1u; else phase0 ^= 1u; }
             else atomicOr(sflag, 1);
             __syncthreads();
             if (*sflag) { failed = true; break; }
 
-            const int jbase = c * TJ32;
             const int tj = min(TJ32, P.N - jbase);
-            const float4 *jb = jbuf + b * TJ32;
-#pragma unroll 2
-            for (int jj = 0; jj < tj; ++jj) {
-                const float4 pj = jb[jj];
-#pragma unroll
-                for (int r = 0; r < R32; ++r) {
-                    float dx = __fsub_rn(xi[r], pj.x);
-                    float dy = __fsub_rn(yi[r], pj.y);
-                    float dz = __fsub_rn(zi[r], pj.z);
-                    bool wflag = false;
-                    if (TRI) {
-                        float kz = __fsub_rn(__fmaf_rn(dz, bx.invL[2], MAGIC), MAGIC);
-                        if (WCHK) wflag |= fabsf(__fmaf_rn(dz, bx.invL[2], -kz)) > P.wlim;
-                        dz = __fmaf_rn(-kz, bx.L[2], dz);
-                        dy = __fmaf_rn(-kz, bx.tilt[2], dy);
-                        dx = __fmaf_rn(-kz, bx.tilt[1], dx);
-                        float ky = __fsub_rn(__fmaf_rn(dy, bx.invL[1], MAGIC), MAGIC);
-                        if (WCHK) wflag |= fabsf(__fmaf_rn(dy, bx.invL[1], -ky)) > P.wlim;
-                        dy = __fmaf_rn(-ky, bx.L[1], dy);
-                        dx = __fmaf_rn(-ky, bx.tilt[0], dx);
-                        float kx = __fsub_rn(__fmaf_rn(dx, bx.invL[0], MAGIC), MAGIC);
-                        if (WCHK) wflag |= fabsf(__fmaf_rn(dx, bx.invL[0], -kx)) > P.wlim;
-                        dx = __fmaf_rn(-kx, bx.L[0], dx);
-                    } else {
-                        float kx = __fsub_rn(__fmaf_rn(dx, bx.invL[0], MAGIC), MAGIC);
-                        float ky = __fsub_rn(__fmaf_rn(dy, bx.invL[1], MAGIC), MAGIC);
-                        float kz = __fsub_rn(__fmaf_rn(dz, bx.invL[2], MAGIC), MAGIC);
-                        if (WCHK) {
-                            wflag |= fabsf(__fmaf_rn(dx, bx.invL[0], -kx)) > P.wlim;
-                            wflag |= fabsf(__fmaf_rn(dy, bx.invL[1], -ky)) > P.wlim;
-                            wflag |= fabsf(__fmaf_rn(dz, bx.invL[2], -kz)) > P.wlim;
-                        }
-                        dx = __fmaf_rn(-kx, bx.L[0], dx);
-                        dy = __fmaf_rn(-ky, bx.L[1], dy);
-                        dz = __fmaf_rn(-kz, bx.L[2], dz);
-                    }
-                    float d2 = __fmul_rn(dx, dx);
-                    d2 = __fmaf_rn(dy, dy, d2);
-                    d2 = __fmaf_rn(dz, dz, d2);
-                    if (d2 <= P.hi_f || (WCHK && wflag)) {
+            const float *bxp = jx + b * 3 * TJ32;
+            const unsigned char *btp = jt + b * TJ32;
+
+            // Bins every slot of this warp's lanes (all lanes take part; each
+            // processes its own slots), then empties them.
+            auto warp_flush = [&]() {
+                const int maxc = __reduce_max_sync(0xffffffffu, (unsigned)cnt);
+                for (int q = 0; q < maxc; ++q) {
+                    if (q < cnt) {
+                        const uint2 e = my_slots[q * NT];
+                        const float d2 = __uint_as_float(e.x);
+                        const int r = e.y & 3;
+                        const int jj = (e.y >> 2) & 0x1fff;
+                        const int ia = ia0 + r * NT;
                         const int ja = jbase + jj;
-                        const int tj_ = __float_as_int(pj.w);
-                        int ch = chtab[ti[r] * P.ntypes + tj_] + (ia[r] == ja ? half : 0);
-                        ++n_cand;
-                        bool need = WCHK && wflag;
+                        int t_i = ti[0];
+#pragma unroll
+                        for (int rr = 1; rr < R32; ++rr) t_i = (r == rr) ? ti[rr] : t_i;
+                        const int ch = chtab[t_i * P.ntypes + btp[jj]] + (ia == ja ? half : 0);
+                        bool need = WCHK && (e.y >> 31);
                         if (!need && d2 >= P.lo_f) {
-                            float rr = __fsqrt_rn(d2);
-                            int bi = __float2int_rd(__fmul_rn(__fsub_rn(rr, P.rmin_f), P.inv_dr_f));
+                            const float rr_ = __fsqrt_rn(d2);
+                            int bi = __float2int_rd(__fmul_rn(__fsub_rn(rr_, P.rmin_f), P.inv_dr_f));
                             bi = min(max(bi, 0), P.nbin - 1);
                             const float2 w = win[bi];
                             if (d2 >= w.x && d2 <= w.y) atomicAdd(hist + ch * P.nbin + bi, 1u);
@@ -251,13 +405,81 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f32(const PairLaunch P)
                         }
                         if (need) {
                             ++n_rech;
-                            recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, ia[r], ja, hist, ch,
-                                              P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err);
+                            const int slot = atomicAdd(rqn, 1);
+                            if (slot < QCAP) {
+                                rq[slot] = make_uint4((unsigned)ia, (unsigned)ja, (unsigned)ch, 0u);
+                            } else {
+                                recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, ia, ja, hist, ch,
+                                                  P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err);
+                            }
                         }
                     }
                 }
+                n_cand += cnt;
+                cnt = 0;
+            };
+
+            for (int jj = 0; jj < tj; jj += 4) {
+                const float4 X = *reinterpret_cast<const float4 *>(bxp + jj);
+                const float4 Y = *reinterpret_cast<const float4 *>(bxp + TJ32 + jj);
+                const float4 Z = *reinterpret_cast<const float4 *>(bxp + 2 * TJ32 + jj);
+                const f2 xa = f2pk(X.x, X.y), xb = f2pk(X.z, X.w);
+                const f2 ya = f2pk(Y.x, Y.y), yb = f2pk(Y.z, Y.w);
+                const f2 za = f2pk(Z.x, Z.y), zb = f2pk(Z.z, Z.w);
+#pragma unroll
+                for (int r = 0; r < R32; ++r) {
+                    unsigned wa = 0u, wb = 0u;
+                    const f2 da = pair2<TRI, WCHK>(xi[r], yi[r], zi[r], xa, ya, za, bx, P.wlim, &wa);
+                    const f2 db = pair2<TRI, WCHK>(xi[r], yi[r], zi[r], xb, yb, zb, bx, P.wlim, &wb);
+                    float d0, d1, d2v, d3;
+                    f2up(da, d0, d1);
+                    f2up(db, d2v, d3);
+                    const unsigned m0 = (unsigned)((jj << 2) | r);
+                    if (d0 <= hi_f || (WCHK && (wa & 1u))) {
+                        my_slots[cnt * NT] = make_uint2(__float_as_uint(d0), m0 | (WCHK && (wa & 1u) ? 0x80000000u : 0u));
+                        ++cnt;
+                    }
+                    if (d1 <= hi_f || (WCHK && (wa & 2u))) {
+                        my_slots[cnt * NT] = make_uint2(__float_as_uint(d1), (m0 + 4u) | (WCHK && (wa & 2u) ? 0x80000000u : 0u));
+                        ++cnt;
+                    }
+                    if (d2v <= hi_f || (WCHK && (wb & 1u))) {
+                        my_slots[cnt * NT] = make_uint2(__float_as_uint(d2v), (m0 + 8u) | (WCHK && (wb & 1u) ? 0x80000000u : 0u));
+                        ++cnt;
+                    }
+                    if (d3 <= hi_f || (WCHK && (wb & 2u))) {
+                        my_slots[cnt * NT] = make_uint2(__float_as_uint(d3), (m0 + 12u) | (WCHK && (wb & 2u) ? 0x80000000u : 0u));
+                        ++cnt;
+                    }
+                    if (__any_sync(0xffffffffu, cnt > SLOTS - 4)) warp_flush();
+                }
             }
+            if (__any_sync(0xffffffffu, cnt > 0)) warp_flush();
             __syncthreads();  // all reads of buffer b done before it is refilled
+            // drain the FP64 recheck queue when half full (uniform decision)
+            if (*rqn > QCAP / 2) {
+                const int n = min(*rqn, QCAP);
+                for (int q = tid; q < n; q += NT) {
+                    const uint4 e = rq[q];
+                    recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, (int)e.x, (int)e.y, hist,
+                                      (int)e.z, P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err);
+                }
+                __syncthreads();
+                if (tid == 0) *rqn = 0;
+                __syncthreads();
+            }
+        }
+        if (failed) break;
+        // end of item: the queue refers to this item's frames
+        {
+            const int n = min(*rqn, QCAP);
+            for (int q = tid; q < n; q += NT) {
+                const uint4 e = rq[q];
+                recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, (int)e.x, (int)e.y, hist,
+                                  (int)e.z, P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err);
+            }
+            __syncthreads();
+            if (tid == 0) *rqn = 0;
         }
     }
     if (failed) {
@@ -330,8 +552,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f64(const PairLaunch P)
             int a = vi[r] ? ia[r] : P.a0;
             const double *p = P.pos64 + (fo * N + a) * 3;
             xi[r] = p[0]; yi[r] = p[1]; zi[r] = p[2];
-            // type ids travel in the FP32 frame's w lane
-            ti[r] = __float_as_int(P.pos32[fo * N + a].w);
+            ti[r] = P.types8[a];
         }
         for (int jbase = 0; jbase < P.N; jbase += TJ64) {
             const int tj = min(TJ64, P.N - jbase);
@@ -339,7 +560,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f64(const PairLaunch P)
             for (int q = tid; q < tj; q += NT) {
                 const double *p = P.pos64 + (fl * N + jbase + q) * 3;
                 jx[q] = p[0]; jy[q] = p[1]; jz[q] = p[2];
-                jt[q] = __float_as_int(P.pos32[fl * N + jbase + q].w);
+                jt[q] = P.types8[jbase + q];
             }
             __syncthreads();
             for (int jj = 0; jj < tj; ++jj) {
@@ -362,7 +583,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f64(const PairLaunch P)
 }
 
 // ---------------------------------------------------------------------------
-// Frame residency: FP64 min/max per axis and FP64 AoS -> FP32 {x,y,z,type}
+// Frame residency: FP64 min/max per axis and FP64 AoS -> FP32 SoA
 // ---------------------------------------------------------------------------
 __global__ void k_minmax(const double *__restrict__ pos, size_t natoms_total, double *out,
                          unsigned *nonfinite)
@@ -397,19 +618,28 @@ __global__ void k_minmax(const double *__restrict__ pos, size_t natoms_total, do
     if (bad) atomicAdd(nonfinite, bad);
 }
 
+// [T][N][3] FP64 -> [T][3][NP] FP32 (x-cx | y-cy | z-cz), padding NaN; types -> u8.
 __global__ void k_convert(const double *__restrict__ pos, const int *__restrict__ types, size_t T,
-                          size_t N, double cx, double cy, double cz, float4 *__restrict__ out)
+                          size_t N, size_t NP, double cx, double cy, double cz,
+                          float *__restrict__ out, unsigned char *__restrict__ types8)
 {
-    size_t total = T * N;
-    for (size_t a = blockIdx.x * (size_t)blockDim.x + threadIdx.x; a < total;
-         a += (size_t)gridDim.x * blockDim.x) {
-        const double *p = pos + a * 3;
-        float4 v;
-        v.x = __double2float_rn(__dsub_rn(p[0], cx));
-        v.y = __double2float_rn(__dsub_rn(p[1], cy));
-        v.z = __double2float_rn(__dsub_rn(p[2], cz));
-        v.w = __int_as_float(types[a % N]);
-        out[a] = v;
+    const size_t total = T * NP;
+    const float qnan = __int_as_float(0x7fc00000);
+    for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < total;
+         g += (size_t)gridDim.x * blockDim.x) {
+        const size_t f = g / NP, a = g - f * NP;
+        float x = qnan, y = qnan, z = qnan;
+        if (a < N) {
+            const double *p = pos + (f * N + a) * 3;
+            x = __double2float_rn(__dsub_rn(p[0], cx));
+            y = __double2float_rn(__dsub_rn(p[1], cy));
+            z = __double2float_rn(__dsub_rn(p[2], cz));
+        }
+        float *o = out + f * 3 * NP;
+        o[a] = x;
+        o[NP + a] = y;
+        o[2 * NP + a] = z;
+        if (f == 0) types8[a] = (unsigned char)(a < N ? types[a] : 0);
     }
 }
 
@@ -434,13 +664,14 @@ int launch_minmax(const double *pos64, size_t natoms_total, double *d_out6, unsi
 }
 
 int launch_convert(const double *pos64, const int *types, size_t T, size_t N, double cx,
-                   double cy, double cz, float4 *pos32, cudaStream_t s)
+                   double cy, double cz, float *pos32, unsigned char *types8, cudaStream_t s)
 {
-    size_t total = T * N;
+    const size_t NP = padded_natoms(N);
+    size_t total = T * NP;
     int blocks = (int)((total + NT - 1) / NT);
     if (blocks > 152 * 16) blocks = 152 * 16;
     if (blocks < 1) blocks = 1;
-    k_convert<<<blocks, NT, 0, s>>>(pos64, types, T, N, cx, cy, cz, pos32);
+    k_convert<<<blocks, NT, 0, s>>>(pos64, types, T, N, NP, cx, cy, cz, pos32, types8);
     return cuda_ok(cudaGetLastError());
 }
 
@@ -455,12 +686,12 @@ int launch_zero_u64(unsigned long long *p, size_t n, cudaStream_t s)
 
 int pairs_smem_bytes(int kind, int nch, int nbin, int ntypes)
 {
-    size_t hist = (size_t)nch * nbin * 4, tab = (size_t)ntypes * ntypes * 2;
-    size_t b;
-    if (kind == 0) b = 2 * TJ32 * sizeof(float4) + 32 + (size_t)nbin * 8 + hist + tab;
-    else b = (size_t)TJ64 * (3 * 8 + 4) + hist + tab;
+    if (kind == 0) return F32Smem(nbin, nch, ntypes).total;
+    size_t b = (size_t)TJ64 * (3 * 8 + 4) + (size_t)nch * nbin * 4 + (size_t)ntypes * ntypes * 2;
     return (int)((b + 127) / 128 * 128);
 }
+
+int pairs_tile_atoms(int kind) { return kind == 0 ? TI32 : TI64; }
 
 template <typename K>
 static int launch_persistent(K kernel, const PairLaunch &P, int smem, int num_sms, cudaStream_t s)
