@@ -26,6 +26,7 @@ EXPORTED = [
     "gofr_output_size", "gofr_run", "gofr_run_device", "gofr_sync", "gofr_get_stats",
     "gofr_counts_to_buffer", "gofr_bin_thresholds", "gofr_batch_set",
     "gofr_batch_output_layout", "gofr_batch_run", "gofr_measure_peaks",
+    "gofr_run_f64_noalloc",
 ]
 
 
@@ -102,10 +103,13 @@ def load_library(path=None):
                                            ctypes.POINTER(ctypes.c_size_t)]
     L.gofr_batch_run.argtypes = [vp, ctypes.c_int, up]
     L.gofr_measure_peaks.argtypes = [ctypes.c_int, dp, dp]
+    L.gofr_run_f64_noalloc.argtypes = [vp, vp, ctypes.c_int, vp, ctypes.c_uint, ctypes.c_size_t,
+                                       ctypes.c_size_t, ctypes.POINTER(Params), vp, vp,
+                                       ctypes.c_char_p, ctypes.c_size_t]
     for name in ("gofr_ctx_create", "gofr_set_frames", "gofr_output_size", "gofr_run",
                  "gofr_run_device", "gofr_sync", "gofr_get_stats", "gofr_counts_to_buffer",
                  "gofr_bin_thresholds", "gofr_batch_set", "gofr_batch_output_layout",
-                 "gofr_batch_run", "gofr_measure_peaks"):
+                 "gofr_batch_run", "gofr_measure_peaks", "gofr_run_f64_noalloc"):
         getattr(L, name).restype = ctypes.c_int
     if path is None:
         _lib = L

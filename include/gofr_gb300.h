@@ -157,6 +157,35 @@ int gofr_bin_thresholds(double rmin, double rmax, unsigned nbin, double *th);
  * reference counterpart: the reference has no GPU path. */
 int gofr_measure_peaks(int device, double *fp32_lane_ops_per_s, double *smem_atomics_per_s);
 
+/* Allocation-free variant of the plain FP64 pair kernel.  No counterpart in
+ * the reference (whose calculation never touches a GPU).
+ *
+ * For callers that cannot call cudaMalloc: code running under a framework
+ * that owns all device memory through its own pool, a real-time loop that
+ * must not allocate, or a plug-in whose host has laid out every device byte
+ * already.  The caller passes its own DEVICE buffers: positions
+ * [nframes][natoms][3] and boxes [nframes][6 or 9] in the reference's internal
+ * format (as for gofr_set_frames), type ids [natoms] in 0..ntypes-1, and the
+ * output counts [leff][ntypes*(ntypes+1)][nbin] (zeroed here).  boxes is read
+ * on the device only.  The same exact counts as gofr_run with GOFR_KERNEL_F64.
+ *
+ * Nothing is allocated: the only scratch (channel table, error word) is a
+ * file-scope __device__ array of 768 bytes that every GPU loading this library
+ * holds until the process exits.  Limits: ntypes <= 16, nparts <= 1, and the
+ * shared-memory histogram of ntypes*(ntypes+1)*nbin u32 must fit one CTA.
+ * p->kernel is ignored.  Work runs on `stream` (a cudaStream_t; NULL = the
+ * legacy default stream) of the current device; the call waits for it and
+ * returns the kernel's error status.  The first call on a device resolves the
+ * scratch array's device address (cudaGetSymbolAddress): make that first
+ * call before any stream capture on that device.  All calls share the one
+ * scratch array, so calls that overlap on the GPU (several host threads or
+ * streams at once) race and must be serialised by the caller.  errbuf
+ * (optional, errlen bytes) receives the message of a failure. */
+int gofr_run_f64_noalloc(const double *d_positions, const double *d_boxes, int box_kind,
+                         const int *d_type_ids, unsigned ntypes, size_t natoms, size_t nframes,
+                         const gofr_params *p, unsigned long long *d_counts, void *stream,
+                         char *errbuf, size_t errlen);
+
 /* ---- batched trajectories (one persistent launch) --------------------- */
 
 /* Description of one trajectory of a batch.  Pointers are host buffers in
