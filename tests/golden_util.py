@@ -1,0 +1,24 @@
+"""Loading of the reference-generated fixtures in tests/golden/."""
+import glob
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    d = {k: z[k] for k in z.files if k != "meta"}
+    d["meta"] = json.loads(str(z["meta"]))
+    return d
+
+
+def incr(meta):
+    n, skip = meta["ntimesteps"], meta["skip"] or 1
+    return 1.0 / (n // skip) if n // skip > 0 else 1.0
