@@ -118,7 +118,8 @@ def build_host(force=False):
                      "-I", sysconfig.get_paths()["include"],
                      os.path.join(HOST, "pyanalisi.cpp"), os.path.join(HOST, "trajectory.cpp"),
                      "-o", mod] + link)
-    if os.path.exists(os.path.join(HOST, "analisi_main.cpp")) and (
+    if os.path.exists(os.path.join(HOST, "analisi_main.cpp")) and os.path.exists(
+            os.path.join(HOST, "lammps_file.cpp")) and (
             force or _stale(cli, host_srcs + [lib])):
         jobs.append([cxx] + common + [os.path.join(HOST, "analisi_main.cpp"),
                      os.path.join(HOST, "trajectory.cpp"), os.path.join(HOST, "lammps_file.cpp"),

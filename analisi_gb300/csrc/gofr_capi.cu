@@ -842,7 +842,7 @@ int gofr_counts_to_buffer(const unsigned long long *counts, size_t n, unsigned n
     if ((!counts || !out) && n) return GOFR_ERR_ARG;
     if (skip == 0) skip = 1;
     const double incr = (ntimesteps / skip > 0) ? 1.0 / (int)(ntimesteps / skip) : 1.0;
-    if (nparts <= 1) {
+    if (nparts == 0) {
         for (size_t i = 0; i < n; ++i) out[i] = (double)counts[i] * incr;
         return GOFR_OK;
     }

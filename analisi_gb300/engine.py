@@ -147,12 +147,14 @@ def bin_thresholds(rmin, rmax, nbin):
     return th
 
 
-def counts_to_buffer(counts, ntimesteps, skip, nparts=1):
-    """The reference's double result buffer from counts (host code).  With
-    nparts > 1, counts is [nparts][...] and the result is the exact thread fold."""
+def counts_to_buffer(counts, ntimesteps, skip, nparts=0):
+    """The reference's double result buffer from counts (host code).
+    nparts >= 1: counts is [nparts][...] per reference thread partition and the
+    result is the reference's exact value (sequential incr sums, folded in
+    thread order).  nparts == 0: counts are totals, result counts*incr."""
     L = load_library()
     c = np.ascontiguousarray(counts, dtype=np.uint64)
-    shape = c.shape[1:] if nparts > 1 else c.shape
+    shape = c.shape[1:] if nparts >= 1 else c.shape
     n = int(np.prod(shape))
     out = np.zeros(shape, dtype=np.float64)
     rc = L.gofr_counts_to_buffer(c.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)), n,

@@ -1,0 +1,200 @@
+// Python module `pyanalisi` of analisi_gb300: the reference's Gofrt path API
+// (pyanalisi/src/pyanalisi.cpp:67-82 for Gofrt, :487-532 for Trajectory and
+// BoxFormat) with the GB300 engine behind it.
+//
+//   import pyanalisi        # analisi_gb300/_build on sys.path
+//   t = pyanalisi.Trajectory(pos, vel, types, box, pyanalisi.BoxFormat.CellVectors, False, False)
+//   g = pyanalisi.Gofrt(t, rmin, rmax, nbin, tmax, nthreads, skip, every, debug)
+//   g.reset(n); g.calculate(primo); a = np.array(g, copy=True)
+//
+// Argument checks and their messages follow lib/src/trajectory_numpy.cpp:20-118.
+#include <pybind11/numpy.h>
+#include <pybind11/pybind11.h>
+#include <pybind11/stl.h>
+
+#include <cstring>
+#include <memory>
+
+#include "gofrt.h"
+#include "trajectory.h"
+
+namespace py = pybind11;
+using analisi_gb300::BoxFormat;
+using analisi_gb300::Trajectory;
+using GofrtT = analisi_gb300::Gofrt<double, Trajectory>;
+
+namespace {
+
+template <typename T>
+bool has_no_stride(const py::buffer_info &b)
+{
+    ssize_t stride = sizeof(T);
+    for (int i = (int)b.ndim - 1; i >= 0; --i) {
+        if (b.strides[i] != stride) return false;
+        stride *= b.shape[i];
+    }
+    return true;
+}
+
+std::unique_ptr<Trajectory> make_trajectory(py::buffer pos, py::buffer vel, py::buffer types,
+                                            py::buffer box, BoxFormat fmt, bool wrap,
+                                            bool save_rot)
+{
+    py::buffer_info ip = pos.request(), iv = vel.request(), it = types.request(),
+                    ib = box.request();
+    if (ip.ndim != 3) throw std::runtime_error("Wrong number of dimension of position array (must be 3)");
+    if (iv.ndim != 3) throw std::runtime_error("Wrong number of dimension of velocities array (must be 3)");
+    if (ip.shape[2] != 3)
+        throw std::runtime_error("Wrong number of cartesian components in the third dimension of positions array");
+    if (iv.shape[2] != 3)
+        throw std::runtime_error("Wrong number of cartesian components in the third dimension of velocities array");
+    for (int i = 0; i < 3; ++i)
+        if (ip.shape[i] != iv.shape[i])
+            throw std::runtime_error("Shape of positions and velocities array is different");
+    if (it.ndim != 1) throw std::runtime_error("Wrong number of dimension of types array (must be 1)");
+    if (it.shape[0] != ip.shape[1]) throw std::runtime_error("Wrong size of the type array");
+    if (fmt == BoxFormat::Cell_vectors) {
+        if (ib.ndim != 3)
+            throw std::runtime_error("Wrong number of dimensions of box array (must be 3) for cell matrix format");
+        if (ib.shape[0] != ip.shape[0] || ib.shape[1] != 3 || ib.shape[2] != 3)
+            throw std::runtime_error("Wrong shape of box array: must be (nsteps, 3, 3) for matrix format");
+    } else {
+        if (ib.ndim != 2)
+            throw std::runtime_error("Wrong number of dimensions of box array (must be 2 for lammps ortho/triclinic cell format)");
+        if (ib.shape[0] != ip.shape[0])
+            throw std::runtime_error("Wrong shape of box array: first dimension must be nsteps");
+        if (fmt == BoxFormat::Lammps_ortho && ib.shape[1] != 6)
+            throw std::runtime_error("Wrong shape of box array: must be (:, 6) for orthogonal lammps cell format");
+        if (fmt == BoxFormat::Lammps_triclinic && ib.shape[1] != 9)
+            throw std::runtime_error("Wrong shape of box array: must be (:, 9) for triclinic lammps cell format");
+    }
+    if (ib.format != py::format_descriptor<double>::format())
+        throw std::runtime_error("Format of box array should be double");
+    if (it.format != py::format_descriptor<int>::format())
+        throw std::runtime_error("Format of types array should be int (" +
+                                 py::format_descriptor<int>::format() + ") while it was " +
+                                 it.format);
+    if (iv.format != py::format_descriptor<double>::format())
+        throw std::runtime_error("Format of velocities array should be double");
+    if (ip.format != py::format_descriptor<double>::format())
+        throw std::runtime_error("Format of positions array should be double");
+    if (!has_no_stride<double>(ib)) throw std::runtime_error("Unsupported stride in box array");
+    if (!has_no_stride<int>(it)) throw std::runtime_error("Unsupported stride in types array");
+    if (!has_no_stride<double>(iv)) throw std::runtime_error("Unsupported stride in vel array");
+    if (!has_no_stride<double>(ip)) throw std::runtime_error("Unsupported stride in pos array");
+    if (fmt == BoxFormat::Invalid) throw std::runtime_error("Invalid input cell format");
+    return std::make_unique<Trajectory>(
+        static_cast<const double *>(ip.ptr), static_cast<const double *>(iv.ptr),
+        static_cast<const int *>(it.ptr), static_cast<const double *>(ib.ptr),
+        (size_t)ip.shape[0], (size_t)ip.shape[1], fmt, wrap, save_rot);
+}
+
+py::array_t<double> copy3(const double *p, size_t a, size_t b, size_t c)
+{
+    py::array_t<double> out({a, b, c});
+    if (a * b * c) std::memcpy(out.mutable_data(), p, sizeof(double) * a * b * c);
+    return out;
+}
+
+}  // namespace
+
+PYBIND11_MODULE(pyanalisi, m)
+{
+    m.doc() = "analisi's Gofrt (van Hove g(r,t)) on the GB300 engine";
+
+    py::enum_<BoxFormat>(m, "BoxFormat", py::arithmetic())
+        .value("Invalid", BoxFormat::Invalid)
+        .value("CellVectors", BoxFormat::Cell_vectors)
+        .value("LammpsOrtho", BoxFormat::Lammps_ortho)
+        .value("LammpsTriclinic", BoxFormat::Lammps_triclinic);
+
+    py::class_<Trajectory>(m, "Trajectory")
+        .def(py::init(&make_trajectory), py::arg("positions"), py::arg("velocities"),
+             py::arg("types"), py::arg("box"), py::arg("box_format") = BoxFormat::Cell_vectors,
+             py::arg("wrap") = false, py::arg("save_rotation_matrix") = false,
+             R"doc(Parameters
+----------
+positions (double) array (ntimesteps, natoms, 3)
+velocities (double) array (ntimesteps, natoms, 3)
+types (int) array (natoms)
+box (double): (ntimesteps, 3, 3) cell vectors as columns, or (ntimesteps, 6|9) lammps rows
+format of the box (BoxFormat)
+wrap atoms inside the cell using pbc
+save rotation matrix if triclinic format is used and a rotation is needed)doc")
+        .def("get_positions_copy", [](Trajectory &t) {
+            return copy3(t.positions_data(), t.get_ntimesteps(), t.get_natoms(), 3);
+        })
+        .def("get_velocities_copy", [](Trajectory &t) {
+            if (!t.velocity_data()) return py::array_t<double>();
+            return copy3(t.velocity_data(), t.get_ntimesteps(), t.get_natoms(), 3);
+        })
+        .def("get_box_copy", [](Trajectory &t) {
+            py::array_t<double> out({t.get_ntimesteps(), t.get_box_stride()});
+            std::memcpy(out.mutable_data(), t.box(0),
+                        sizeof(double) * t.get_ntimesteps() * t.get_box_stride());
+            return out;
+        })
+        .def("get_rotation_matrix", [](Trajectory &t) {
+            const auto &r = t.rotation_matrix();
+            if (r.empty()) return py::array_t<double>();
+            return copy3(r.data(), t.get_ntimesteps(), 3, 3);
+        })
+        .def("get_type", &Trajectory::get_type, "get the type used for the internal representation")
+        .def("get_type_ids", [](Trajectory &t) {
+            py::array_t<int> out(t.get_natoms());
+            std::memcpy(out.mutable_data(), t.type_ids(), sizeof(int) * t.get_natoms());
+            return out;
+        })
+        .def("get_ntypes", &Trajectory::get_ntypes)
+        .def("get_natoms", &Trajectory::get_natoms)
+        .def("is_triclinic", &Trajectory::is_triclinic)
+        .def("get_nloaded_timesteps", &Trajectory::get_nloaded_timesteps)
+        .def("getNtimesteps", &Trajectory::get_ntimesteps)
+        .def("get_current_timestep", [](Trajectory &) { return (ssize_t)0; })
+        .def("getWrapPbc", &Trajectory::get_pbc_wrap);
+
+    py::class_<GofrtT>(m, "Gofrt", py::buffer_protocol())
+        .def(py::init<Trajectory *, double, double, unsigned int, unsigned int, unsigned int,
+                      unsigned int, unsigned int, bool>(),
+             py::arg("trajectory"), py::arg("rmin"), py::arg("rmax"), py::arg("nbin"),
+             py::arg("tmax") = 0, py::arg("nthreads") = 0, py::arg("skip") = 1,
+             py::arg("every") = 1, py::arg("debug") = false, py::keep_alive<1, 2>(),
+             R"doc(calculates g(r) and, in general, g(r,t) on the GPU
+
+Parameters
+----------
+Trajectory instance, rmin, rmax, nbin, maximum time lag, number of threads
+(the reference's atom split; its per-thread sums are reproduced exactly),
+time skip, every time, debug flag)doc")
+        .def("reset", &GofrtT::reset)
+        .def("getNumberOfExtraTimestepsNeeded", &GofrtT::nExtraTimesteps)
+        .def("calculate", [](GofrtT &g, size_t primo) {
+            py::gil_scoped_release release;
+            g.calculate(primo);
+        })
+        .def("get_columns_description", &GofrtT::get_columns_description)
+        .def("set_kernel", &GofrtT::set_kernel,
+             "0 auto (FP32 + FP64 edge recheck), 1 FP32 forced, 2 plain FP64")
+        .def("last_stats", [](GofrtT &g) {
+            gofr_stats s = g.last_stats();
+            py::dict d;
+            d["pairs"] = s.pairs;
+            d["evaluated"] = s.evaluated;
+            d["candidates"] = s.candidates;
+            d["rechecks"] = s.rechecks;
+            d["kernel_ms"] = s.kernel_ms;
+            d["total_ms"] = s.total_ms;
+            d["kernel_used"] = s.kernel_used;
+            d["wrap_checked"] = s.wrap_checked;
+            d["err_bound_d2"] = s.err_bound_d2;
+            return d;
+        })
+        .def_buffer([](GofrtT &g) -> py::buffer_info {
+            return py::buffer_info(g.access_vdata(), sizeof(double),
+                                   py::format_descriptor<double>::format(), g.get_shape().size(),
+                                   g.get_shape(), g.get_stride());
+        });
+
+    m.def("info", []() { return std::string("analisi_gb300: Gofrt on GB300 (sm_103a)"); });
+    m.def("has_mmap", []() { return false; });
+}

@@ -35,8 +35,11 @@ def lammps_to_internal(box_lammps):
 
 
 def dense_type_ids(types):
-    u = np.unique(types)
-    return np.searchsorted(u, types).astype(np.int32), len(u)
+    """Dense ids in the order of the raw labels compared as unsigned integers
+    (lib/src/basetrajectory.cpp:60-79 sorts a std::vector<unsigned int>)."""
+    t = np.asarray(types).astype(np.int64) & 0xFFFFFFFF
+    u = np.unique(t)
+    return np.searchsorted(u, t).astype(np.int32), len(u)
 
 
 def random_walk(seed, N, T, L, sigma, counts, triclinic_tilt=None, wrap_into_cell=False,

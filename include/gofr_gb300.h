@@ -134,11 +134,12 @@ int gofr_sync(gofr_ctx *ctx);
 /* Statistics of the last completed run. */
 int gofr_get_stats(const gofr_ctx *ctx, gofr_stats *out);
 
-/* Converts counts to the reference's double result buffer: out[i] =
- * counts[i] * incr, with incr = 1/int(ntimesteps/skip) (gofrt.cpp:91-92).
- * When nparts > 1 the counts are per partition and the result is the
- * reference's exact thread fold (gofrt.cpp:118,128-132): each partition's
- * value is incr added count times in sequence, partitions summed in order.
+/* Converts counts to the reference's double result buffer, with
+ * incr = 1/int(ntimesteps/skip) (gofrt.cpp:91-92).  nparts >= 1: counts are
+ * [nparts][n] per reference thread partition and the result is the
+ * reference's exact value: each partition's bin is incr added count times in
+ * sequence (gofrt.cpp:118), partitions folded in order (gofrt.cpp:128-132).
+ * nparts == 0: counts are [n] totals and out[i] = counts[i] * incr.
  * n is the number of doubles (leff*nch*nbin). */
 int gofr_counts_to_buffer(const unsigned long long *counts, size_t n, unsigned nparts,
                           unsigned ntimesteps, unsigned skip, double *out);

@@ -83,8 +83,11 @@ def test_exact_thread_fold(built_engine, oracle_mod, nts, skip):
     a = engine.counts_to_buffer(c, nts, skip, nparts=4)
     b = oracle_mod.fold_buffer(c, oracle_mod.incr(nts, skip))
     assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
-    t = engine.counts_to_buffer(c[0], nts, skip, nparts=1)
+    t = engine.counts_to_buffer(c[0], nts, skip, nparts=0)
     assert np.array_equal(t, c[0].astype(np.float64) * oracle_mod.incr(nts, skip))
+    one = engine.counts_to_buffer(c[:1], nts, skip, nparts=1)
+    assert np.array_equal(one.view(np.uint64),
+                          oracle_mod.fold_buffer(c[:1], oracle_mod.incr(nts, skip)).view(np.uint64))
 
 
 def test_exact_fold_large_counts(built_engine):
@@ -95,8 +98,10 @@ def test_exact_fold_large_counts(built_engine):
         s = 0.0
         for _ in range(k):
             s += inc
-        got = engine.counts_to_buffer(np.array([[k]], dtype=np.uint64), 1800, 4, nparts=1)
+        got = engine.counts_to_buffer(np.array([[k]], dtype=np.uint64), 1800, 4, nparts=0)
         assert got[0, 0] == k * inc
+        one = engine.counts_to_buffer(np.array([[[k]]], dtype=np.uint64), 1800, 4, nparts=1)
+        assert one[0, 0] == s, k
         got2 = engine.counts_to_buffer(np.array([[[k]], [[0]]], dtype=np.uint64), 1800, 4,
                                        nparts=2)
         assert got2[0, 0] == s, k

@@ -93,6 +93,7 @@ def test_partition_counts_and_exact_buffer(gpu_engine, oracle_mod):
     np.testing.assert_array_equal(got, ref)
     p = w["params"]
     buf = engine.counts_to_buffer(got, p["ntimesteps"], p["skip"], nparts=3)
+    assert buf.shape == got.shape[1:]
     obuf = oracle_mod.fold_buffer(ref, oracle_mod.incr(p["ntimesteps"], p["skip"]))
     assert np.array_equal(buf.view(np.uint64), obuf.view(np.uint64))
 
