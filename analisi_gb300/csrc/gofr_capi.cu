@@ -77,6 +77,23 @@ struct gofr_ctx {
     gofr_stats stats{};
     size_t batch_total = 0;
     unsigned long long launches = 0;  // kernels launched on this context
+    // batched trajectories (gofr_batch_set / gofr_batch_run)
+    struct Batch {
+        std::vector<PairLaunch> launches;       // one per trajectory (FP32 path)
+        std::vector<WorkDesc> work[2];          // descriptors, orthorhombic / triclinic
+        std::vector<int> f64_trajs;             // trajectories that need the FP64 kernel
+        int max_nbin = 1, max_nch = 1, max_ntypes = 1;
+        PairLaunch *d_launches = nullptr;
+        WorkDesc *d_work[2] = {nullptr, nullptr};
+        unsigned *d_head = nullptr;             // queue heads [2]
+        float2 *d_win = nullptr;
+        unsigned short *d_chtab = nullptr;
+        unsigned long long *h_stage = nullptr;  // pinned copy of the counts
+        unsigned long long *d_counts = nullptr; // concatenated counts of every trajectory
+        unsigned long long pairs = 0;
+        int grid[2] = {0, 0};
+        cudaGraphExec_t graph = nullptr;
+    } batch;
 };
 
 // ---------------------------------------------------------------------------
@@ -658,6 +675,192 @@ int run_common(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_d
     return GOFR_OK;
 }
 
+void free_batch(gofr_ctx *ctx)
+{
+    auto &B = ctx->batch;
+    if (B.graph) cudaGraphExecDestroy(B.graph);
+    cudaFree(B.d_launches);
+    cudaFree(B.d_work[0]);
+    cudaFree(B.d_work[1]);
+    cudaFree(B.d_head);
+    cudaFree(B.d_win);
+    cudaFree(B.d_chtab);
+    cudaFree(B.d_counts);
+    if (B.h_stage) cudaFreeHost(B.h_stage);
+    B = gofr_ctx::Batch{};
+}
+
+// Plans every trajectory of the batch and lays out the device work queue:
+// descriptors of about `target` pairs (never more than 2^31, so no u32
+// shared-memory bin can overflow before the flush that ends a descriptor),
+// sorted by decreasing cost so the persistent CTAs finish together.
+int build_batch(gofr_ctx *ctx)
+{
+    auto &B = ctx->batch;
+    const int TI = pairs_tile_atoms(0);
+    std::vector<float2> wins;
+    std::vector<unsigned short> tabs;
+    std::vector<size_t> win_off(ctx->trajs.size(), 0), tab_off(ctx->trajs.size(), 0);
+    unsigned long long total = 0;
+    std::vector<Plan> plans(ctx->trajs.size());
+    std::vector<RunShape> shapes(ctx->trajs.size());
+    for (size_t k = 0; k < ctx->trajs.size(); ++k) {
+        TrajDev &t = ctx->trajs[k];
+        gofr_params p = t.params;
+        p.kernel = GOFR_KERNEL_AUTO;
+        p.nparts = 1;
+        int rc = shape_of(ctx, t, p, shapes[k]);
+        if (rc) return rc;
+        rc = make_plan(ctx, t, p, plans[k]);
+        if (rc) return rc;
+        total += (unsigned long long)shapes[k].n_lags * shapes[k].n_orig * t.N * t.N;
+    }
+    B.pairs = total;
+    const unsigned long long target =
+        std::max<unsigned long long>(total / ((unsigned long long)ctx->num_sms * 2 * 24), 1ull << 24);
+    struct Cost { unsigned long long c; WorkDesc w; bool tri; };
+    std::vector<Cost> all;
+    B.launches.resize(ctx->trajs.size());
+    for (size_t k = 0; k < ctx->trajs.size(); ++k) {
+        TrajDev &t = ctx->trajs[k];
+        const RunShape &rs = shapes[k];
+        const Plan &pl = plans[k];
+        if (pl.empty || rs.n_lags == 0 || rs.n_orig == 0) continue;
+        if (pl.kind != 0) { B.f64_trajs.push_back((int)k); continue; }
+        win_off[k] = wins.size();
+        wins.insert(wins.end(), pl.w.win.begin(), pl.w.win.end());
+        std::vector<unsigned short> tab = channel_table(t.ntypes);
+        tab_off[k] = tabs.size();
+        tabs.insert(tabs.end(), tab.begin(), tab.end());
+        B.max_nbin = std::max(B.max_nbin, (int)t.params.nbin);
+        B.max_nch = std::max(B.max_nch, (int)rs.nch);
+        B.max_ntypes = std::max(B.max_ntypes, (int)t.ntypes);
+        const int n_itiles = (int)((t.N + TI - 1) / TI);
+        for (unsigned l = 0; l < rs.n_lags; ++l)
+            for (int it = 0; it < n_itiles; ++it) {
+                const unsigned long long tile = std::min<size_t>(TI, t.N - (size_t)it * TI);
+                const unsigned long long per_item = tile * t.N;
+                unsigned long long chunk = std::max<unsigned long long>(1, target / per_item);
+                chunk = std::min<unsigned long long>(chunk, std::max<unsigned long long>(
+                                                                1, (1ull << 31) / per_item));
+                for (unsigned k0 = 0; k0 < rs.n_orig; k0 += (unsigned)chunk) {
+                    const unsigned k1 = (unsigned)std::min<unsigned long long>(k0 + chunk, rs.n_orig);
+                    WorkDesc w{(int)k, (int)l, it, (int)k0, (int)k1, 0, 0, 0};
+                    all.push_back({(k1 - k0) * per_item, w, t.tric != 0});
+                }
+            }
+    }
+    std::stable_sort(all.begin(), all.end(), [](const Cost &a, const Cost &b) { return a.c > b.c; });
+    for (auto &c : all) B.work[c.tri ? 1 : 0].push_back(c.w);
+    CK(cudaMalloc(&B.d_win, std::max<size_t>(wins.size(), 1) * sizeof(float2)));
+    CK(cudaMalloc(&B.d_chtab, std::max<size_t>(tabs.size(), 1) * sizeof(unsigned short)));
+    if (!wins.empty())
+        CK(cudaMemcpy(B.d_win, wins.data(), wins.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    if (!tabs.empty())
+        CK(cudaMemcpy(B.d_chtab, tabs.data(), tabs.size() * sizeof(unsigned short),
+                      cudaMemcpyHostToDevice));
+    for (size_t k = 0; k < ctx->trajs.size(); ++k) {
+        TrajDev &t = ctx->trajs[k];
+        const RunShape &rs = shapes[k];
+        const Plan &pl = plans[k];
+        PairLaunch &L = B.launches[k];
+        L = PairLaunch{};
+        if (pl.kind != 0 || pl.empty) continue;
+        L.pos32 = t.pos32;
+        L.types8 = t.types8;
+        L.pos64 = t.pos64;
+        L.box64 = t.box64;
+        L.box32 = t.box32;
+        L.win = B.d_win + win_off[k];
+        L.chtab = B.d_chtab + tab_off[k];
+        L.counts = B.d_counts + t.out_offset;
+        L.err = ctx->d_err;
+        L.stats = ctx->d_stats;
+        L.N = (int)t.N;
+        L.NP = (int)padded_natoms(t.N);
+        L.nbin = (int)t.params.nbin;
+        L.nch = (int)rs.nch;
+        L.ntypes = (int)t.ntypes;
+        L.a0 = 0;
+        L.a1 = (int)t.N;
+        L.n_lags = (int)rs.n_lags;
+        L.every = (int)rs.every;
+        L.n_orig = (int)rs.n_orig;
+        L.skip = (int)rs.skip;
+        L.primo = (long long)t.params.primo;
+        L.n_itiles = (int)((t.N + TI - 1) / TI);
+        BinMap bm(t.params.rmin, t.params.rmax, t.params.nbin);
+        L.rmin = bm.rmin; L.rmax = bm.rmax; L.dr = bm.dr; L.rmin2 = bm.rmin2; L.rmax2 = bm.rmax2;
+        L.hi_f = pl.w.hi_f;
+        L.lo_f = pl.w.lo_f;
+        L.rmin_f = (float)t.params.rmin;
+        L.inv_dr_f = (float)(1.0 / bm.dr);
+        L.wlim = (float)(0.5 - pl.b.eta);
+        L.tric = t.tric;
+        L.wchk = pl.wrapcheck ? 1 : 0;
+    }
+    CK(cudaMalloc(&B.d_launches, std::max<size_t>(B.launches.size(), 1) * sizeof(PairLaunch)));
+    CK(cudaMemcpy(B.d_launches, B.launches.data(), B.launches.size() * sizeof(PairLaunch),
+                  cudaMemcpyHostToDevice));
+    for (int v = 0; v < 2; ++v) {
+        if (B.work[v].empty()) continue;
+        CK(cudaMalloc(&B.d_work[v], B.work[v].size() * sizeof(WorkDesc)));
+        CK(cudaMemcpy(B.d_work[v], B.work[v].data(), B.work[v].size() * sizeof(WorkDesc),
+                      cudaMemcpyHostToDevice));
+    }
+    CK(cudaMalloc(&B.d_head, 2 * sizeof(unsigned)));
+    CK(cudaMallocHost(&B.h_stage, std::max<size_t>(ctx->batch_total, 1) * sizeof(unsigned long long)));
+    const int smem = batch_smem_bytes(B.max_nbin, B.max_nch, B.max_ntypes);
+    int max_smem = 0;
+    CK(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    if (smem > max_smem)
+        return fail(ctx, GOFR_ERR_UNSUPPORTED, "batch histograms need %d B of shared memory", smem);
+    for (int v = 0; v < 2; ++v) {
+        if (B.work[v].empty()) continue;
+        if (prepare_batch(B.max_nbin, B.max_nch, B.max_ntypes, v == 1, ctx->num_sms,
+                          (int)B.work[v].size(), &B.grid[v]))
+            return fail(ctx, GOFR_ERR_CUDA, "batched kernel setup failed");
+    }
+    return GOFR_OK;
+}
+
+// The launch sequence of one batch run (captured into a graph or issued directly).
+int enqueue_batch(gofr_ctx *ctx)
+{
+    auto &B = ctx->batch;
+    CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_stats, 0, ST_COUNT * sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(B.d_head, 0, 2 * sizeof(unsigned), ctx->stream));
+    CK(cudaMemsetAsync(B.d_counts, 0, std::max<size_t>(ctx->batch_total, 1) * 8, ctx->stream));
+    for (int v = 0; v < 2; ++v) {
+        if (B.work[v].empty()) continue;
+        ++ctx->launches;
+        if (launch_batch_grid(B.d_launches, B.d_work[v], (int)B.work[v].size(), B.d_head + v,
+                              B.max_nbin, B.max_nch, B.max_ntypes, v == 1, ctx->d_err,
+                              ctx->d_stats, B.grid[v], ctx->stream))
+            return fail(ctx, GOFR_ERR_CUDA, "batched kernel launch failed: %s",
+                        cudaGetErrorString(cudaGetLastError()));
+    }
+    for (int k : B.f64_trajs) {
+        TrajDev &t = ctx->trajs[k];
+        gofr_params p = t.params;
+        p.kernel = GOFR_KERNEL_F64;
+        p.nparts = 1;
+        RunShape rs;
+        int rc = shape_of(ctx, t, p, rs);
+        if (rc) return rc;
+        Plan pl;
+        rc = make_plan(ctx, t, p, pl);
+        if (rc) return rc;
+        unsigned long long pairs = 0;
+        rc = enqueue_run(ctx, t, p, rs, pl, B.d_counts + t.out_offset, &pairs);
+        if (rc) return rc;
+    }
+    CK(cudaMemcpyAsync(B.h_stage, B.d_counts, ctx->batch_total * 8, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    return GOFR_OK;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -707,6 +910,7 @@ void gofr_ctx_destroy(gofr_ctx *ctx)
         DevGuard g(ctx->device);
         if (ctx->stream) cudaStreamSynchronize(ctx->stream);
         for (auto &t : ctx->trajs) free_traj(t);
+        free_batch(ctx);
         cudaFree(ctx->d_counts);
         cudaFree(ctx->d_win);
         cudaFree(ctx->d_chtab);
@@ -733,6 +937,7 @@ int gofr_set_frames(gofr_ctx *ctx, const double *positions, const double *boxes,
     if (!ctx) return GOFR_ERR_ARG;
     DevGuard g(ctx->device);
     for (auto &t : ctx->trajs) free_traj(t);
+    free_batch(ctx);
     ctx->trajs.clear();
     ctx->trajs.emplace_back();
     int rc = upload_traj(ctx, ctx->trajs[0], positions, boxes, box_kind, type_ids, ntypes, natoms,
@@ -854,13 +1059,14 @@ int gofr_counts_to_buffer(const unsigned long long *counts, size_t n, unsigned n
     return GOFR_OK;
 }
 
-// ---- batch: v1 runs the trajectories one launch each (see gofr_batch_run) --
+// ---- batched trajectories ----------------------------------------------
 int gofr_batch_set(gofr_ctx *ctx, const gofr_traj_desc *trajs, unsigned ntraj)
 {
     if (!ctx) return GOFR_ERR_ARG;
     if (!trajs || ntraj == 0) return fail(ctx, GOFR_ERR_ARG, "empty batch");
     DevGuard g(ctx->device);
     for (auto &t : ctx->trajs) free_traj(t);
+    free_batch(ctx);
     ctx->trajs.clear();
     ctx->trajs.resize(ntraj);
     size_t off = 0;
@@ -884,6 +1090,17 @@ int gofr_batch_set(gofr_ctx *ctx, const gofr_traj_desc *trajs, unsigned ntraj)
         }
     }
     ctx->batch_total = off;
+    int rc = GOFR_OK;
+    if (cudaMalloc(&ctx->batch.d_counts, std::max<size_t>(off, 1) * 8) != cudaSuccess)
+        rc = fail(ctx, GOFR_ERR_NOMEM, "cannot allocate the batch counts");
+    if (rc == GOFR_OK) rc = build_batch(ctx);
+    if (rc) {
+        std::string m = ctx->err;
+        free_batch(ctx);
+        for (auto &t : ctx->trajs) free_traj(t);
+        ctx->trajs.clear();
+        return fail(ctx, rc, "%s", m.c_str());
+    }
     return GOFR_OK;
 }
 
@@ -897,43 +1114,53 @@ int gofr_batch_output_layout(const gofr_ctx *ctx, unsigned k, size_t *offset, si
 
 int gofr_batch_run(gofr_ctx *ctx, int use_graph, unsigned long long *counts_host)
 {
-    (void)use_graph;
     if (!ctx) return GOFR_ERR_ARG;
     if (!counts_host) return fail(ctx, GOFR_ERR_ARG, "null output buffer");
-    if (ctx->trajs.empty()) return fail(ctx, GOFR_ERR_STATE, "no batch uploaded");
+    if (ctx->trajs.empty() || !ctx->batch.h_stage)
+        return fail(ctx, GOFR_ERR_STATE, "no batch uploaded");
     DevGuard g(ctx->device);
-    int rc = ensure(ctx, ctx->d_counts, ctx->cap_counts, ctx->batch_total);
-    if (rc) return rc;
+    auto &B = ctx->batch;
+    if (use_graph && !B.graph) {
+        cudaGraph_t graph = nullptr;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        const unsigned long long launches_before = ctx->launches;
+        int rc = enqueue_batch(ctx);
+        cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+        ctx->launches = launches_before;
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (e != cudaSuccess)
+            return fail(ctx, GOFR_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&B.graph, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            B.graph = nullptr;
+            return fail(ctx, GOFR_ERR_CUDA, "graph instantiation failed: %s",
+                        cudaGetErrorString(e));
+        }
+    }
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
-    CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), ctx->stream));
-    CK(cudaMemsetAsync(ctx->d_stats, 0, ST_COUNT * sizeof(unsigned long long), ctx->stream));
-    CK(cudaMemsetAsync(ctx->d_counts, 0, std::max<size_t>(ctx->batch_total, 1) * 8, ctx->stream));
     CK(cudaEventRecord(ctx->ev[1], ctx->stream));
-    unsigned long long pairs_total = 0;
-    for (auto &t : ctx->trajs) {
-        gofr_params p = t.params;
-        p.kernel = GOFR_KERNEL_AUTO;
-        p.nparts = 1;
-        RunShape rs;
-        rc = shape_of(ctx, t, p, rs);
+    if (use_graph) {
+        CK(cudaGraphLaunch(B.graph, ctx->stream));
+        ctx->launches += (B.work[0].empty() ? 0 : 1) + (B.work[1].empty() ? 0 : 1) +
+                         B.f64_trajs.size();
+    } else {
+        int rc = enqueue_batch(ctx);
         if (rc) return rc;
-        Plan pl;
-        rc = make_plan(ctx, t, p, pl);
-        if (rc) return rc;
-        unsigned long long pairs = 0;
-        rc = enqueue_run(ctx, t, p, rs, pl, ctx->d_counts + t.out_offset, &pairs);
-        if (rc) return rc;
-        pairs_total += pairs;
     }
     CK(cudaEventRecord(ctx->ev[2], ctx->stream));
-    CK(cudaMemcpyAsync(counts_host, ctx->d_counts, ctx->batch_total * 8, cudaMemcpyDeviceToHost,
-                       ctx->stream));
     CK(cudaEventRecord(ctx->ev[3], ctx->stream));
     std::memset(&ctx->stats, 0, sizeof ctx->stats);
-    ctx->stats.pairs = pairs_total;
-    ctx->stats.evaluated = pairs_total;
+    ctx->stats.pairs = B.pairs;
+    ctx->stats.evaluated = B.pairs;
     ctx->stats.kernel_used = GOFR_KERNEL_AUTO;
-    return gofr_sync(ctx);
+    int rc = gofr_sync(ctx);
+    if (rc) return rc;
+    std::memcpy(counts_host, B.h_stage, ctx->batch_total * sizeof(unsigned long long));
+    return GOFR_OK;
 }
 
 }  // extern "C"

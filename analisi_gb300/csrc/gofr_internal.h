@@ -52,6 +52,13 @@ struct PairLaunch {
     float wlim;               // wrap check: |frac| > wlim flags a recheck
     double rmin, rmax, dr, rmin2, rmax2;  // reference binning constants
     int tric;
+    int wchk;                 // batched kernel: per-pair wrap-decision check on
+};
+
+// One work descriptor of the batched kernel: origins [k0, k1) of one
+// (trajectory, lag, first-atom tile).
+struct WorkDesc {
+    int traj, lag_idx, itile, k0, k1, pad0, pad1, pad2;
 };
 
 // Launch configuration helpers implemented in gofr_kernels.cu.
@@ -66,6 +73,12 @@ int launch_pairs(const PairLaunch &P, int kind, bool wrapcheck, int num_sms, cud
                  size_t *smem_bytes_out);
 int pairs_smem_bytes(int kind, int nch, int nbin, int ntypes);
 int pairs_tile_atoms(int kind);
+int batch_smem_bytes(int max_nbin, int max_nch, int max_ntypes);
+int prepare_batch(int max_nbin, int max_nch, int max_ntypes, bool tric, int num_sms, int n_work,
+                  int *grid_out);
+int launch_batch_grid(const PairLaunch *d_trajs, const WorkDesc *d_work, int n_work,
+                      unsigned *d_head, int max_nbin, int max_nch, int max_ntypes, bool tric,
+                      unsigned *d_err, unsigned long long *d_stats, int grid, cudaStream_t s);
 int launch_zero_u64(unsigned long long *p, size_t n, cudaStream_t s);
 
 }  // namespace gofr

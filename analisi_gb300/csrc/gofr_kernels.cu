@@ -253,248 +253,341 @@ struct F32Smem {
 // second atoms at once -- and one compare against hi_f.  The bound behind
 // hi_f, lo_f and the per-bin windows is derived on the host (gofr_capi.cu,
 // certify()).
+
+// Shared-memory views of the FP32 kernels.
+struct F32Views {
+    float *jx;
+    unsigned char *jt;
+    uint64_t *bars;
+    int *sflag, *rqn;
+    uint2 *slots;
+    uint4 *rq;
+    float2 *win;
+    unsigned *hist;
+    unsigned short *chtab;
+    __device__ F32Views(unsigned char *smem, const F32Smem &L)
+        : jx(reinterpret_cast<float *>(smem + L.jx)), jt(smem + L.jt),
+          bars(reinterpret_cast<uint64_t *>(smem + L.bars)),
+          sflag(reinterpret_cast<int *>(smem + L.flag)),
+          rqn(reinterpret_cast<int *>(smem + L.rqn)),
+          slots(reinterpret_cast<uint2 *>(smem + L.slots)),
+          rq(reinterpret_cast<uint4 *>(smem + L.rq)),
+          win(reinterpret_cast<float2 *>(smem + L.win)),
+          hist(reinterpret_cast<unsigned *>(smem + L.hist)),
+          chtab(reinterpret_cast<unsigned short *>(smem + L.chtab))
+    {
+    }
+};
+
+// Per-thread state carried across items: mbarrier phases and counters.
+struct F32Thread {
+    unsigned phase0 = 0u, phase1 = 0u;
+    unsigned long long n_cand = 0, n_rech = 0;
+};
+
+__device__ __forceinline__ void f32_init_barriers(const F32Views &V)
+{
+    if (threadIdx.x == 0) {
+        mbar_init(&V.bars[0], 1);
+        mbar_init(&V.bars[1], 1);
+        *V.sflag = 0;
+        *V.rqn = 0;
+        fence_mbar_init();
+    }
+}
+
+// A bounded wait ran out: a copy may still be in flight into either buffer
+// (the one waited for, and the prefetch of the next tile).  Give both a
+// bounded chance to land before the CTA exits and its shared memory is reused.
+__device__ __forceinline__ void f32_abort(const F32Views &V, const F32Thread &th, unsigned *err)
+{
+    if (threadIdx.x == 0) {
+        mbar_wait_bounded(&V.bars[0], th.phase0);
+        mbar_wait_bounded(&V.bars[1], th.phase1);
+        atomicOr(err, ERRW_WAIT_TIMEOUT);
+    }
+}
+
+// One item: the first atoms of tile `itile` at origin k against every second
+// atom at lag lag_idx, binned into V.hist.  Returns false if a bounded wait
+// ran out (the caller aborts the CTA).  All threads of the CTA call it.
+template <bool TRI, bool WCHK>
+__device__ __forceinline__ bool f32_item(const PairLaunch &P, const F32Views &V, F32Thread &th,
+                                         int lag_idx, int itile, int k)
+{
+    const int tid = threadIdx.x;
+    const int half = P.nch / 2;
+    const long long N = P.N, NP = P.NP;
+    const int nchunks = (P.N + TJ32 - 1) / TJ32;
+    const float hi_f = P.hi_f;
+    uint2 *const my_slots = V.slots + tid;
+    const long long fo = P.primo + (long long)k * P.skip;
+    const long long fl = fo + (long long)lag_idx * P.every;
+    Box2 bx;
+    {
+        const Box32 b = P.box32[fo];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            bx.invL[a] = f2pk(b.invL[a], b.invL[a]);
+            bx.negL[a] = f2pk(-b.L[a], -b.L[a]);
+            bx.negT[a] = f2pk(-b.tilt[a], -b.tilt[a]);
+        }
+    }
+    // first atoms of this item
+    const int ia0 = P.a0 + itile * TI32 + tid;
+    f2 xi[R32], yi[R32], zi[R32];
+    int ti[R32];
+    const float *fi = P.pos32 + fo * 3 * NP;
+#pragma unroll
+    for (int r = 0; r < R32; ++r) {
+        const int ia = ia0 + r * NT;
+        float x, y, z;
+        if (ia < P.a1) {
+            x = fi[ia]; y = fi[NP + ia]; z = fi[2 * NP + ia];
+            ti[r] = P.types8[ia];
+        } else {
+            // no atom: NaN never passes d2 <= hi_f nor the wrap check
+            x = y = z = __int_as_float(0x7fc00000);
+            ti[r] = 0;
+        }
+        xi[r] = f2pk(x, x); yi[r] = f2pk(y, y); zi[r] = f2pk(z, z);
+    }
+
+    const float *fj = P.pos32 + fl * 3 * NP;
+    int cnt = 0;
+    __syncthreads();  // previous item done with both buffers
+    if (tid == 0) {
+        const int tj = min(TJ32, P.N);
+        const unsigned fb = (unsigned)(((tj + 3) & ~3) * 4), tb = (unsigned)((tj + 15) & ~15);
+        mbar_arrive_expect_tx(&V.bars[0], 3 * fb + tb);
+        bulk_g2s(V.jx, fj, fb, &V.bars[0]);
+        bulk_g2s(V.jx + TJ32, fj + NP, fb, &V.bars[0]);
+        bulk_g2s(V.jx + 2 * TJ32, fj + 2 * NP, fb, &V.bars[0]);
+        bulk_g2s(V.jt, P.types8, tb, &V.bars[0]);
+    }
+    for (int c = 0; c < nchunks; ++c) {
+        const int b = c & 1;
+        const int jbase = c * TJ32;
+        if (tid == 0 && c + 1 < nchunks) {
+            const int nb = jbase + TJ32;
+            const int tj = min(TJ32, P.N - nb);
+            const unsigned fb = (unsigned)(((tj + 3) & ~3) * 4);
+            const unsigned tb = (unsigned)((tj + 15) & ~15);
+            float *dst = V.jx + (b ^ 1) * 3 * TJ32;
+            mbar_arrive_expect_tx(&V.bars[b ^ 1], 3 * fb + tb);
+            bulk_g2s(dst, fj + nb, fb, &V.bars[b ^ 1]);
+            bulk_g2s(dst + TJ32, fj + NP + nb, fb, &V.bars[b ^ 1]);
+            bulk_g2s(dst + 2 * TJ32, fj + 2 * NP + nb, fb, &V.bars[b ^ 1]);
+            bulk_g2s(V.jt + (b ^ 1) * TJ32, P.types8 + nb, tb, &V.bars[b ^ 1]);
+        }
+        const bool ok = mbar_wait_bounded(&V.bars[b], b ? th.phase1 : th.phase0);
+        if (ok) { if (b) th.phase1 ^= 1u; else th.phase0 ^= 1u; }
+        else atomicOr(V.sflag, 1);
+        __syncthreads();
+        if (*V.sflag) return false;
+
+        const int tj = min(TJ32, P.N - jbase);
+        const float *bxp = V.jx + b * 3 * TJ32;
+        const unsigned char *btp = V.jt + b * TJ32;
+
+        // Bins every slot of this warp's lanes (all lanes take part; each
+        // processes its own slots), then empties them.
+        auto warp_flush = [&]() {
+            const int maxc = __reduce_max_sync(0xffffffffu, (unsigned)cnt);
+            for (int q = 0; q < maxc; ++q) {
+                if (q < cnt) {
+                    const uint2 e = my_slots[q * NT];
+                    const float d2 = __uint_as_float(e.x);
+                    const int r = e.y & 3;
+                    const int jj = (e.y >> 2) & 0x1fff;
+                    const int ia = ia0 + r * NT;
+                    const int ja = jbase + jj;
+                    int t_i = ti[0];
+#pragma unroll
+                    for (int rr = 1; rr < R32; ++rr) t_i = (r == rr) ? ti[rr] : t_i;
+                    const int ch = V.chtab[t_i * P.ntypes + btp[jj]] + (ia == ja ? half : 0);
+                    bool need = WCHK && (e.y >> 31);
+                    if (!need && d2 >= P.lo_f) {
+                        const float rr_ = __fsqrt_rn(d2);
+                        int bi = __float2int_rd(__fmul_rn(__fsub_rn(rr_, P.rmin_f), P.inv_dr_f));
+                        bi = min(max(bi, 0), P.nbin - 1);
+                        const float2 w = V.win[bi];
+                        if (d2 >= w.x && d2 <= w.y) atomicAdd(V.hist + ch * P.nbin + bi, 1u);
+                        else need = true;
+                    }
+                    if (need) {
+                        ++th.n_rech;
+                        const int slot = atomicAdd(V.rqn, 1);
+                        if (slot < QCAP) {
+                            V.rq[slot] = make_uint4((unsigned)ia, (unsigned)ja, (unsigned)ch, 0u);
+                        } else {
+                            recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, ia, ja, V.hist, ch,
+                                              P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err);
+                        }
+                    }
+                }
+            }
+            th.n_cand += cnt;
+            cnt = 0;
+        };
+
+        for (int jj = 0; jj < tj; jj += 4) {
+            const float4 X = *reinterpret_cast<const float4 *>(bxp + jj);
+            const float4 Y = *reinterpret_cast<const float4 *>(bxp + TJ32 + jj);
+            const float4 Z = *reinterpret_cast<const float4 *>(bxp + 2 * TJ32 + jj);
+            const f2 xa = f2pk(X.x, X.y), xb = f2pk(X.z, X.w);
+            const f2 ya = f2pk(Y.x, Y.y), yb = f2pk(Y.z, Y.w);
+            const f2 za = f2pk(Z.x, Z.y), zb = f2pk(Z.z, Z.w);
+#pragma unroll
+            for (int r = 0; r < R32; ++r) {
+                unsigned wa = 0u, wb = 0u;
+                const f2 da = pair2<TRI, WCHK>(xi[r], yi[r], zi[r], xa, ya, za, bx, P.wlim, &wa);
+                const f2 db = pair2<TRI, WCHK>(xi[r], yi[r], zi[r], xb, yb, zb, bx, P.wlim, &wb);
+                float d0, d1, d2v, d3;
+                f2up(da, d0, d1);
+                f2up(db, d2v, d3);
+                const unsigned m0 = (unsigned)((jj << 2) | r);
+                if (d0 <= hi_f || (WCHK && (wa & 1u))) {
+                    my_slots[cnt * NT] = make_uint2(__float_as_uint(d0), m0 | (WCHK && (wa & 1u) ? 0x80000000u : 0u));
+                    ++cnt;
+                }
+                if (d1 <= hi_f || (WCHK && (wa & 2u))) {
+                    my_slots[cnt * NT] = make_uint2(__float_as_uint(d1), (m0 + 4u) | (WCHK && (wa & 2u) ? 0x80000000u : 0u));
+                    ++cnt;
+                }
+                if (d2v <= hi_f || (WCHK && (wb & 1u))) {
+                    my_slots[cnt * NT] = make_uint2(__float_as_uint(d2v), (m0 + 8u) | (WCHK && (wb & 1u) ? 0x80000000u : 0u));
+                    ++cnt;
+                }
+                if (d3 <= hi_f || (WCHK && (wb & 2u))) {
+                    my_slots[cnt * NT] = make_uint2(__float_as_uint(d3), (m0 + 12u) | (WCHK && (wb & 2u) ? 0x80000000u : 0u));
+                    ++cnt;
+                }
+                if (__any_sync(0xffffffffu, cnt > SLOTS - 4)) warp_flush();
+            }
+        }
+        if (__any_sync(0xffffffffu, cnt > 0)) warp_flush();
+        __syncthreads();  // all reads of buffer b done before it is refilled
+        // drain the FP64 recheck queue when half full (uniform decision)
+        if (*V.rqn > QCAP / 2) {
+            const int n = min(*V.rqn, QCAP);
+            for (int q = tid; q < n; q += NT) {
+                const uint4 e = V.rq[q];
+                recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, (int)e.x, (int)e.y, V.hist,
+                                  (int)e.z, P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err);
+            }
+            __syncthreads();
+            if (tid == 0) *V.rqn = 0;
+            __syncthreads();
+        }
+    }
+    // end of item: the queue refers to this item's frames
+    const int n = min(*V.rqn, QCAP);
+    for (int q = tid; q < n; q += NT) {
+        const uint4 e = V.rq[q];
+        recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, (int)e.x, (int)e.y, V.hist, (int)e.z,
+                          P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err);
+    }
+    __syncthreads();
+    if (tid == 0) *V.rqn = 0;
+    return true;
+}
+
+// One trajectory: a persistent grid takes contiguous lag-major item ranges.
 template <bool TRI, bool WCHK>
 __global__ void __launch_bounds__(NT, 2) k_pairs_f32(const PairLaunch P)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    const F32Smem L(P.nbin, P.nch, P.ntypes);
-    float *jx = reinterpret_cast<float *>(smem + L.jx);
-    unsigned char *jt = smem + L.jt;
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.bars);
-    int *sflag = reinterpret_cast<int *>(smem + L.flag);
-    int *rqn = reinterpret_cast<int *>(smem + L.rqn);
-    uint2 *slots = reinterpret_cast<uint2 *>(smem + L.slots);
-    uint4 *rq = reinterpret_cast<uint4 *>(smem + L.rq);
-    float2 *win = reinterpret_cast<float2 *>(smem + L.win);
-    unsigned *hist = reinterpret_cast<unsigned *>(smem + L.hist);
-    unsigned short *chtab = reinterpret_cast<unsigned short *>(smem + L.chtab);
-
+    const F32Views V(smem, F32Smem(P.nbin, P.nch, P.ntypes));
     const int tid = threadIdx.x;
     const int hlen = P.nch * P.nbin;
-    const int half = P.nch / 2;
-    for (int i = tid; i < P.nbin; i += NT) win[i] = P.win[i];
-    for (int i = tid; i < hlen; i += NT) hist[i] = 0u;
-    for (int i = tid; i < P.ntypes * P.ntypes; i += NT) chtab[i] = P.chtab[i];
-    if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        *sflag = 0;
-        *rqn = 0;
-        fence_mbar_init();
-    }
+    for (int i = tid; i < P.nbin; i += NT) V.win[i] = P.win[i];
+    for (int i = tid; i < hlen; i += NT) V.hist[i] = 0u;
+    for (int i = tid; i < P.ntypes * P.ntypes; i += NT) V.chtab[i] = P.chtab[i];
+    f32_init_barriers(V);
     __syncthreads();
 
     const long long per = (P.n_items + gridDim.x - 1) / gridDim.x;
     const long long it0 = (long long)blockIdx.x * per;
     const long long it1 = min(it0 + per, P.n_items);
-    const long long N = P.N, NP = P.NP;
-    const int nchunks = (P.N + TJ32 - 1) / TJ32;
     const long long flush_every = items_per_flush(TI32, P.N);
-    const float hi_f = P.hi_f;
-
-    unsigned phase0 = 0u, phase1 = 0u;
     int cur_lag = -1;
     long long since_flush = 0;
-    unsigned long long n_cand = 0, n_rech = 0;
-    bool failed = false;
-    uint2 *const my_slots = slots + tid;
-
-    for (long long item = it0; item < it1 && !failed; ++item) {
+    F32Thread th;
+    for (long long item = it0; item < it1; ++item) {
         int lag_idx, itile, k;
         decompose(item, P, lag_idx, itile, k);
         if (lag_idx != cur_lag || since_flush >= flush_every) {
             if (cur_lag >= 0)
-                flush_hist(hist, hlen, P.counts + (long long)cur_lag * P.every * hlen);
+                flush_hist(V.hist, hlen, P.counts + (long long)cur_lag * P.every * hlen);
             cur_lag = lag_idx;
             since_flush = 0;
         }
         ++since_flush;
-        const long long fo = P.primo + (long long)k * P.skip;
-        const long long fl = fo + (long long)lag_idx * P.every;
-        Box2 bx;
-        {
-            const Box32 b = P.box32[fo];
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                bx.invL[a] = f2pk(b.invL[a], b.invL[a]);
-                bx.negL[a] = f2pk(-b.L[a], -b.L[a]);
-                bx.negT[a] = f2pk(-b.tilt[a], -b.tilt[a]);
-            }
-        }
-        // first atoms of this item
-        const int ia0 = P.a0 + itile * TI32 + tid;
-        f2 xi[R32], yi[R32], zi[R32];
-        int ti[R32];
-        const float *fi = P.pos32 + fo * 3 * NP;
-#pragma unroll
-        for (int r = 0; r < R32; ++r) {
-            const int ia = ia0 + r * NT;
-            float x, y, z;
-            if (ia < P.a1) {
-                x = fi[ia]; y = fi[NP + ia]; z = fi[2 * NP + ia];
-                ti[r] = P.types8[ia];
-            } else {
-                // no atom: NaN never passes d2 <= hi_f nor the wrap check
-                x = y = z = __int_as_float(0x7fc00000);
-                ti[r] = 0;
-            }
-            xi[r] = f2pk(x, x); yi[r] = f2pk(y, y); zi[r] = f2pk(z, z);
-        }
-
-        const float *fj = P.pos32 + fl * 3 * NP;
-        int cnt = 0;
-        __syncthreads();  // previous item done with both buffers
-        if (tid == 0) {
-            const int tj = min(TJ32, P.N);
-            const unsigned fb = (unsigned)(((tj + 3) & ~3) * 4), tb = (unsigned)((tj + 15) & ~15);
-            mbar_arrive_expect_tx(&bars[0], 3 * fb + tb);
-            bulk_g2s(jx, fj, fb, &bars[0]);
-            bulk_g2s(jx + TJ32, fj + NP, fb, &bars[0]);
-            bulk_g2s(jx + 2 * TJ32, fj + 2 * NP, fb, &bars[0]);
-            bulk_g2s(jt, P.types8, tb, &bars[0]);
-        }
-        for (int c = 0; c < nchunks; ++c) {
-            const int b = c & 1;
-            const int jbase = c * TJ32;
-            if (tid == 0 && c + 1 < nchunks) {
-                const int nb = jbase + TJ32;
-                const int tj = min(TJ32, P.N - nb);
-                const unsigned fb = (unsigned)(((tj + 3) & ~3) * 4);
-                const unsigned tb = (unsigned)((tj + 15) & ~15);
-                float *dst = jx + (b ^ 1) * 3 * TJ32;
-                mbar_arrive_expect_tx(&bars[b ^ 1], 3 * fb + tb);
-                bulk_g2s(dst, fj + nb, fb, &bars[b ^ 1]);
-                bulk_g2s(dst + TJ32, fj + NP + nb, fb, &bars[b ^ 1]);
-                bulk_g2s(dst + 2 * TJ32, fj + 2 * NP + nb, fb, &bars[b ^ 1]);
-                bulk_g2s(jt + (b ^ 1) * TJ32, P.types8 + nb, tb, &bars[b ^ 1]);
-            }
-            const bool ok = mbar_wait_bounded(&bars[b], b ? phase1 : phase0);
-            if (ok) { if (b) phase1 ^= 1u; else phase0 ^= 1u; }
-            else atomicOr(sflag, 1);
-            __syncthreads();
-            if (*sflag) { failed = true; break; }
-
-            const int tj = min(TJ32, P.N - jbase);
-            const float *bxp = jx + b * 3 * TJ32;
-            const unsigned char *btp = jt + b * TJ32;
-
-            // Bins every slot of this warp's lanes (all lanes take part; each
-            // processes its own slots), then empties them.
-            auto warp_flush = [&]() {
-                const int maxc = __reduce_max_sync(0xffffffffu, (unsigned)cnt);
-                for (int q = 0; q < maxc; ++q) {
-                    if (q < cnt) {
-                        const uint2 e = my_slots[q * NT];
-                        const float d2 = __uint_as_float(e.x);
-                        const int r = e.y & 3;
-                        const int jj = (e.y >> 2) & 0x1fff;
-                        const int ia = ia0 + r * NT;
-                        const int ja = jbase + jj;
-                        int t_i = ti[0];
-#pragma unroll
-                        for (int rr = 1; rr < R32; ++rr) t_i = (r == rr) ? ti[rr] : t_i;
-                        const int ch = chtab[t_i * P.ntypes + btp[jj]] + (ia == ja ? half : 0);
-                        bool need = WCHK && (e.y >> 31);
-                        if (!need && d2 >= P.lo_f) {
-                            const float rr_ = __fsqrt_rn(d2);
-                            int bi = __float2int_rd(__fmul_rn(__fsub_rn(rr_, P.rmin_f), P.inv_dr_f));
-                            bi = min(max(bi, 0), P.nbin - 1);
-                            const float2 w = win[bi];
-                            if (d2 >= w.x && d2 <= w.y) atomicAdd(hist + ch * P.nbin + bi, 1u);
-                            else need = true;
-                        }
-                        if (need) {
-                            ++n_rech;
-                            const int slot = atomicAdd(rqn, 1);
-                            if (slot < QCAP) {
-                                rq[slot] = make_uint4((unsigned)ia, (unsigned)ja, (unsigned)ch, 0u);
-                            } else {
-                                recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, ia, ja, hist, ch,
-                                                  P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err);
-                            }
-                        }
-                    }
-                }
-                n_cand += cnt;
-                cnt = 0;
-            };
-
-            for (int jj = 0; jj < tj; jj += 4) {
-                const float4 X = *reinterpret_cast<const float4 *>(bxp + jj);
-                const float4 Y = *reinterpret_cast<const float4 *>(bxp + TJ32 + jj);
-                const float4 Z = *reinterpret_cast<const float4 *>(bxp + 2 * TJ32 + jj);
-                const f2 xa = f2pk(X.x, X.y), xb = f2pk(X.z, X.w);
-                const f2 ya = f2pk(Y.x, Y.y), yb = f2pk(Y.z, Y.w);
-                const f2 za = f2pk(Z.x, Z.y), zb = f2pk(Z.z, Z.w);
-#pragma unroll
-                for (int r = 0; r < R32; ++r) {
-                    unsigned wa = 0u, wb = 0u;
-                    const f2 da = pair2<TRI, WCHK>(xi[r], yi[r], zi[r], xa, ya, za, bx, P.wlim, &wa);
-                    const f2 db = pair2<TRI, WCHK>(xi[r], yi[r], zi[r], xb, yb, zb, bx, P.wlim, &wb);
-                    float d0, d1, d2v, d3;
-                    f2up(da, d0, d1);
-                    f2up(db, d2v, d3);
-                    const unsigned m0 = (unsigned)((jj << 2) | r);
-                    if (d0 <= hi_f || (WCHK && (wa & 1u))) {
-                        my_slots[cnt * NT] = make_uint2(__float_as_uint(d0), m0 | (WCHK && (wa & 1u) ? 0x80000000u : 0u));
-                        ++cnt;
-                    }
-                    if (d1 <= hi_f || (WCHK && (wa & 2u))) {
-                        my_slots[cnt * NT] = make_uint2(__float_as_uint(d1), (m0 + 4u) | (WCHK && (wa & 2u) ? 0x80000000u : 0u));
-                        ++cnt;
-                    }
-                    if (d2v <= hi_f || (WCHK && (wb & 1u))) {
-                        my_slots[cnt * NT] = make_uint2(__float_as_uint(d2v), (m0 + 8u) | (WCHK && (wb & 1u) ? 0x80000000u : 0u));
-                        ++cnt;
-                    }
-                    if (d3 <= hi_f || (WCHK && (wb & 2u))) {
-                        my_slots[cnt * NT] = make_uint2(__float_as_uint(d3), (m0 + 12u) | (WCHK && (wb & 2u) ? 0x80000000u : 0u));
-                        ++cnt;
-                    }
-                    if (__any_sync(0xffffffffu, cnt > SLOTS - 4)) warp_flush();
-                }
-            }
-            if (__any_sync(0xffffffffu, cnt > 0)) warp_flush();
-            __syncthreads();  // all reads of buffer b done before it is refilled
-            // drain the FP64 recheck queue when half full (uniform decision)
-            if (*rqn > QCAP / 2) {
-                const int n = min(*rqn, QCAP);
-                for (int q = tid; q < n; q += NT) {
-                    const uint4 e = rq[q];
-                    recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, (int)e.x, (int)e.y, hist,
-                                      (int)e.z, P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err);
-                }
-                __syncthreads();
-                if (tid == 0) *rqn = 0;
-                __syncthreads();
-            }
-        }
-        if (failed) break;
-        // end of item: the queue refers to this item's frames
-        {
-            const int n = min(*rqn, QCAP);
-            for (int q = tid; q < n; q += NT) {
-                const uint4 e = rq[q];
-                recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, (int)e.x, (int)e.y, hist,
-                                  (int)e.z, P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err);
-            }
-            __syncthreads();
-            if (tid == 0) *rqn = 0;
+        if (!f32_item<TRI, WCHK>(P, V, th, lag_idx, itile, k)) {
+            f32_abort(V, th, P.err);
+            return;
         }
     }
-    if (failed) {
-        // A copy may still be in flight into either buffer (the one whose wait
-        // ran out, and the prefetch of the next tile): give both a bounded
-        // chance to land before the CTA exits and its shared memory is reused.
-        if (tid == 0) {
-            mbar_wait_bounded(&bars[0], phase0);
-            mbar_wait_bounded(&bars[1], phase1);
-            atomicOr(P.err, ERRW_WAIT_TIMEOUT);
+    if (cur_lag >= 0) flush_hist(V.hist, hlen, P.counts + (long long)cur_lag * P.every * hlen);
+    add_stats(P.stats, th.n_cand, th.n_rech);
+}
+
+// Many trajectories in one persistent launch.  Each CTA pulls work
+// descriptors (trajectory, lag, first-atom tile, origin range) from a device
+// queue (one atomic counter; descriptors sorted by decreasing cost on the
+// host), switches the shared tables when the trajectory changes, and flushes
+// its histogram into that trajectory's counts at the end of every descriptor.
+template <bool TRI>
+__global__ void __launch_bounds__(NT, 2) k_pairs_batch(const PairLaunch *__restrict__ trajs,
+                                                       const WorkDesc *__restrict__ work,
+                                                       int n_work, unsigned *head, int max_nbin,
+                                                       int max_nch, int max_ntypes, unsigned *err,
+                                                       unsigned long long *stats)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int s_next;
+    // the current trajectory's parameters live in shared memory: a register
+    // copy of the whole struct would crowd out the hot loop
+    __shared__ __align__(16) PairLaunch sP;
+    const F32Views V(smem, F32Smem(max_nbin, max_nch, max_ntypes));
+    const int tid = threadIdx.x;
+    for (int i = tid; i < max_nch * max_nbin; i += NT) V.hist[i] = 0u;
+    f32_init_barriers(V);
+    __syncthreads();
+    const PairLaunch &P = sP;
+    int cur = -1;
+    F32Thread th;
+    for (;;) {
+        if (tid == 0) s_next = (int)atomicAdd(head, 1u);
+        __syncthreads();
+        const int idx = s_next;
+        __syncthreads();
+        if (idx >= n_work) break;
+        const WorkDesc w = work[idx];
+        if (w.traj != cur) {
+            constexpr int words = (int)(sizeof(PairLaunch) / 4);
+            const unsigned *src = reinterpret_cast<const unsigned *>(trajs + w.traj);
+            for (int i = tid; i < words; i += NT) reinterpret_cast<unsigned *>(&sP)[i] = src[i];
+            __syncthreads();
+            for (int i = tid; i < P.nbin; i += NT) V.win[i] = P.win[i];
+            for (int i = tid; i < P.ntypes * P.ntypes; i += NT) V.chtab[i] = P.chtab[i];
+            cur = w.traj;
+            __syncthreads();
         }
-        return;
+        const bool wchk = P.wchk != 0;
+        for (int k = w.k0; k < w.k1; ++k) {
+            const bool ok = wchk ? f32_item<TRI, true>(P, V, th, w.lag_idx, w.itile, k)
+                                 : f32_item<TRI, false>(P, V, th, w.lag_idx, w.itile, k);
+            if (!ok) {
+                f32_abort(V, th, err);
+                return;
+            }
+        }
+        const int hlen = P.nch * P.nbin;
+        flush_hist(V.hist, hlen, P.counts + (long long)w.lag_idx * P.every * hlen);
     }
-    if (cur_lag >= 0) flush_hist(hist, hlen, P.counts + (long long)cur_lag * P.every * hlen);
-    add_stats(P.stats, n_cand, n_rech);
+    add_stats(stats, th.n_cand, th.n_rech);
 }
 
 // ---------------------------------------------------------------------------
@@ -707,6 +800,41 @@ static int launch_persistent(K kernel, const PairLaunch &P, int smem, int num_sm
     if (grid > P.n_items) grid = P.n_items;
     if (grid < 1) grid = 1;
     kernel<<<(unsigned)grid, NT, smem, s>>>(P);
+    return cuda_ok(cudaGetLastError());
+}
+
+int batch_smem_bytes(int max_nbin, int max_nch, int max_ntypes)
+{
+    return F32Smem(max_nbin, max_nch, max_ntypes).total;
+}
+
+int prepare_batch(int max_nbin, int max_nch, int max_ntypes, bool tric, int num_sms, int n_work,
+                  int *grid_out)
+{
+    const int smem = batch_smem_bytes(max_nbin, max_nch, max_ntypes);
+    auto kernel = tric ? k_pairs_batch<true> : k_pairs_batch<false>;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+        cudaSuccess)
+        return -1;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, NT, smem) != cudaSuccess)
+        return -1;
+    if (per_sm < 1) return -2;
+    long long grid = (long long)num_sms * per_sm;
+    if (grid > n_work) grid = n_work;
+    *grid_out = (int)(grid < 1 ? 1 : grid);
+    return 0;
+}
+
+int launch_batch_grid(const PairLaunch *d_trajs, const WorkDesc *d_work, int n_work,
+                      unsigned *d_head, int max_nbin, int max_nch, int max_ntypes, bool tric,
+                      unsigned *d_err, unsigned long long *d_stats, int grid, cudaStream_t s)
+{
+    if (n_work <= 0) return 0;
+    const int smem = batch_smem_bytes(max_nbin, max_nch, max_ntypes);
+    auto kernel = tric ? k_pairs_batch<true> : k_pairs_batch<false>;
+    kernel<<<(unsigned)grid, NT, smem, s>>>(d_trajs, d_work, n_work, d_head, max_nbin, max_nch,
+                                            max_ntypes, d_err, d_stats);
     return cuda_ok(cudaGetLastError());
 }
 
