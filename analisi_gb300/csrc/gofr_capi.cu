@@ -53,6 +53,12 @@ struct TrajDev {
     BoxStats bs{};
     gofr_params params{};       // batch parameters
     size_t out_offset = 0, out_count = 0;
+    bool box_constant = true;   // every frame has the same box
+    // cell lists (built on first use for a grid, kept while the frames stay)
+    int cell_nc[3] = {0, 0, 0};
+    int *d_cstart = nullptr, *d_sid = nullptr;
+    float *d_spos = nullptr;
+    unsigned char *d_stype = nullptr;
 };
 
 }  // namespace
@@ -156,8 +162,14 @@ void free_traj(TrajDev &t)
     cudaFree(t.box32);
     cudaFree(t.types);
     cudaFree(t.types8);
+    cudaFree(t.d_cstart);
+    cudaFree(t.d_sid);
+    cudaFree(t.d_spos);
+    cudaFree(t.d_stype);
     t.pos64 = nullptr; t.pos32 = nullptr; t.box64 = nullptr; t.box32 = nullptr; t.types = nullptr;
     t.types8 = nullptr;
+    t.d_cstart = nullptr; t.d_sid = nullptr; t.d_spos = nullptr; t.d_stype = nullptr;
+    t.cell_nc[0] = t.cell_nc[1] = t.cell_nc[2] = 0;
 }
 
 inline uint64_t dbits(double x) { uint64_t u; std::memcpy(&u, &x, 8); return u; }
@@ -435,6 +447,9 @@ int upload_traj(gofr_ctx *ctx, TrajDev &t, const double *positions, const double
             s.eT[k] = std::max(s.eT[k], std::fabs((double)bb.tilt[k] - tl));
         }
     }
+    t.box_constant = true;
+    for (size_t f = 1; f < nframes && t.box_constant; ++f)
+        t.box_constant = std::memcmp(&t.h_box[f * 9], &t.h_box[0], 9 * sizeof(double)) == 0;
     free_traj(t);
     const size_t n3 = nframes * natoms * 3;
     CK(cudaMalloc(&t.pos64, n3 * sizeof(double)));
@@ -502,12 +517,58 @@ std::vector<unsigned short> channel_table(unsigned ntypes)
 
 struct Plan {
     int kind = 1;              // 0 = FP32+recheck, 1 = FP64
+    bool cells = false;        // FP32 kernel in its cell-list form
+    int nc[3] = {0, 0, 0}, blk[3] = {1, 1, 1}, nb[3] = {1, 1, 1};
+    double cell_fraction = 1.0;  // evaluated pairs / all pairs (estimate)
     bool wrapcheck = false;
     bool empty = false;        // accepted window empty: nothing can be counted
     Windows w;
     Bound b{};
     std::vector<double> th;
 };
+
+// Cell-list grid for an orthorhombic box that does not change: cells of edge
+// >= rmax (1 + 1e-6), so two atoms at minimum-image distance <= rmax are in
+// neighbouring cells on every axis (periodically); at least 3 cells per axis.
+// The block of cells one CTA takes is chosen to minimise the evaluated pairs
+// per useful first-atom slot.
+bool cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl)
+{
+    if (t.tric || !t.box_constant || p.nparts > 1) return false;
+    if (!(p.rmax > 0.0)) return false;
+    long long ncell = 1;
+    for (int k = 0; k < 3; ++k) {
+        const double L = 2.0 * t.h_box[3 + k];
+        const double nc = std::floor(L / (p.rmax * (1.0 + 1e-6)));
+        if (!(nc >= 3.0) || nc > 1024.0) return false;
+        pl.nc[k] = (int)nc;
+        ncell *= pl.nc[k];
+    }
+    if (ncell > (1ll << 22)) return false;
+    const double per_cell = (double)t.N / (double)ncell;
+    const int TI = cell_block_atoms();
+    double best = 1e300;
+    for (int bx = 1; bx <= 4; ++bx)
+        for (int by = 1; by <= 4; ++by)
+            for (int bz = 1; bz <= 4; ++bz) {
+                if (bx > pl.nc[0] || by > pl.nc[1] || bz > pl.nc[2]) continue;
+                const int jy = std::min(by + 2, pl.nc[1]), jz = std::min(bz + 2, pl.nc[2]);
+                if (2 * jy * jz > cell_max_ranges() || by * bz > cell_max_ranges()) continue;
+                const double atoms = per_cell * bx * by * bz;
+                if (atoms > 0.9 * TI && bx * by * bz > 1) continue;
+                const double nbhd = (double)std::min(bx + 2, pl.nc[0]) * jy * jz;
+                const double slots = std::ceil(std::max(atoms, 1.0) / TI) * TI;
+                const double cost = nbhd * slots / std::max(atoms, 1e-9);
+                if (cost < best) {
+                    best = cost;
+                    pl.blk[0] = bx; pl.blk[1] = by; pl.blk[2] = bz;
+                    pl.cell_fraction = nbhd / (double)ncell;
+                }
+            }
+    if (best >= 1e300) return false;
+    for (int k = 0; k < 3; ++k) pl.nb[k] = (pl.nc[k] + pl.blk[k] - 1) / pl.blk[k];
+    return true;
+}
 
 int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
 {
@@ -540,6 +601,17 @@ int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
         return fail(ctx, GOFR_ERR_UNSUPPORTED,
                     "coordinates too far outside the box for a certified FP32 wrap");
     }
+    if ((req == GOFR_KERNEL_CELL || req == GOFR_KERNEL_AUTO) && !pl.wrapcheck) {
+        Plan c = pl;
+        if (cell_plan(t, p, c) && (req == GOFR_KERNEL_CELL || c.cell_fraction < 0.35)) {
+            c.cells = true;
+            pl = c;
+        }
+    }
+    if (req == GOFR_KERNEL_CELL && !pl.cells)
+        return fail(ctx, GOFR_ERR_UNSUPPORTED,
+                    "cell lists need an orthorhombic box constant over the frames with at least "
+                    "3 cells of edge >= rmax per axis, and nparts <= 1");
     return GOFR_OK;
 }
 
@@ -611,6 +683,55 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
         L.inv_dr_f = (float)(1.0 / bm.dr);
         L.wlim = (float)(0.5 - pl.b.eta);
     }
+    if (pl.cells) {
+        TrajDev &tm = const_cast<TrajDev &>(t);
+        if (tm.cell_nc[0] != pl.nc[0] || tm.cell_nc[1] != pl.nc[1] || tm.cell_nc[2] != pl.nc[2]) {
+            cudaFree(tm.d_cstart); cudaFree(tm.d_sid); cudaFree(tm.d_spos); cudaFree(tm.d_stype);
+            tm.d_cstart = nullptr; tm.d_sid = nullptr; tm.d_spos = nullptr; tm.d_stype = nullptr;
+            tm.cell_nc[0] = tm.cell_nc[1] = tm.cell_nc[2] = 0;
+            const size_t ncell = (size_t)pl.nc[0] * pl.nc[1] * pl.nc[2];
+            const size_t NP = padded_natoms(t.N);
+            int *cell_of = nullptr, *rank_of = nullptr, *count = nullptr;
+            CK(cudaMalloc(&tm.d_cstart, t.T * (ncell + 1) * sizeof(int)));
+            CK(cudaMalloc(&tm.d_sid, t.T * NP * sizeof(int)));
+            CK(cudaMalloc(&tm.d_spos, t.T * 3 * NP * sizeof(float)));
+            CK(cudaMalloc(&tm.d_stype, t.T * NP));
+            CK(cudaMalloc(&cell_of, t.T * t.N * sizeof(int)));
+            CK(cudaMalloc(&rank_of, t.T * t.N * sizeof(int)));
+            CK(cudaMalloc(&count, t.T * (ncell + 1) * sizeof(int)));
+            ctx->launches += 3;
+            const int brc = launch_cell_build(t.pos64, t.pos32, t.types8, t.T, t.N, &t.h_box[0],
+                                              pl.nc, cell_of, rank_of, count, tm.d_cstart,
+                                              tm.d_spos, tm.d_sid, tm.d_stype, ctx->stream);
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(cell_of);
+            cudaFree(rank_of);
+            cudaFree(count);
+            if (brc) return fail(ctx, GOFR_ERR_CUDA, "cell-list build failed: %s",
+                                 cudaGetErrorString(cudaGetLastError()));
+            for (int k = 0; k < 3; ++k) tm.cell_nc[k] = pl.nc[k];
+        }
+        CellLaunch C{};
+        C.pair = L;
+        C.pair.a0 = 0;
+        C.pair.a1 = (int)t.N;
+        C.pair.counts = counts;
+        C.pair.n_items = (long long)L.n_lags * pl.nb[0] * pl.nb[1] * pl.nb[2] * L.n_orig;
+        C.start = t.d_cstart;
+        C.spos = t.d_spos;
+        C.sid = t.d_sid;
+        C.stype = t.d_stype;
+        for (int k = 0; k < 3; ++k) { C.nc[k] = pl.nc[k]; C.b[k] = pl.blk[k]; C.nb[k] = pl.nb[k]; }
+        const int csmem = cell_smem_bytes(L.nch, L.nbin, L.ntypes);
+        if (csmem > max_smem)
+            return fail(ctx, GOFR_ERR_UNSUPPORTED, "cell-list histogram does not fit shared memory");
+        ++ctx->launches;
+        if (launch_cell_pairs(C, ctx->num_sms, ctx->stream))
+            return fail(ctx, GOFR_ERR_CUDA, "cell pair kernel launch failed: %s",
+                        cudaGetErrorString(cudaGetLastError()));
+        *pairs_out = (unsigned long long)rs.n_lags * rs.n_orig * t.N * t.N;
+        return GOFR_OK;
+    }
     const unsigned nparts = p.nparts > 1 ? p.nparts : 1;
     const int TI = pairs_tile_atoms(pl.kind);
     const size_t per = t.N / nparts;
@@ -668,7 +789,8 @@ int run_common(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_d
     std::memset(&ctx->stats, 0, sizeof ctx->stats);
     ctx->stats.pairs = pairs;
     ctx->stats.evaluated = pairs;
-    ctx->stats.kernel_used = pl.kind == 0 ? GOFR_KERNEL_F32_RECHECK : GOFR_KERNEL_F64;
+    ctx->stats.kernel_used = pl.kind == 0 ? (pl.cells ? GOFR_KERNEL_CELL : GOFR_KERNEL_F32_RECHECK)
+                                          : GOFR_KERNEL_F64;
     ctx->stats.wrap_checked = pl.wrapcheck ? 1 : 0;
     ctx->stats.err_bound_d2 = pl.kind == 0 ? pl.w.E_rmax : 0.0;
     if (counts_host) return gofr_sync(ctx);
@@ -988,6 +1110,7 @@ int gofr_sync(gofr_ctx *ctx)
     CK(cudaMemcpy(st, ctx->d_stats, sizeof st, cudaMemcpyDeviceToHost));
     ctx->stats.candidates = st[ST_CANDIDATES];
     ctx->stats.rechecks = st[ST_RECHECKS];
+    if (ctx->stats.kernel_used == GOFR_KERNEL_CELL) ctx->stats.evaluated = st[ST_EVALUATED];
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]) == cudaSuccess) ctx->stats.kernel_ms = ms;
     if (cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[3]) == cudaSuccess) ctx->stats.total_ms = ms;

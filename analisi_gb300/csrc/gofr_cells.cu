@@ -1,0 +1,520 @@
+// Cell-list form of the FP32 + FP64-recheck pair kernel, for large N.
+//
+// The reference evaluates all N^2 ordered pairs per (lag, origin)
+// (lib/src/gofrt.cpp:101-102).  Here, for orthorhombic boxes that do not
+// change over the trajectory, every frame's atoms are binned into a grid of
+// cells whose edge is at least rmax (plus a margin): a pair at minimum-image
+// distance <= rmax always lies in cells that are neighbours (periodically) in
+// every axis, so pairs outside the neighbourhood are never counted by the
+// reference and need not be evaluated.  Every pair inside the neighbourhood
+// goes through exactly the same certified FP32 test and FP64 recheck as the
+// all-pairs kernel, so the counts are identical.
+//
+// Layout per frame: atoms sorted by cell (x fastest), FP32 SoA x|y|z (the
+// same values as the all-pairs frames), original atom ids, u8 types, and the
+// cell start offsets.  A work item is (lag, block of bx*by*bz cells, origin):
+// the block's atoms at the origin frame against the atoms of the block's
+// neighbourhood ((bx+2)(by+2)(bz+2) cells, fewer where that wraps the whole
+// box) at the lagged frame, streamed through shared memory.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gofr_device.cuh"
+#include "gofr_internal.h"
+
+namespace gofr {
+
+namespace cells {
+
+constexpr int NT = 256;
+constexpr int R = 4;          // first atoms per thread
+constexpr int TI = NT * R;
+constexpr int TJ = 1024;      // second atoms per shared-memory tile
+constexpr int SLOTS = 16;
+constexpr int QCAP = 1024;
+constexpr int MAXR = 64;      // max contiguous ranges of a neighbourhood (checked on host)
+
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 f2pk(float a, float b)
+{
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2up(f2 v, float &a, float &b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2 f2sub(f2 a, f2 b)
+{
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2mul(f2 a, f2 b)
+{
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2fma(f2 a, f2 b, f2 c)
+{
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// Orthorhombic minimum-image d2 of (i, j0) and (i, j1), the same operations
+// as the all-pairs kernel's pair2 (so FP32 values and bounds are identical).
+__device__ __forceinline__ f2 pair2o(f2 xi, f2 yi, f2 zi, f2 xj, f2 yj, f2 zj, const f2 *invL,
+                                     const f2 *negL)
+{
+    const f2 MAG = f2pk(12582912.0f, 12582912.0f);
+    f2 dx = f2sub(xi, xj), dy = f2sub(yi, yj), dz = f2sub(zi, zj);
+    const f2 kx = f2sub(f2fma(dx, invL[0], MAG), MAG);
+    const f2 ky = f2sub(f2fma(dy, invL[1], MAG), MAG);
+    const f2 kz = f2sub(f2fma(dz, invL[2], MAG), MAG);
+    dx = f2fma(kx, negL[0], dx);
+    dy = f2fma(ky, negL[1], dy);
+    dz = f2fma(kz, negL[2], dz);
+    f2 d2 = f2mul(dx, dx);
+    d2 = f2fma(dy, dy, d2);
+    d2 = f2fma(dz, dz, d2);
+    return d2;
+}
+
+__device__ __forceinline__ int wrapi(int a, int n)
+{
+    a %= n;
+    return a < 0 ? a + n : a;
+}
+
+// ---------------------------------------------------------------------------
+// cell build
+// ---------------------------------------------------------------------------
+__global__ void k_cell_assign(const double *__restrict__ pos, size_t T, size_t N, double xlo,
+                              double ylo, double zlo, double Lx, double Ly, double Lz, int ncx,
+                              int ncy, int ncz, int *__restrict__ cell_of,
+                              int *__restrict__ rank_of, int *__restrict__ count)
+{
+    const int ncell = ncx * ncy * ncz;
+    for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < T * N;
+         g += (size_t)gridDim.x * blockDim.x) {
+        const size_t f = g / N;
+        const double *p = pos + g * 3;
+        double u[3] = {(p[0] - xlo) / Lx, (p[1] - ylo) / Ly, (p[2] - zlo) / Lz};
+        const int nc[3] = {ncx, ncy, ncz};
+        int c[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            double w = u[k] - floor(u[k]);
+            int ck = (int)(w * nc[k]);
+            c[k] = ck < 0 ? 0 : (ck >= nc[k] ? nc[k] - 1 : ck);
+        }
+        const int cell = (c[2] * ncy + c[1]) * ncx + c[0];
+        cell_of[g] = cell;
+        rank_of[g] = atomicAdd(count + f * (size_t)(ncell + 1) + cell, 1);
+    }
+}
+
+// exclusive scan of each frame's counts into starts (one CTA per frame)
+__global__ void k_cell_scan(const int *__restrict__ count, int *__restrict__ start, int ncell)
+{
+    __shared__ int part[NT];
+    const size_t f = blockIdx.x;
+    const int *c = count + f * (size_t)(ncell + 1);
+    int *s = start + f * (size_t)(ncell + 1);
+    const int per = (ncell + NT - 1) / NT;
+    const int b0 = threadIdx.x * per, b1 = min(ncell, b0 + per);
+    int sum = 0;
+    for (int i = b0; i < b1; ++i) sum += c[i];
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int t = 0; t < NT; ++t) {
+            const int v = part[t];
+            part[t] = run;
+            run += v;
+        }
+        s[ncell] = run;
+    }
+    __syncthreads();
+    int run = part[threadIdx.x];
+    for (int i = b0; i < b1; ++i) {
+        s[i] = run;
+        run += c[i];
+    }
+}
+
+__global__ void k_cell_scatter(const float *__restrict__ pos32, const unsigned char *__restrict__ types8,
+                               size_t T, size_t N, size_t NP, int ncell,
+                               const int *__restrict__ cell_of, const int *__restrict__ rank_of,
+                               const int *__restrict__ start, float *__restrict__ spos,
+                               int *__restrict__ sid, unsigned char *__restrict__ stype)
+{
+    for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < T * N;
+         g += (size_t)gridDim.x * blockDim.x) {
+        const size_t f = g / N, a = g - f * N;
+        const size_t d = (size_t)start[f * (size_t)(ncell + 1) + cell_of[g]] + rank_of[g];
+        const float *src = pos32 + f * 3 * NP;
+        float *dst = spos + f * 3 * NP;
+        dst[d] = src[a];
+        dst[NP + d] = src[NP + a];
+        dst[2 * NP + d] = src[2 * NP + a];
+        sid[f * NP + d] = (int)a;
+        stype[f * NP + d] = types8[a];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pair kernel
+// ---------------------------------------------------------------------------
+struct Range {
+    int begin, end;   // sorted atom indices [begin, end)
+};
+
+// Rows of contiguous atom ranges making up a set of cells.
+// ys, zs: the y and z cell coordinates to visit; x cells [x0, x0+nx) wrapped.
+__device__ int build_ranges(const int *start, int ncx, int ncy, int ncz, int x0, int nx, int y0,
+                            int ny, int z0, int nz, Range *out)
+{
+    int n = 0;
+    for (int dz = 0; dz < nz; ++dz) {
+        const int cz = wrapi(z0 + dz, ncz);
+        for (int dy = 0; dy < ny; ++dy) {
+            const int cy = wrapi(y0 + dy, ncy);
+            const int rowbase = (cz * ncy + cy) * ncx;
+            if (nx >= ncx) {
+                out[n++] = {start[rowbase], start[rowbase + ncx]};
+            } else {
+                const int a = wrapi(x0, ncx);
+                const int b = a + nx;  // exclusive, may pass the row end
+                if (b <= ncx) {
+                    out[n++] = {start[rowbase + a], start[rowbase + b]};
+                } else {
+                    out[n++] = {start[rowbase + a], start[rowbase + ncx]};
+                    out[n++] = {start[rowbase], start[rowbase + (b - ncx)]};
+                }
+            }
+        }
+    }
+    return n;
+}
+
+// flat index q of a range list -> sorted atom index
+__device__ __forceinline__ int flat_to_atom(const Range *rg, const int *pre, int nr, int q)
+{
+    int r = 0;
+    while (r + 1 < nr && pre[r + 1] <= q) ++r;
+    return rg[r].begin + (q - pre[r]);
+}
+
+__global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    const PairLaunch &P = C.pair;
+    float *jx = reinterpret_cast<float *>(smem);                 // [3][TJ]
+    int *jid = reinterpret_cast<int *>(jx + 3 * TJ);              // [TJ]
+    unsigned char *jt = reinterpret_cast<unsigned char *>(jid + TJ);  // [TJ]
+    uint2 *slots = reinterpret_cast<uint2 *>(jt + TJ);            // [SLOTS][NT]
+    uint4 *rq = reinterpret_cast<uint4 *>(slots + SLOTS * NT);    // [QCAP]
+    float2 *win = reinterpret_cast<float2 *>(rq + QCAP);          // [nbin]
+    unsigned *hist = reinterpret_cast<unsigned *>(win + P.nbin);  // [nch][nbin]
+    unsigned short *chtab = reinterpret_cast<unsigned short *>(hist + P.nch * P.nbin);
+    __shared__ Range irg[MAXR], jrg[MAXR];
+    __shared__ int ipre[MAXR + 1], jpre[MAXR + 1];
+    __shared__ int nir, njr, rqn;
+
+    const int tid = threadIdx.x;
+    const int hlen = P.nch * P.nbin;
+    const int half = P.nch / 2;
+    for (int i = tid; i < P.nbin; i += NT) win[i] = P.win[i];
+    for (int i = tid; i < hlen; i += NT) hist[i] = 0u;
+    for (int i = tid; i < P.ntypes * P.ntypes; i += NT) chtab[i] = P.chtab[i];
+    if (tid == 0) rqn = 0;
+    __syncthreads();
+
+    const int nbx = C.nb[0], nby = C.nb[1], nbz = C.nb[2];
+    const long long nblocks = (long long)nbx * nby * nbz;
+    const long long per_lag = nblocks * P.n_orig;
+    const long long per = (P.n_items + gridDim.x - 1) / gridDim.x;
+    const long long it0 = (long long)blockIdx.x * per;
+    const long long it1 = min(it0 + per, P.n_items);
+    const long long NP = P.NP;
+    const int ncell = C.nc[0] * C.nc[1] * C.nc[2];
+    const float hi_f = P.hi_f;
+    f2 invL[3], negL[3];
+    int cur_lag = -1;
+    long long pairs_since = 0;
+    unsigned long long n_cand = 0, n_rech = 0, n_eval = 0;
+    uint2 *const my_slots = slots + tid;
+
+    for (long long item = it0; item < it1; ++item) {
+        const int lag_idx = (int)(item / per_lag);
+        const long long rem = item - (long long)lag_idx * per_lag;
+        const int blk = (int)(rem / P.n_orig);
+        const int k = (int)(rem - (long long)blk * P.n_orig);
+        const long long fo = P.primo + (long long)k * P.skip;
+        const long long fl = fo + (long long)lag_idx * P.every;
+        {
+            const Box32 b = P.box32[fo];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                invL[a] = f2pk(b.invL[a], b.invL[a]);
+                negL[a] = f2pk(-b.L[a], -b.L[a]);
+            }
+        }
+        const int bz = blk / (nbx * nby), by = (blk / nbx) % nby, bx = blk % nbx;
+        const int cx0 = bx * C.b[0], cy0 = by * C.b[1], cz0 = bz * C.b[2];
+        const int cnx = min(C.b[0], C.nc[0] - cx0), cny = min(C.b[1], C.nc[1] - cy0),
+                  cnz = min(C.b[2], C.nc[2] - cz0);
+        __syncthreads();  // previous item done with the range tables and tiles
+        if (tid == 0) {
+            const int *st_o = C.start + fo * (size_t)(ncell + 1);
+            const int *st_l = C.start + fl * (size_t)(ncell + 1);
+            nir = build_ranges(st_o, C.nc[0], C.nc[1], C.nc[2], cx0, cnx, cy0, cny, cz0, cnz, irg);
+            const int jnx = min(cnx + 2, C.nc[0]), jny = min(cny + 2, C.nc[1]),
+                      jnz = min(cnz + 2, C.nc[2]);
+            const int jx0 = jnx == C.nc[0] ? 0 : cx0 - 1;
+            const int jy0 = jny == C.nc[1] ? 0 : cy0 - 1;
+            const int jz0 = jnz == C.nc[2] ? 0 : cz0 - 1;
+            njr = build_ranges(st_l, C.nc[0], C.nc[1], C.nc[2], jx0, jnx, jy0, jny, jz0, jnz, jrg);
+            ipre[0] = 0;
+            for (int r = 0; r < nir; ++r) ipre[r + 1] = ipre[r] + (irg[r].end - irg[r].begin);
+            jpre[0] = 0;
+            for (int r = 0; r < njr; ++r) jpre[r + 1] = jpre[r] + (jrg[r].end - jrg[r].begin);
+        }
+        __syncthreads();
+        {
+            // flush when the lag changes, or before a u32 shared bin could
+            // overflow: one item adds at most n_i*n_j hits to a bin
+            const long long pairs_item = (long long)ipre[nir] * jpre[njr];
+            if (lag_idx != cur_lag || pairs_since + pairs_item >= (1ll << 31)) {
+                if (cur_lag >= 0) {
+                    for (int i = tid; i < hlen; i += NT) {
+                        const unsigned v = hist[i];
+                        if (v) {
+                            atomicAdd(P.counts + (long long)cur_lag * P.every * hlen + i,
+                                      (unsigned long long)v);
+                            hist[i] = 0u;
+                        }
+                    }
+                    __syncthreads();
+                }
+                cur_lag = lag_idx;
+                pairs_since = 0;
+            }
+            pairs_since += pairs_item;
+        }
+        const int n_i = ipre[nir], n_j = jpre[njr];
+        n_eval += (tid == 0) ? (unsigned long long)n_i * n_j : 0ull;
+        const float *fo32 = C.spos + fo * 3 * NP;
+        const float *fl32 = C.spos + fl * 3 * NP;
+        const int *fo_id = C.sid + fo * NP;
+        const int *fl_id = C.sid + fl * NP;
+        const unsigned char *fo_t = C.stype + fo * NP;
+        const unsigned char *fl_t = C.stype + fl * NP;
+
+        for (int ibase = 0; ibase < n_i; ibase += TI) {
+            f2 xi[R], yi[R], zi[R];
+            int ti[R], iid[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int q = ibase + r * NT + tid;
+                float x, y, z;
+                if (q < n_i) {
+                    const int s = flat_to_atom(irg, ipre, nir, q);
+                    x = fo32[s]; y = fo32[NP + s]; z = fo32[2 * NP + s];
+                    ti[r] = fo_t[s];
+                    iid[r] = fo_id[s];
+                } else {
+                    x = y = z = __int_as_float(0x7fc00000);
+                    ti[r] = 0;
+                    iid[r] = -1;
+                }
+                xi[r] = f2pk(x, x); yi[r] = f2pk(y, y); zi[r] = f2pk(z, z);
+            }
+            int cnt = 0;
+            for (int jbase = 0; jbase < n_j; jbase += TJ) {
+                const int tj = min(TJ, n_j - jbase);
+                __syncthreads();  // previous tile consumed
+                for (int q = tid; q < TJ; q += NT) {
+                    if (q < tj) {
+                        const int s = flat_to_atom(jrg, jpre, njr, jbase + q);
+                        jx[q] = fl32[s];
+                        jx[TJ + q] = fl32[NP + s];
+                        jx[2 * TJ + q] = fl32[2 * NP + s];
+                        jid[q] = fl_id[s];
+                        jt[q] = fl_t[s];
+                    } else if (q < ((tj + 3) & ~3)) {
+                        const float nan = __int_as_float(0x7fc00000);
+                        jx[q] = nan; jx[TJ + q] = nan; jx[2 * TJ + q] = nan;
+                        jid[q] = -2;
+                        jt[q] = 0;
+                    }
+                }
+                __syncthreads();
+
+                auto warp_flush = [&]() {
+                    const int maxc = __reduce_max_sync(0xffffffffu, (unsigned)cnt);
+                    for (int qq = 0; qq < maxc; ++qq) {
+                        if (qq < cnt) {
+                            const uint2 e = my_slots[qq * NT];
+                            const float d2 = __uint_as_float(e.x);
+                            const int r = e.y & 3;
+                            const int jj = (e.y >> 2) & 0x1fff;
+                            int t_i = ti[0], ia = iid[0];
+#pragma unroll
+                            for (int rr = 1; rr < R; ++rr) {
+                                t_i = (r == rr) ? ti[rr] : t_i;
+                                ia = (r == rr) ? iid[rr] : ia;
+                            }
+                            const int ja = jid[jj];
+                            const int ch = chtab[t_i * P.ntypes + jt[jj]] + (ia == ja ? half : 0);
+                            bool need = false;
+                            if (d2 >= P.lo_f) {
+                                const float rr_ = __fsqrt_rn(d2);
+                                int bi = __float2int_rd(__fmul_rn(__fsub_rn(rr_, P.rmin_f), P.inv_dr_f));
+                                bi = min(max(bi, 0), P.nbin - 1);
+                                const float2 w = win[bi];
+                                if (d2 >= w.x && d2 <= w.y) atomicAdd(hist + ch * P.nbin + bi, 1u);
+                                else need = true;
+                            }
+                            if (need) {
+                                ++n_rech;
+                                const int slot = atomicAdd(&rqn, 1);
+                                if (slot < QCAP) {
+                                    rq[slot] = make_uint4((unsigned)ia, (unsigned)ja, (unsigned)ch, 0u);
+                                } else {
+                                    const double *xi64 = P.pos64 + (fo * P.N + ia) * 3;
+                                    const double *xj64 = P.pos64 + (fl * P.N + ja) * 3;
+                                    const double d2d = ref_d2<false>(xi64[0], xi64[1], xi64[2], xj64[0],
+                                                                     xj64[1], xj64[2], P.box64 + fo * 9, P.err);
+                                    const int bb = ref_bin(d2d, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
+                                    if (bb >= 0) atomicAdd(hist + ch * P.nbin + bb, 1u);
+                                }
+                            }
+                        }
+                    }
+                    n_cand += cnt;
+                    cnt = 0;
+                };
+
+                for (int jj = 0; jj < tj; jj += 4) {
+                    const float4 X = *reinterpret_cast<const float4 *>(jx + jj);
+                    const float4 Y = *reinterpret_cast<const float4 *>(jx + TJ + jj);
+                    const float4 Z = *reinterpret_cast<const float4 *>(jx + 2 * TJ + jj);
+                    const f2 xa = f2pk(X.x, X.y), xb = f2pk(X.z, X.w);
+                    const f2 ya = f2pk(Y.x, Y.y), yb = f2pk(Y.z, Y.w);
+                    const f2 za = f2pk(Z.x, Z.y), zb = f2pk(Z.z, Z.w);
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const f2 da = pair2o(xi[r], yi[r], zi[r], xa, ya, za, invL, negL);
+                        const f2 db = pair2o(xi[r], yi[r], zi[r], xb, yb, zb, invL, negL);
+                        float d0, d1, d2v, d3;
+                        f2up(da, d0, d1);
+                        f2up(db, d2v, d3);
+                        const unsigned m0 = (unsigned)((jj << 2) | r);
+                        if (d0 <= hi_f) { my_slots[cnt * NT] = make_uint2(__float_as_uint(d0), m0); ++cnt; }
+                        if (d1 <= hi_f) { my_slots[cnt * NT] = make_uint2(__float_as_uint(d1), m0 + 4u); ++cnt; }
+                        if (d2v <= hi_f) { my_slots[cnt * NT] = make_uint2(__float_as_uint(d2v), m0 + 8u); ++cnt; }
+                        if (d3 <= hi_f) { my_slots[cnt * NT] = make_uint2(__float_as_uint(d3), m0 + 12u); ++cnt; }
+                        if (__any_sync(0xffffffffu, cnt > SLOTS - 4)) warp_flush();
+                    }
+                }
+                if (__any_sync(0xffffffffu, cnt > 0)) warp_flush();
+            }
+        }
+        // end of item: FP64 recheck queue of this item's frames, all threads together
+        __syncthreads();
+        const int nq = min(rqn, QCAP);
+        for (int q = tid; q < nq; q += NT) {
+            const uint4 e = rq[q];
+            const double *xi64 = P.pos64 + (fo * P.N + (int)e.x) * 3;
+            const double *xj64 = P.pos64 + (fl * P.N + (int)e.y) * 3;
+            const double d2d = ref_d2<false>(xi64[0], xi64[1], xi64[2], xj64[0], xj64[1], xj64[2],
+                                             P.box64 + fo * 9, P.err);
+            const int bb = ref_bin(d2d, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
+            if (bb >= 0) atomicAdd(hist + (int)e.z * P.nbin + bb, 1u);
+        }
+        __syncthreads();
+        if (tid == 0) rqn = 0;
+    }
+    if (cur_lag >= 0) {
+        __syncthreads();
+        for (int i = tid; i < hlen; i += NT) {
+            const unsigned v = hist[i];
+            if (v) atomicAdd(P.counts + (long long)cur_lag * P.every * hlen + i, (unsigned long long)v);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        n_cand += __shfl_xor_sync(0xffffffffu, n_cand, o);
+        n_rech += __shfl_xor_sync(0xffffffffu, n_rech, o);
+        n_eval += __shfl_xor_sync(0xffffffffu, n_eval, o);
+    }
+    if ((tid & 31) == 0) {
+        if (n_cand) atomicAdd(P.stats + ST_CANDIDATES, n_cand);
+        if (n_rech) atomicAdd(P.stats + ST_RECHECKS, n_rech);
+        if (n_eval) atomicAdd(P.stats + ST_EVALUATED, n_eval);
+    }
+}
+
+}  // namespace cells
+
+int cell_smem_bytes(int nch, int nbin, int ntypes)
+{
+    using namespace cells;
+    size_t b = (size_t)3 * TJ * 4 + TJ * 4 + TJ + (size_t)SLOTS * NT * 8 + (size_t)QCAP * 16 +
+               (size_t)nbin * 8 + (size_t)nch * nbin * 4 + (size_t)ntypes * ntypes * 2;
+    return (int)((b + 127) / 128 * 128);
+}
+
+int cell_block_atoms() { return cells::TI; }
+int cell_max_ranges() { return cells::MAXR; }
+
+int launch_cell_build(const double *pos64, const float *pos32, const unsigned char *types8,
+                      size_t T, size_t N, const double *box_internal, const int *nc,
+                      int *cell_of, int *rank_of, int *count, int *start, float *spos, int *sid,
+                      unsigned char *stype, cudaStream_t s)
+{
+    using namespace cells;
+    const int ncell = nc[0] * nc[1] * nc[2];
+    if (cudaMemsetAsync(count, 0, T * (size_t)(ncell + 1) * sizeof(int), s) != cudaSuccess)
+        return -1;
+    const size_t NP = padded_natoms(N);
+    // padding of the sorted frames: NaN coordinates, id -1
+    if (cudaMemsetAsync(spos, 0xff, T * 3 * NP * sizeof(float), s) != cudaSuccess) return -1;
+    const size_t total = T * N;
+    int blocks = (int)((total + NT - 1) / NT);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_cell_assign<<<blocks, NT, 0, s>>>(pos64, T, N, box_internal[0], box_internal[1],
+                                        box_internal[2], 2.0 * box_internal[3],
+                                        2.0 * box_internal[4], 2.0 * box_internal[5], nc[0], nc[1],
+                                        nc[2], cell_of, rank_of, count);
+    k_cell_scan<<<(unsigned)T, NT, 0, s>>>(count, start, ncell);
+    k_cell_scatter<<<blocks, NT, 0, s>>>(pos32, types8, T, N, NP, ncell, cell_of, rank_of, start,
+                                         spos, sid, stype);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_cell_pairs(const CellLaunch &C, int num_sms, cudaStream_t s)
+{
+    using namespace cells;
+    if (C.pair.n_items <= 0) return 0;
+    const int smem = cell_smem_bytes(C.pair.nch, C.pair.nbin, C.pair.ntypes);
+    if (cudaFuncSetAttribute(k_pairs_cell, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+        cudaSuccess)
+        return -1;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairs_cell, NT, smem) !=
+        cudaSuccess)
+        return -1;
+    if (per_sm < 1) return -2;
+    long long grid = (long long)num_sms * per_sm;
+    if (grid > C.pair.n_items) grid = C.pair.n_items;
+    k_pairs_cell<<<(unsigned)grid, NT, smem, s>>>(C);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace gofr

@@ -1,0 +1,56 @@
+"""Cell-list form of the FP32 kernel (GOFR_KERNEL_CELL): same exact counts as
+the oracle and as the all-pairs kernels, for boxes with at least 3 cells of
+edge >= rmax per axis (unwrapped coordinates, shifted and non-cubic boxes,
+several types, skip/every/primo)."""
+import numpy as np
+import pytest
+
+from analisi_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+CASES = [
+    # seed, N, T, L, sigma, counts, params
+    (61, 2000, 10, 27.0, 0.3, [1200, 500, 300],
+     dict(rmin=0.0, rmax=6.0, nbin=60, tmax=3, skip=3, every=1, ntimesteps=6, primo=1)),
+    (62, 3000, 8, 31.0, 0.2, [3000],
+     dict(rmin=0.5, rmax=5.1, nbin=37, tmax=2, skip=2, every=1, ntimesteps=5, primo=0)),
+    (63, 2500, 9, 29.5, 0.25, [1000, 1000, 500],
+     dict(rmin=0.0, rmax=4.0, nbin=80, tmax=4, skip=4, every=2, ntimesteps=5, primo=0)),
+]
+
+
+def _run(eng, w, kernel):
+    p = w["params"]
+    eng.set_frames(w["positions"], w["boxes"], w["type_ids"], w["ntypes"])
+    c = eng.run(p["rmin"], p["rmax"], p["nbin"], p["tmax"], p["skip"], p["every"],
+                p["ntimesteps"], p["primo"], kernel=kernel)
+    return c, eng.stats()
+
+
+@pytest.mark.parametrize("case", CASES, ids=[str(c[0]) for c in CASES])
+def test_cells_match_oracle_and_all_pairs(gpu_engine, oracle_mod, case):
+    seed, N, T, L, sigma, counts, params = case
+    w = workloads.small_case(seed, N, T, L, sigma, counts, **params)
+    if seed == 62:  # shifted, non-cubic box
+        w["boxes"] = w["boxes"].copy()
+        w["boxes"][:, 0] -= 3.0
+        w["boxes"][:, 4] *= 1.08
+    p = w["params"]
+    ref = oracle_mod.gofrt_counts(w["positions"], w["boxes"], w["type_ids"], w["ntypes"],
+                                  p["rmin"], p["rmax"], p["nbin"], p["tmax"], 8, p["skip"],
+                                  p["every"], p["ntimesteps"], p["primo"])
+    cell, st = _run(gpu_engine, w, "cell")
+    assert st["kernel_used"] == 3
+    assert st["evaluated"] < st["pairs"]
+    np.testing.assert_array_equal(cell, ref)
+    allp, _ = _run(gpu_engine, w, "f32")
+    np.testing.assert_array_equal(allp, ref)
+
+
+def test_cell_kernel_refuses_small_box(gpu_engine):
+    from analisi_gb300 import engine
+    w = workloads.small_case(64, 200, 6, 10.0, 0.1, [200], rmin=0.0, rmax=4.0, nbin=10, tmax=2,
+                             skip=1, every=1, ntimesteps=3, primo=0)
+    with pytest.raises(engine.GofrError):
+        _run(gpu_engine, w, "cell")
