@@ -118,7 +118,7 @@ def build_host(force=False):
         jobs.append([cxx] + common + ["-shared", "-I", _pybind_include(),
                      "-I", sysconfig.get_paths()["include"],
                      os.path.join(HOST, "pyanalisi.cpp"), os.path.join(HOST, "trajectory.cpp"),
-                     "-o", mod] + link)
+                     os.path.join(HOST, "lammps_file.cpp"), "-o", mod] + link)
     if os.path.exists(os.path.join(HOST, "analisi_main.cpp")) and os.path.exists(
             os.path.join(HOST, "lammps_file.cpp")) and (
             force or _stale(cli, host_srcs + [lib])):

@@ -16,6 +16,7 @@
 #include <memory>
 
 #include "gofrt.h"
+#include "lammps_file.h"
 #include "trajectory.h"
 
 namespace py = pybind11;
@@ -195,6 +196,21 @@ time skip, every time, debug flag)doc")
                                    g.get_shape(), g.get_stride());
         });
 
+    m.def("read_lammps_binary", [](const std::string &path) {
+        analisi_gb300::LammpsFrames f = analisi_gb300::read_lammps_binary(path);
+        py::dict d;
+        d["positions"] = copy3(f.positions.data(), f.nframes, f.natoms, 3);
+        d["velocities"] = copy3(f.velocities.data(), f.nframes, f.natoms, 3);
+        const size_t st = f.triclinic ? 9 : 6;
+        py::array_t<double> b({f.nframes, st});
+        std::memcpy(b.mutable_data(), f.boxes.data(), sizeof(double) * f.nframes * st);
+        d["boxes"] = b;
+        d["types"] = py::array_t<int>(f.types.size(), f.types.data());
+        d["timesteps"] = py::array_t<long long>(f.timesteps.size(),
+                                                reinterpret_cast<const long long *>(f.timesteps.data()));
+        d["triclinic"] = f.triclinic;
+        return d;
+    }, "reads analisi's binary trajectory format (the CLI's -i input)");
     m.def("info", []() { return std::string("analisi_gb300: Gofrt on GB300 (sm_103a)"); });
     m.def("has_mmap", []() { return false; });
 }

@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-f64", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the batched (64 trajectories) and cell-list (131k atoms) lines")
     ap.add_argument("--lags", type=int, default=200,
                     help="tmax of every step (200 = the workload; smaller only for ncu captures)")
     return ap.parse_args()
@@ -226,6 +228,79 @@ def traffic_from_profiles():
     return None
 
 
+def bench_batch(engine, workloads, device):
+    """The 64 uneven trajectories (seeds 2000+k) in one persistent, graph-captured
+    launch, against the same trajectories run one by one.  Bounded: 20 origins
+    per trajectory (all its lags)."""
+    import numpy as np
+    mem = workloads.c4(64)
+    trajs = []
+    for m in mem:
+        p = m["params"]
+        trajs.append(dict(positions=m["positions"], boxes=m["boxes"], type_ids=m["type_ids"],
+                          ntypes=m["ntypes"],
+                          params=engine.make_params(p["rmin"], p["rmax"], p["nbin"], p["tmax"],
+                                                    p["skip"], p["every"],
+                                                    min(p["ntimesteps"], 20 * p["skip"]), 0)))
+    e = engine.Engine(device)
+    e.batch_set(trajs)
+    for _ in range(3):
+        outs = e.batch_run(use_graph=True)
+    ms = []
+    for _ in range(5):
+        e.batch_run(use_graph=True)
+        ms.append(e.stats()["kernel_ms"])
+    st = e.stats()
+    batch_rate = st["pairs"] / (sum(ms) / len(ms)) / 1e6
+    seq_ms, seq_pairs, same = 0.0, 0, True
+    best_single = 0.0
+    e2 = engine.Engine(device)
+    for k, (m, t) in enumerate(zip(mem, trajs)):
+        e2.set_frames(m["positions"], m["boxes"], m["type_ids"], m["ntypes"])
+        P = t["params"]
+        c = e2.run(P.rmin, P.rmax, P.nbin, P.tmax, P.skip, P.every, P.ntimesteps, P.primo)
+        s2 = e2.stats()
+        seq_ms += s2["kernel_ms"]
+        seq_pairs += s2["pairs"]
+        best_single = max(best_single, s2["pairs"] / s2["kernel_ms"] / 1e6)
+        same &= bool(np.array_equal(c, outs[k]))
+    e.close()
+    e2.close()
+    seq_rate = seq_pairs / seq_ms / 1e6
+    return {"workload": "64 trajectories, N log-uniform 256..16384, T 100..1000, 1-4 types, "
+                        "300 bins on [0,10], 20 origins x all lags each",
+            "pairs": st["pairs"], "value": round(batch_rate, 2), "unit": UNIT,
+            "sequential_same_trajectories": round(seq_rate, 2),
+            "best_single_trajectory": round(best_single, 2),
+            "ratio_vs_sequential": round(batch_rate / seq_rate, 3),
+            "ratio_vs_best_single": round(batch_rate / best_single, 3),
+            "counts_identical_to_single_runs": same, "cuda_graph": True}
+
+
+def bench_cells(engine, workloads, device):
+    """131072 atoms, 4 types, 250 bins on [0,10]: the cell-list kernel on a sample
+    (10 origins x 50 lags), its counts checked against the all-pairs FP32 kernel on
+    a sub-sample (1 origin x 5 lags)."""
+    import numpy as np
+    w = workloads.c5(T=150)
+    p = w["params"]
+    e = engine.Engine(device)
+    e.set_frames(w["positions"], w["boxes"], w["type_ids"], w["ntypes"])
+    for _ in range(2):
+        e.run(p["rmin"], p["rmax"], p["nbin"], 50, p["skip"], 1, 100, 0, kernel="cell")
+    st = e.stats()
+    a = e.run(p["rmin"], p["rmax"], p["nbin"], 5, p["skip"], 1, 5, 0, kernel="cell")
+    b = e.run(p["rmin"], p["rmax"], p["nbin"], 5, p["skip"], 1, 5, 0, kernel="f32")
+    sf = e.stats()
+    e.close()
+    return {"workload": "c5: N=131072, 4 types, L=109.47, rmax=10, 250 bins; 10 origins x 50 lags",
+            "value": round(st["pairs"] / st["kernel_ms"] / 1e6, 1), "unit": UNIT + " (all-pairs equivalent)",
+            "evaluated_gpairs_per_s": round(st["evaluated"] / st["kernel_ms"] / 1e6, 1),
+            "evaluated_fraction": round(st["evaluated"] / st["pairs"], 5),
+            "all_pairs_f32_gpairs_per_s": round(sf["pairs"] / sf["kernel_ms"] / 1e6, 1),
+            "counts_identical_to_all_pairs": bool(np.array_equal(a, b))}
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -342,6 +417,11 @@ def run_gpu(args):
             torch.distributed.barrier()
         return 0
 
+    extra = {}
+    if not args.no_extra:
+        del w
+        extra["batch64"] = bench_batch(engine, workloads, local)
+        extra["cells131k"] = bench_cells(engine, workloads, local)
     fp32_peak, satom_peak = engine.measure_peaks(local)
     achieved = pairs_per_launch * OPS_PER_PAIR / kernel_avg_s / 1e12
     peak = fp32_peak / 1e12
@@ -369,7 +449,7 @@ def run_gpu(args):
                                       "candidates_frac": round(cands / pairs, 6),
                                       "recheck_frac": rech / pairs}),
            "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
-           "clocks": clocks, "fp64_kernel": f64,
+           "clocks": clocks, "fp64_kernel": f64, **extra,
            "kernel_ms_per_step": round(1e3 * kernel_avg_s, 3)}
     print(json.dumps(res))
     if world > 1:
