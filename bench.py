@@ -417,11 +417,6 @@ def run_gpu(args):
             torch.distributed.barrier()
         return 0
 
-    extra = {}
-    if not args.no_extra:
-        del w
-        extra["batch64"] = bench_batch(engine, workloads, local)
-        extra["cells131k"] = bench_cells(engine, workloads, local)
     fp32_peak, satom_peak = engine.measure_peaks(local)
     achieved = pairs_per_launch * OPS_PER_PAIR / kernel_avg_s / 1e12
     peak = fp32_peak / 1e12
@@ -440,6 +435,11 @@ def run_gpu(args):
         cpu = {"value": round(v, 4), "unit": UNIT, "cores": thr, "kind": "port",
                "sample": desc, "seconds": round(dt, 2)}
     clocks = clk.summary(local)
+    extra = {}
+    if not args.no_extra:
+        del w
+        extra["batch64"] = bench_batch(engine, workloads, local)
+        extra["cells131k"] = bench_cells(engine, workloads, local)
     res = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": round(1e3 * dev_s / args.steps, 3), "higher_is_better": True,
