@@ -22,7 +22,7 @@
 
 #include <cuda_runtime.h>
 
-#include "../../include/gofr_gb300.h"
+#include "gofr_gb300.h"
 #include "gofr_internal.h"
 
 using namespace gofr;
@@ -1097,6 +1097,149 @@ int gofr_run_device(gofr_ctx *ctx, const gofr_params *p, unsigned long long *cou
     if (!counts_device) return fail(ctx, GOFR_ERR_ARG, "null output buffer");
     DevGuard g(ctx->device);
     return run_common(ctx, p, counts_device, nullptr);
+}
+
+int gofr_run_windows(gofr_ctx *ctx, const gofr_params *p, unsigned nwin,
+                     const unsigned long long *primos, unsigned long long *counts_host)
+{
+    if (!ctx) return GOFR_ERR_ARG;
+    if (!p || !primos || !counts_host || nwin == 0)
+        return fail(ctx, GOFR_ERR_ARG, "null argument or no windows");
+    if (ctx->trajs.size() != 1) return fail(ctx, GOFR_ERR_STATE, "no frames uploaded");
+    DevGuard g(ctx->device);
+    const TrajDev &t = ctx->trajs[0];
+    const unsigned nparts = p->nparts > 1 ? p->nparts : 1;
+    RunShape rs;
+    for (unsigned w = 0; w < nwin; ++w) {
+        gofr_params q = *p;
+        q.primo = primos[w];
+        const int rc = shape_of(ctx, t, q, rs);
+        if (rc) return rc;
+    }
+    Plan pl;
+    int rc = make_plan(ctx, t, *p, pl);
+    if (rc) return rc;
+    const size_t per_win = rs.data_length * nparts;
+    const size_t n_out = per_win * nwin;
+    rc = ensure(ctx, ctx->d_counts, ctx->cap_counts, n_out);
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_stats, 0, ST_COUNT * sizeof(unsigned long long), ctx->stream));
+    if (n_out) CK(cudaMemsetAsync(ctx->d_counts, 0, n_out * sizeof(unsigned long long), ctx->stream));
+    CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+    unsigned long long pairs = 0;
+    PairLaunch *d_l = nullptr;
+    WorkDesc *d_w = nullptr;
+    unsigned *d_head = nullptr;
+    bool one_launch = pl.kind == 0 && !pl.cells && !pl.empty && rs.n_lags > 0 && rs.n_orig > 0;
+    if (!one_launch) {
+        for (unsigned w = 0; w < nwin && rc == GOFR_OK; ++w) {
+            gofr_params q = *p;
+            q.primo = primos[w];
+            unsigned long long pw = 0;
+            rc = enqueue_run(ctx, t, q, rs, pl, ctx->d_counts + w * per_win, &pw);
+            pairs += pw;
+        }
+        if (rc) return rc;
+    } else {
+        // one parameter record per (window, partition), descriptors over all of them
+        const int TI = pairs_tile_atoms(0);
+        std::vector<unsigned short> tab = channel_table(t.ntypes);
+        rc = ensure(ctx, ctx->d_chtab, ctx->cap_chtab, tab.size());
+        if (rc == GOFR_OK) rc = ensure(ctx, ctx->d_win, ctx->cap_win, pl.w.win.size());
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(ctx->d_chtab, tab.data(), tab.size() * sizeof(unsigned short),
+                           cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->d_win, pl.w.win.data(), pl.w.win.size() * sizeof(float2),
+                           cudaMemcpyHostToDevice, ctx->stream));
+        BinMap bm(p->rmin, p->rmax, p->nbin);
+        std::vector<PairLaunch> ls;
+        struct Cost { unsigned long long c; WorkDesc w; };
+        std::vector<Cost> all;
+        const size_t per = t.N / nparts;
+        const unsigned long long target = 1ull << 26;
+        for (unsigned w = 0; w < nwin; ++w)
+            for (unsigned q = 0; q < nparts; ++q) {
+                const size_t a0 = q * per, a1 = (q == nparts - 1) ? t.N : (q + 1) * per;
+                if (a1 <= a0) continue;
+                PairLaunch L{};
+                L.pos32 = t.pos32; L.types8 = t.types8; L.pos64 = t.pos64; L.box64 = t.box64;
+                L.box32 = t.box32; L.win = ctx->d_win; L.chtab = ctx->d_chtab;
+                L.counts = ctx->d_counts + w * per_win + q * rs.data_length;
+                L.err = ctx->d_err; L.stats = ctx->d_stats;
+                L.N = (int)t.N; L.NP = (int)padded_natoms(t.N);
+                L.nbin = (int)p->nbin; L.nch = (int)rs.nch; L.ntypes = (int)t.ntypes;
+                L.a0 = (int)a0; L.a1 = (int)a1;
+                L.n_lags = (int)rs.n_lags; L.every = (int)rs.every;
+                L.n_orig = (int)rs.n_orig; L.skip = (int)rs.skip; L.primo = (long long)primos[w];
+                L.n_itiles = (int)((a1 - a0 + TI - 1) / TI);
+                L.rmin = bm.rmin; L.rmax = bm.rmax; L.dr = bm.dr; L.rmin2 = bm.rmin2;
+                L.rmax2 = bm.rmax2;
+                L.hi_f = pl.w.hi_f; L.lo_f = pl.w.lo_f; L.rmin_f = (float)p->rmin;
+                L.inv_dr_f = (float)(1.0 / bm.dr); L.wlim = (float)(0.5 - pl.b.eta);
+                L.tric = t.tric; L.wchk = pl.wrapcheck ? 1 : 0;
+                const int li = (int)ls.size();
+                ls.push_back(L);
+                for (unsigned l = 0; l < rs.n_lags; ++l)
+                    for (int it = 0; it < L.n_itiles; ++it) {
+                        const unsigned long long tile =
+                            std::min<size_t>(TI, a1 - a0 - (size_t)it * TI);
+                        const unsigned long long per_item = tile * t.N;
+                        unsigned long long chunk = std::max<unsigned long long>(1, target / per_item);
+                        chunk = std::min<unsigned long long>(
+                            chunk, std::max<unsigned long long>(1, (1ull << 31) / per_item));
+                        for (unsigned k0 = 0; k0 < rs.n_orig; k0 += (unsigned)chunk) {
+                            const unsigned k1 =
+                                (unsigned)std::min<unsigned long long>(k0 + chunk, rs.n_orig);
+                            all.push_back({(k1 - k0) * per_item, WorkDesc{li, (int)l, it, (int)k0,
+                                                                       (int)k1, 0, 0, 0}});
+                        }
+                    }
+            }
+        std::stable_sort(all.begin(), all.end(),
+                         [](const Cost &a, const Cost &b) { return a.c > b.c; });
+        std::vector<WorkDesc> work;
+        for (auto &c : all) work.push_back(c.w);
+        int grid = 0;
+        if (prepare_batch((int)p->nbin, (int)rs.nch, (int)t.ntypes, t.tric != 0, ctx->num_sms,
+                          (int)work.size(), &grid))
+            return fail(ctx, GOFR_ERR_CUDA, "batched kernel setup failed");
+        CK(cudaMalloc(&d_l, ls.size() * sizeof(PairLaunch)));
+        CK(cudaMalloc(&d_w, std::max<size_t>(work.size(), 1) * sizeof(WorkDesc)));
+        CK(cudaMalloc(&d_head, sizeof(unsigned)));
+        CK(cudaMemcpyAsync(d_l, ls.data(), ls.size() * sizeof(PairLaunch), cudaMemcpyHostToDevice,
+                           ctx->stream));
+        CK(cudaMemcpyAsync(d_w, work.data(), work.size() * sizeof(WorkDesc),
+                           cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemsetAsync(d_head, 0, sizeof(unsigned), ctx->stream));
+        ++ctx->launches;
+        if (launch_batch_grid(d_l, d_w, (int)work.size(), d_head, (int)p->nbin, (int)rs.nch,
+                              (int)t.ntypes, t.tric != 0, ctx->d_err, ctx->d_stats, grid,
+                              ctx->stream))
+            rc = fail(ctx, GOFR_ERR_CUDA, "windows launch failed: %s",
+                      cudaGetErrorString(cudaGetLastError()));
+        pairs = (unsigned long long)nwin * rs.n_lags * rs.n_orig * t.N * t.N;
+    }
+    if (rc == GOFR_OK) {
+        CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+        if (n_out)
+            CK(cudaMemcpyAsync(counts_host, ctx->d_counts, n_out * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+        std::memset(&ctx->stats, 0, sizeof ctx->stats);
+        ctx->stats.pairs = pairs;
+        ctx->stats.evaluated = pairs;
+        ctx->stats.kernel_used = pl.kind == 0 ? (pl.cells ? GOFR_KERNEL_CELL : GOFR_KERNEL_F32_RECHECK)
+                                              : GOFR_KERNEL_F64;
+        ctx->stats.wrap_checked = pl.wrapcheck ? 1 : 0;
+        rc = gofr_sync(ctx);
+    }
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(d_l);
+    cudaFree(d_w);
+    cudaFree(d_head);
+    return rc;
 }
 
 int gofr_sync(gofr_ctx *ctx)

@@ -23,7 +23,7 @@
 #include <cstring>
 #include <mutex>
 
-#include "../../include/gofr_gb300.h"
+#include "gofr_gb300.h"
 #include "gofr_device.cuh"
 
 namespace gofr {

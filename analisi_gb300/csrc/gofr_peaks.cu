@@ -8,7 +8,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
-#include "../../include/gofr_gb300.h"
+#include "gofr_gb300.h"
 
 namespace gofr {
 

@@ -26,7 +26,7 @@ EXPORTED = [
     "gofr_output_size", "gofr_run", "gofr_run_device", "gofr_sync", "gofr_get_stats",
     "gofr_counts_to_buffer", "gofr_bin_thresholds", "gofr_batch_set",
     "gofr_batch_output_layout", "gofr_batch_run", "gofr_measure_peaks",
-    "gofr_run_f64_noalloc",
+    "gofr_run_f64_noalloc", "gofr_run_windows",
 ]
 
 
@@ -103,13 +103,15 @@ def load_library(path=None):
                                            ctypes.POINTER(ctypes.c_size_t)]
     L.gofr_batch_run.argtypes = [vp, ctypes.c_int, up]
     L.gofr_measure_peaks.argtypes = [ctypes.c_int, dp, dp]
+    L.gofr_run_windows.argtypes = [vp, ctypes.POINTER(Params), ctypes.c_uint, up, up]
     L.gofr_run_f64_noalloc.argtypes = [vp, vp, ctypes.c_int, vp, ctypes.c_uint, ctypes.c_size_t,
                                        ctypes.c_size_t, ctypes.POINTER(Params), vp, vp,
                                        ctypes.c_char_p, ctypes.c_size_t]
     for name in ("gofr_ctx_create", "gofr_set_frames", "gofr_output_size", "gofr_run",
                  "gofr_run_device", "gofr_sync", "gofr_get_stats", "gofr_counts_to_buffer",
                  "gofr_bin_thresholds", "gofr_batch_set", "gofr_batch_output_layout",
-                 "gofr_batch_run", "gofr_measure_peaks", "gofr_run_f64_noalloc"):
+                 "gofr_batch_run", "gofr_measure_peaks", "gofr_run_f64_noalloc",
+                 "gofr_run_windows"):
         getattr(L, name).restype = ctypes.c_int
     if path is None:
         _lib = L
@@ -234,6 +236,24 @@ class Engine:
         self._check(self.L.gofr_run(self._ctx, ctypes.byref(p),
                                     out.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong))))
         return out[:n].reshape(shape)
+
+    def run_windows(self, rmin, rmax, nbin, tmax, skip, every, ntimesteps, primos,
+                    kernel="auto", nparts=1):
+        """Counts of several calculate(primo) windows in one launch:
+        [nwin][leff][nch][nbin] (or [nwin][nparts][...] when nparts > 1)."""
+        primos = np.ascontiguousarray(primos, dtype=np.uint64)
+        p = make_params(rmin, rmax, nbin, tmax, skip, every, ntimesteps, 0, kernel, nparts)
+        n = self.output_size(p)
+        leff = ntimesteps if (ntimesteps < tmax or tmax == 0) else tmax
+        nch = self.ntypes * (self.ntypes + 1)
+        out = np.zeros(max(n * len(primos), 1), dtype=np.uint64)
+        self._check(self.L.gofr_run_windows(
+            self._ctx, ctypes.byref(p), len(primos),
+            primos.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)),
+            out.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong))))
+        shape = (len(primos), leff, nch, int(nbin)) if nparts <= 1 else \
+            (len(primos), int(nparts), leff, nch, int(nbin))
+        return out[:n * len(primos)].reshape(shape)
 
     def run_params(self, p, out):
         """gofr_run with prepared Params and a preallocated uint64 output (hot loop form)."""

@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-f64", action="store_true")
+    ap.add_argument("--workload", default="c2", choices=["c2", "batch", "cells"],
+                    help="c2: the headline line (default); batch / cells: only that measurement")
+    ap.add_argument("--batch-origins", type=int, default=20,
+                    help="origins per trajectory of the batched measurement")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the batched (64 trajectories) and cell-list (131k atoms) lines")
     ap.add_argument("--lags", type=int, default=200,
@@ -228,10 +232,10 @@ def traffic_from_profiles():
     return None
 
 
-def bench_batch(engine, workloads, device):
+def bench_batch(engine, workloads, device, origins=20, reps=5):
     """The 64 uneven trajectories (seeds 2000+k) in one persistent, graph-captured
-    launch, against the same trajectories run one by one.  Bounded: 20 origins
-    per trajectory (all its lags)."""
+    launch, against the same trajectories run one by one.  Bounded: `origins`
+    origins per trajectory (all its lags)."""
     import numpy as np
     mem = workloads.c4(64)
     trajs = []
@@ -241,13 +245,13 @@ def bench_batch(engine, workloads, device):
                           ntypes=m["ntypes"],
                           params=engine.make_params(p["rmin"], p["rmax"], p["nbin"], p["tmax"],
                                                     p["skip"], p["every"],
-                                                    min(p["ntimesteps"], 20 * p["skip"]), 0)))
+                                                    min(p["ntimesteps"], origins * p["skip"]), 0)))
     e = engine.Engine(device)
     e.batch_set(trajs)
     for _ in range(3):
         outs = e.batch_run(use_graph=True)
     ms = []
-    for _ in range(5):
+    for _ in range(reps):
         e.batch_run(use_graph=True)
         ms.append(e.stats()["kernel_ms"])
     st = e.stats()
@@ -268,7 +272,7 @@ def bench_batch(engine, workloads, device):
     e2.close()
     seq_rate = seq_pairs / seq_ms / 1e6
     return {"workload": "64 trajectories, N log-uniform 256..16384, T 100..1000, 1-4 types, "
-                        "300 bins on [0,10], 20 origins x all lags each",
+                        f"300 bins on [0,10], {origins} origins x all lags each",
             "pairs": st["pairs"], "value": round(batch_rate, 2), "unit": UNIT,
             "sequential_same_trajectories": round(seq_rate, 2),
             "best_single_trajectory": round(best_single, 2),
@@ -438,7 +442,7 @@ def run_gpu(args):
     extra = {}
     if not args.no_extra:
         del w
-        extra["batch64"] = bench_batch(engine, workloads, local)
+        extra["batch64"] = bench_batch(engine, workloads, local, args.batch_origins)
         extra["cells131k"] = bench_cells(engine, workloads, local)
     res = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup,
@@ -457,10 +461,23 @@ def run_gpu(args):
     return 0
 
 
+def run_one(args):
+    """One secondary measurement alone (for profiling captures)."""
+    from analisi_gb300 import engine, workloads
+    if args.workload == "batch":
+        r = bench_batch(engine, workloads, 0, args.batch_origins, reps=max(1, args.steps))
+    else:
+        r = bench_cells(engine, workloads, 0)
+    print(json.dumps(r))
+    return 0
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload != "c2":
+        return run_one(args)
     return run_gpu(args)
 
 

@@ -131,6 +131,16 @@ int gofr_run_device(gofr_ctx *ctx, const gofr_params *p, unsigned long long *cou
 /* Waits for the context's stream and reports device-side errors. */
 int gofr_sync(gofr_ctx *ctx);
 
+/* Several Gofrt::calculate windows of the resident frames in one persistent
+ * launch: window w is calculate(primos[w]) with the parameters p (the segmented
+ * loop of pyanalisi/analysis.py:131-142 and pyanalisi/common.py:196-203, or the
+ * blocks of lib/include/blockaverage.h:107-190).  counts_host receives
+ * [nwin][nparts][leff][nch][nbin] (nparts taken as 1 when p->nparts <= 1).
+ * The FP32 kernel runs every (window, partition) in one launch; parameters
+ * that need the FP64 or cell-list kernel run one launch per window. */
+int gofr_run_windows(gofr_ctx *ctx, const gofr_params *p, unsigned nwin,
+                     const unsigned long long *primos, unsigned long long *counts_host);
+
 /* Statistics of the last completed run. */
 int gofr_get_stats(const gofr_ctx *ctx, gofr_stats *out);
 
