@@ -12,7 +12,7 @@
 // device copies of the frames and per-run tables.  This entry point instead
 // reads the caller's device buffers directly and keeps its only scratch --
 // the type-pair channel table and the device error word -- in the
-// file-scope array g_noalloc_scratch below (NOALLOC_SCRATCH_BYTES bytes; every
+// file-scope array g_noalloc_scratch below (SCRATCH_BYTES = 768 bytes; every
 // GPU that loads this library holds it until the process exits).  The
 // histogram itself lives in shared memory and is added straight into the
 // caller's output.
