@@ -536,6 +536,8 @@ bool cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl)
 {
     if (t.tric || !t.box_constant || p.nparts > 1) return false;
     if (!(p.rmax > 0.0)) return false;
+    if (cell_smem_bytes((int)(t.ntypes * (t.ntypes + 1)), (int)p.nbin, (int)t.ntypes) > 160 * 1024)
+        return false;  // large histograms use the global-memory form of the all-pairs kernel
     long long ncell = 1;
     for (int k = 0; k < 3; ++k) {
         const double L = 2.0 * t.h_box[3 + k];
@@ -646,13 +648,16 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
         CK(cudaMemcpyAsync(ctx->d_win, pl.w.win.data(), pl.w.win.size() * sizeof(float2),
                            cudaMemcpyHostToDevice, ctx->stream));
     }
-    const int smem = pairs_smem_bytes(pl.kind, (int)rs.nch, (int)p.nbin, (int)t.ntypes);
     int max_smem = 0;
     CK(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    // a histogram that would not leave room for one CTA (with headroom) per SM
+    // goes to global memory: slower atomics, same counts
+    const bool ghist = pairs_smem_bytes(pl.kind, (int)rs.nch, (int)p.nbin, (int)t.ntypes) >
+                       max_smem - 8192;
+    const int smem = pairs_smem_bytes(pl.kind, (int)rs.nch, (int)p.nbin, (int)t.ntypes, ghist);
     if (smem > max_smem)
-        return fail(ctx, GOFR_ERR_UNSUPPORTED,
-                    "histogram of %u channels x %u bins needs %d B of shared memory (max %d)",
-                    rs.nch, p.nbin, smem, max_smem);
+        return fail(ctx, GOFR_ERR_UNSUPPORTED, "kernel needs %d B of shared memory (max %d)",
+                    smem, max_smem);
     PairLaunch L{};
     L.pos32 = t.pos32;
     L.types8 = t.types8;
@@ -674,6 +679,7 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
     L.skip = (int)rs.skip;
     L.primo = (long long)p.primo;
     L.tric = t.tric;
+    L.ghist = ghist ? 1 : 0;
     BinMap bm(p.rmin, p.rmax, p.nbin);
     L.rmin = bm.rmin; L.rmax = bm.rmax; L.dr = bm.dr; L.rmin2 = bm.rmin2; L.rmax2 = bm.rmax2;
     if (pl.kind == 0) {
@@ -683,7 +689,7 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
         L.inv_dr_f = (float)(1.0 / bm.dr);
         L.wlim = (float)(0.5 - pl.b.eta);
     }
-    if (pl.cells) {
+    if (pl.cells && !ghist) {
         TrajDev &tm = const_cast<TrajDev &>(t);
         if (tm.cell_nc[0] != pl.nc[0] || tm.cell_nc[1] != pl.nc[1] || tm.cell_nc[2] != pl.nc[2]) {
             cudaFree(tm.d_cstart); cudaFree(tm.d_sid); cudaFree(tm.d_spos); cudaFree(tm.d_stype);
@@ -1132,7 +1138,10 @@ int gofr_run_windows(gofr_ctx *ctx, const gofr_params *p, unsigned nwin,
     PairLaunch *d_l = nullptr;
     WorkDesc *d_w = nullptr;
     unsigned *d_head = nullptr;
-    bool one_launch = pl.kind == 0 && !pl.cells && !pl.empty && rs.n_lags > 0 && rs.n_orig > 0;
+    int max_smem = 0;
+    CK(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    bool one_launch = pl.kind == 0 && !pl.cells && !pl.empty && rs.n_lags > 0 && rs.n_orig > 0 &&
+                      batch_smem_bytes((int)p->nbin, (int)rs.nch, (int)t.ntypes) <= max_smem - 8192;
     if (!one_launch) {
         for (unsigned w = 0; w < nwin && rc == GOFR_OK; ++w) {
             gofr_params q = *p;

@@ -53,6 +53,8 @@ struct PairLaunch {
     double rmin, rmax, dr, rmin2, rmax2;  // reference binning constants
     int tric;
     int wchk;                 // batched kernel: per-pair wrap-decision check on
+    int ghist;                // histogram too large for shared memory: atomics go
+                              // straight to the u64 counts in global memory
 };
 
 // One work descriptor of the batched kernel: origins [k0, k1) of one
@@ -93,7 +95,7 @@ int launch_convert(const double *pos64, const int *types, size_t T, size_t N, do
 // kind: 0 = FP32+recheck, 1 = FP64.  wrapcheck only for kind 0.
 int launch_pairs(const PairLaunch &P, int kind, bool wrapcheck, int num_sms, cudaStream_t s,
                  size_t *smem_bytes_out);
-int pairs_smem_bytes(int kind, int nch, int nbin, int ntypes);
+int pairs_smem_bytes(int kind, int nch, int nbin, int ntypes, bool ghist = false);
 int pairs_tile_atoms(int kind);
 int batch_smem_bytes(int max_nbin, int max_nch, int max_ntypes);
 int prepare_batch(int max_nbin, int max_nch, int max_ntypes, bool tric, int num_sms, int n_work,

@@ -85,20 +85,29 @@ __device__ __forceinline__ void add_stats(unsigned long long *stats, unsigned lo
 }
 
 // Exact FP64 re-evaluation of one pair, exactly as the reference computes it.
+// Adds one count to bin b of channel ch: the shared-memory histogram, or the
+// lag's u64 counts in global memory when the histogram does not fit (ghist).
+__device__ __forceinline__ void hist_add(unsigned *hist, unsigned long long *gcounts, int ch,
+                                         int nbin, int b)
+{
+    if (gcounts) atomicAdd(gcounts + ch * nbin + b, 1ull);
+    else atomicAdd(hist + ch * nbin + b, 1u);
+}
+
 template <bool TRI>
 __device__ __forceinline__ void recheck_pair(const double *__restrict__ pos64,
                                              const double *__restrict__ box64, long long N,
                                              long long fo, long long fl, int ia, int ja,
                                              unsigned *hist, int ch, int nbin, double rmin,
                                              double dr, double rmin2, double rmax2,
-                                             unsigned *err)
+                                             unsigned *err, unsigned long long *gcounts = nullptr)
 {
     const double *xi = pos64 + (fo * N + ia) * 3;
     const double *xj = pos64 + (fl * N + ja) * 3;
     const double *box = box64 + fo * 9;
     double d2 = ref_d2<TRI>(xi[0], xi[1], xi[2], xj[0], xj[1], xj[2], box, err);
     int b = ref_bin(d2, rmin, dr, rmin2, rmax2, nbin);
-    if (b >= 0) atomicAdd(hist + ch * nbin + b, 1u);
+    if (b >= 0) hist_add(hist, gcounts, ch, nbin, b);
 }
 
 // ---------------------------------------------------------------------------
@@ -225,7 +234,7 @@ __device__ __forceinline__ f2 pair2(f2 xi, f2 yi, f2 zi, f2 xj, f2 yj, f2 zj, co
 // Shared-memory layout of the FP32 kernel (byte offsets).
 struct F32Smem {
     int jx, jt, bars, flag, rqn, win, hist, chtab, slots, rq, total;
-    __host__ __device__ F32Smem(int nbin, int nch, int ntypes)
+    __host__ __device__ F32Smem(int nbin, int nch, int ntypes, bool ghist = false)
     {
         int o = 0;
         jx = o;    o += 2 * 3 * TJ32 * 4;        // [2][3][TJ] floats
@@ -236,7 +245,7 @@ struct F32Smem {
         slots = o; o += SLOTS * NT * 8;          // [SLOTS][NT] uint2
         rq = o;    o += QCAP * 16;               // [QCAP] uint4
         win = o;   o += nbin * 8;                // [nbin] float2
-        hist = o;  o += nch * nbin * 4;          // [nch][nbin] u32
+        hist = o;  o += ghist ? 0 : nch * nbin * 4;  // [nch][nbin] u32
         chtab = o; o += ntypes * ntypes * 2;     // [ntypes][ntypes] u16
         total = (o + 127) / 128 * 128;
     }
@@ -323,6 +332,8 @@ __device__ __forceinline__ bool f32_item(const PairLaunch &P, const F32Views &V,
     uint2 *const my_slots = V.slots + tid;
     const long long fo = P.primo + (long long)k * P.skip;
     const long long fl = fo + (long long)lag_idx * P.every;
+    unsigned long long *const gc =
+        P.ghist ? P.counts + (long long)lag_idx * P.every * P.nch * P.nbin : nullptr;
     Box2 bx;
     {
         const Box32 b = P.box32[fo];
@@ -412,7 +423,7 @@ __device__ __forceinline__ bool f32_item(const PairLaunch &P, const F32Views &V,
                         int bi = __float2int_rd(__fmul_rn(__fsub_rn(rr_, P.rmin_f), P.inv_dr_f));
                         bi = min(max(bi, 0), P.nbin - 1);
                         const float2 w = V.win[bi];
-                        if (d2 >= w.x && d2 <= w.y) atomicAdd(V.hist + ch * P.nbin + bi, 1u);
+                        if (d2 >= w.x && d2 <= w.y) hist_add(V.hist, gc, ch, P.nbin, bi);
                         else need = true;
                     }
                     if (need) {
@@ -422,7 +433,7 @@ __device__ __forceinline__ bool f32_item(const PairLaunch &P, const F32Views &V,
                             V.rq[slot] = make_uint4((unsigned)ia, (unsigned)ja, (unsigned)ch, 0u);
                         } else {
                             recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, ia, ja, V.hist, ch,
-                                              P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err);
+                                              P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err, gc);
                         }
                     }
                 }
@@ -474,7 +485,7 @@ __device__ __forceinline__ bool f32_item(const PairLaunch &P, const F32Views &V,
             for (int q = tid; q < n; q += NT) {
                 const uint4 e = V.rq[q];
                 recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, (int)e.x, (int)e.y, V.hist,
-                                  (int)e.z, P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err);
+                                  (int)e.z, P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err, gc);
             }
             __syncthreads();
             if (tid == 0) *V.rqn = 0;
@@ -486,7 +497,7 @@ __device__ __forceinline__ bool f32_item(const PairLaunch &P, const F32Views &V,
     for (int q = tid; q < n; q += NT) {
         const uint4 e = V.rq[q];
         recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, (int)e.x, (int)e.y, V.hist, (int)e.z,
-                          P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err);
+                          P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err, gc);
     }
     __syncthreads();
     if (tid == 0) *V.rqn = 0;
@@ -498,9 +509,9 @@ template <bool TRI, bool WCHK>
 __global__ void __launch_bounds__(NT, 2) k_pairs_f32(const PairLaunch P)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    const F32Views V(smem, F32Smem(P.nbin, P.nch, P.ntypes));
+    const F32Views V(smem, F32Smem(P.nbin, P.nch, P.ntypes, P.ghist != 0));
     const int tid = threadIdx.x;
-    const int hlen = P.nch * P.nbin;
+    const int hlen = P.ghist ? 0 : P.nch * P.nbin;
     for (int i = tid; i < P.nbin; i += NT) V.win[i] = P.win[i];
     for (int i = tid; i < hlen; i += NT) V.hist[i] = 0u;
     for (int i = tid; i < P.ntypes * P.ntypes; i += NT) V.chtab[i] = P.chtab[i];
@@ -518,7 +529,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f32(const PairLaunch P)
         int lag_idx, itile, k;
         decompose(item, P, lag_idx, itile, k);
         if (lag_idx != cur_lag || since_flush >= flush_every) {
-            if (cur_lag >= 0)
+            if (cur_lag >= 0 && hlen)
                 flush_hist(V.hist, hlen, P.counts + (long long)cur_lag * P.every * hlen);
             cur_lag = lag_idx;
             since_flush = 0;
@@ -529,7 +540,8 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f32(const PairLaunch P)
             return;
         }
     }
-    if (cur_lag >= 0) flush_hist(V.hist, hlen, P.counts + (long long)cur_lag * P.every * hlen);
+    if (cur_lag >= 0 && hlen)
+        flush_hist(V.hist, hlen, P.counts + (long long)cur_lag * P.every * hlen);
     add_stats(P.stats, th.n_cand, th.n_rech);
 }
 
@@ -602,10 +614,10 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f64(const PairLaunch P)
     double *jz = jy + TJ64;
     int *jt = reinterpret_cast<int *>(jz + TJ64);
     unsigned *hist = reinterpret_cast<unsigned *>(jt + TJ64);
-    unsigned short *chtab = reinterpret_cast<unsigned short *>(hist + P.nch * P.nbin);
+    const int hlen = P.ghist ? 0 : P.nch * P.nbin;
+    unsigned short *chtab = reinterpret_cast<unsigned short *>(hist + hlen);
 
     const int tid = threadIdx.x;
-    const int hlen = P.nch * P.nbin;
     const int half = P.nch / 2;
     for (int i = tid; i < hlen; i += NT) hist[i] = 0u;
     for (int i = tid; i < P.ntypes * P.ntypes; i += NT) chtab[i] = P.chtab[i];
@@ -623,7 +635,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f64(const PairLaunch P)
         int lag_idx, itile, k;
         decompose(item, P, lag_idx, itile, k);
         if (lag_idx != cur_lag || since_flush >= flush_every) {
-            if (cur_lag >= 0)
+            if (cur_lag >= 0 && hlen)
                 flush_hist(hist, hlen, P.counts + (long long)cur_lag * P.every * hlen);
             cur_lag = lag_idx;
             since_flush = 0;
@@ -631,6 +643,8 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f64(const PairLaunch P)
         ++since_flush;
         const long long fo = P.primo + (long long)k * P.skip;
         const long long fl = fo + (long long)lag_idx * P.every;
+        unsigned long long *const gc =
+            P.ghist ? P.counts + (long long)lag_idx * P.every * P.nch * P.nbin : nullptr;
         double box[9];
 #pragma unroll
         for (int q = 0; q < 9; ++q) box[q] = P.box64[fo * 9 + q];
@@ -666,13 +680,14 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f64(const PairLaunch P)
                     int b = ref_bin(d2, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
                     if (b >= 0) {
                         int ch = chtab[ti[r] * P.ntypes + tj_] + (ia[r] == jbase + jj ? half : 0);
-                        atomicAdd(hist + ch * P.nbin + b, 1u);
+                        hist_add(hist, gc, ch, P.nbin, b);
                     }
                 }
             }
         }
     }
-    if (cur_lag >= 0) flush_hist(hist, hlen, P.counts + (long long)cur_lag * P.every * hlen);
+    if (cur_lag >= 0 && hlen)
+        flush_hist(hist, hlen, P.counts + (long long)cur_lag * P.every * hlen);
 }
 
 // ---------------------------------------------------------------------------
@@ -777,10 +792,11 @@ int launch_zero_u64(unsigned long long *p, size_t n, cudaStream_t s)
     return cuda_ok(cudaGetLastError());
 }
 
-int pairs_smem_bytes(int kind, int nch, int nbin, int ntypes)
+int pairs_smem_bytes(int kind, int nch, int nbin, int ntypes, bool ghist)
 {
-    if (kind == 0) return F32Smem(nbin, nch, ntypes).total;
-    size_t b = (size_t)TJ64 * (3 * 8 + 4) + (size_t)nch * nbin * 4 + (size_t)ntypes * ntypes * 2;
+    if (kind == 0) return F32Smem(nbin, nch, ntypes, ghist).total;
+    size_t b = (size_t)TJ64 * (3 * 8 + 4) + (ghist ? 0 : (size_t)nch * nbin * 4) +
+               (size_t)ntypes * ntypes * 2;
     return (int)((b + 127) / 128 * 128);
 }
 
@@ -841,7 +857,7 @@ int launch_batch_grid(const PairLaunch *d_trajs, const WorkDesc *d_work, int n_w
 int launch_pairs(const PairLaunch &P, int kind, bool wrapcheck, int num_sms, cudaStream_t s,
                  size_t *smem_bytes_out)
 {
-    const int smem = pairs_smem_bytes(kind, P.nch, P.nbin, P.ntypes);
+    const int smem = pairs_smem_bytes(kind, P.nch, P.nbin, P.ntypes, P.ghist != 0);
     if (smem_bytes_out) *smem_bytes_out = (size_t)smem;
     if (P.n_items <= 0) return 0;
     if (kind == 0) {
