@@ -11,12 +11,17 @@
 //   * the reference's double result buffer from counts, including its exact
 //     per-thread fold (gofr_counts_to_buffer).
 #include <algorithm>
+#include <array>
 #include <cfloat>
 #include <cmath>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -532,7 +537,8 @@ struct Plan {
 // neighbouring cells on every axis (periodically); at least 3 cells per axis.
 // The block of cells one CTA takes is chosen to minimise the evaluated pairs
 // per useful first-atom slot.
-bool cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl)
+bool cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl,
+               std::vector<std::array<int, 3>> *ranked = nullptr)
 {
     if (t.tric || !t.box_constant || p.nparts > 1) return false;
     if (!(p.rmax > 0.0)) return false;
@@ -550,6 +556,7 @@ bool cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl)
     const double per_cell = (double)t.N / (double)ncell;
     const int TI = cell_block_atoms();
     double best = 1e300;
+    std::vector<std::pair<double, std::array<int, 3>>> all;
     for (int bx = 1; bx <= 4; ++bx)
         for (int by = 1; by <= 4; ++by)
             for (int bz = 1; bz <= 4; ++bz) {
@@ -561,6 +568,7 @@ bool cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl)
                 const double nbhd = (double)std::min(bx + 2, pl.nc[0]) * jy * jz;
                 const double slots = std::ceil(std::max(atoms, 1.0) / TI) * TI;
                 const double cost = nbhd * slots / std::max(atoms, 1e-9);
+                all.push_back({cost, {bx, by, bz}});
                 if (cost < best) {
                     best = cost;
                     pl.blk[0] = bx; pl.blk[1] = by; pl.blk[2] = bz;
@@ -569,15 +577,36 @@ bool cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl)
             }
     if (best >= 1e300) return false;
     for (int k = 0; k < 3; ++k) pl.nb[k] = (pl.nc[k] + pl.blk[k] - 1) / pl.blk[k];
+    if (ranked) {
+        std::stable_sort(all.begin(), all.end(),
+                         [](const auto &a, const auto &b) { return a.first < b.first; });
+        ranked->clear();
+        for (auto &c : all) ranked->push_back(c.second);
+    }
     return true;
+}
+
+void set_cell_block(Plan &pl, const std::array<int, 3> &b)
+{
+    for (int k = 0; k < 3; ++k) {
+        pl.blk[k] = b[k];
+        pl.nb[k] = (pl.nc[k] + b[k] - 1) / b[k];
+    }
+    pl.cell_fraction = (double)std::min(b[0] + 2, pl.nc[0]) * std::min(b[1] + 2, pl.nc[1]) *
+                       std::min(b[2] + 2, pl.nc[2]) / ((double)pl.nc[0] * pl.nc[1] * pl.nc[2]);
 }
 
 int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
 {
     const int req = p.kernel;
     if (req != GOFR_KERNEL_AUTO && req != GOFR_KERNEL_F32_RECHECK && req != GOFR_KERNEL_F64 &&
-        req != GOFR_KERNEL_CELL)
+        req != GOFR_KERNEL_CELL && req != GOFR_KERNEL_TUNED)
         return fail(ctx, GOFR_ERR_ARG, "unknown kernel %d", req);
+    if (req == GOFR_KERNEL_TUNED) {
+        gofr_params q = p;
+        q.kernel = GOFR_KERNEL_AUTO;
+        return make_plan(ctx, t, q, pl);
+    }
     const bool reg = regular_bins(p.rmin, p.rmax, p.nbin);
     if (reg) {
         pl.th.resize(p.nbin + 1);
@@ -758,6 +787,145 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
     return GOFR_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Autotuner: for GOFR_KERNEL_TUNED, times the all-pairs FP32 kernel and the
+// cell-list kernel with its best-ranked block shapes on a sample of the job
+// (its first origin and up to four lags) and keeps the fastest per key.
+// ---------------------------------------------------------------------------
+struct TuneChoice {
+    bool cells = false;
+    std::array<int, 3> blk{{1, 1, 1}};
+};
+
+std::mutex g_tune_mutex;
+std::map<std::string, TuneChoice> g_tune;
+bool g_tune_loaded = false;
+
+std::string tune_key(const TrajDev &t, const gofr_params &p, const Plan &cellpl, bool eligible)
+{
+    int lg = 0;
+    while ((1ull << (lg + 1)) <= (unsigned long long)t.N) ++lg;
+    std::ostringstream k;
+    k << "n2^" << lg << "_bins" << p.nbin << "_types" << t.ntypes << (t.tric ? "_tric" : "_ortho");
+    if (eligible) k << "_cells" << cellpl.nc[0] << "x" << cellpl.nc[1] << "x" << cellpl.nc[2];
+    return k.str();
+}
+
+void tune_load_file()
+{
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char *path = std::getenv("ANALISI_GB300_TUNE_CACHE");
+    if (!path) return;
+    std::ifstream in(path);
+    std::string key;
+    int cells, b0, b1, b2;
+    while (in >> key >> cells >> b0 >> b1 >> b2) {
+        TuneChoice c;
+        c.cells = cells != 0;
+        c.blk = {{b0, b1, b2}};
+        g_tune[key] = c;
+    }
+}
+
+void tune_store_file(const std::string &key, const TuneChoice &c)
+{
+    const char *path = std::getenv("ANALISI_GB300_TUNE_CACHE");
+    if (!path) return;
+    std::ofstream out(path, std::ios::app);
+    out << key << " " << (c.cells ? 1 : 0) << " " << c.blk[0] << " " << c.blk[1] << " " << c.blk[2]
+        << "\n";
+}
+
+int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const RunShape &rs,
+                const Plan &pl, unsigned long long *counts, unsigned long long *pairs_out);
+
+// Times one plan on the sample parameters; returns milliseconds (or < 0).
+double tune_time(gofr_ctx *ctx, const TrajDev &t, const gofr_params &q, const Plan &pl)
+{
+    RunShape rs;
+    if (shape_of(ctx, t, q, rs)) return -1.0;
+    if (ensure(ctx, ctx->d_counts, ctx->cap_counts, rs.data_length)) return -1.0;
+    double best = -1.0;
+    for (int rep = 0; rep < 2; ++rep) {  // the first run also builds cell lists
+        if (cudaMemsetAsync(ctx->d_counts, 0, rs.data_length * 8, ctx->stream) != cudaSuccess)
+            return -1.0;
+        cudaEventRecord(ctx->ev[1], ctx->stream);
+        unsigned long long pairs = 0;
+        if (enqueue_run(ctx, t, q, rs, pl, ctx->d_counts, &pairs)) return -1.0;
+        cudaEventRecord(ctx->ev[2], ctx->stream);
+        if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return -1.0;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+        best = ms;
+    }
+    return best;
+}
+
+// Applies (and if needed measures) the tuned choice for p into pl.
+int tune_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
+{
+    if (pl.kind != 0 || pl.wrapcheck || pl.empty) return GOFR_OK;  // nothing to choose
+    Plan cellpl = pl;
+    std::vector<std::array<int, 3>> ranked;
+    const bool eligible = cell_plan(t, p, cellpl, &ranked);
+    if (!eligible) {
+        pl.cells = false;
+        return GOFR_OK;
+    }
+    const std::string key = tune_key(t, p, cellpl, eligible);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        tune_load_file();
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            if (it->second.cells) {
+                pl = cellpl;
+                pl.cells = true;
+                set_cell_block(pl, it->second.blk);
+            } else {
+                pl.cells = false;
+            }
+            return GOFR_OK;
+        }
+    }
+    // sample of the job: its first origin, up to four lags
+    gofr_params q = p;
+    q.kernel = GOFR_KERNEL_AUTO;
+    q.nparts = 1;
+    q.tmax = std::min<unsigned>(p.tmax ? p.tmax : p.ntimesteps, 4);
+    q.ntimesteps = std::max<unsigned>(q.tmax, 1);
+    q.skip = q.ntimesteps;
+    Plan base = pl;
+    base.cells = false;
+    double best_ms = tune_time(ctx, t, q, base);
+    TuneChoice choice;
+    for (size_t c = 0; c < ranked.size() && c < 3; ++c) {
+        Plan cp = cellpl;
+        cp.cells = true;
+        set_cell_block(cp, ranked[c]);
+        const double ms = tune_time(ctx, t, q, cp);
+        if (ms > 0 && (best_ms < 0 || ms < best_ms)) {
+            best_ms = ms;
+            choice.cells = true;
+            choice.blk = ranked[c];
+        }
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tune[key] = choice;
+        tune_store_file(key, choice);
+    }
+    if (choice.cells) {
+        pl = cellpl;
+        pl.cells = true;
+        set_cell_block(pl, choice.blk);
+    } else {
+        pl.cells = false;
+    }
+    return GOFR_OK;
+}
+
 int run_common(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_dev,
                unsigned long long *counts_host)
 {
@@ -771,6 +939,10 @@ int run_common(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_d
     Plan pl;
     rc = make_plan(ctx, t, *p, pl);
     if (rc) return rc;
+    if (p->kernel == GOFR_KERNEL_TUNED && p->nparts <= 1) {
+        rc = tune_plan(ctx, t, *p, pl);
+        if (rc) return rc;
+    }
     const unsigned nparts = p->nparts > 1 ? p->nparts : 1;
     const size_t n_out = rs.data_length * nparts;
     unsigned long long *out = counts_dev;

@@ -18,7 +18,7 @@ STATUS = {
     -5: "GOFR_ERR_STATE", -6: "GOFR_ERR_DEVICE", -7: "GOFR_ERR_UNSUPPORTED",
 }
 BOX_ORTHO, BOX_TRICLINIC = 0, 1
-KERNELS = {"auto": 0, "f32": 1, "f64": 2, "cell": 3}
+KERNELS = {"auto": 0, "f32": 1, "f64": 2, "cell": 3, "tuned": 4}
 
 # every symbol the header declares (checked by the CPU tests)
 EXPORTED = [

@@ -54,3 +54,21 @@ def test_cell_kernel_refuses_small_box(gpu_engine):
                              skip=1, every=1, ntimesteps=3, primo=0)
     with pytest.raises(engine.GofrError):
         _run(gpu_engine, w, "cell")
+
+
+def test_tuned_kernel_choice_is_exact_and_cached(gpu_engine, oracle_mod, tmp_path, monkeypatch):
+    """GOFR_KERNEL_TUNED times the all-pairs and cell-list forms on a sample and
+    keeps the fastest; whichever wins, the counts are the oracle's, and the
+    choice is written to the cache file named by ANALISI_GB300_TUNE_CACHE."""
+    seed, N, T, L, sigma, counts, params = CASES[0]
+    w = workloads.small_case(seed, N, T, L, sigma, counts, **params)
+    p = w["params"]
+    ref = oracle_mod.gofrt_counts(w["positions"], w["boxes"], w["type_ids"], w["ntypes"],
+                                  p["rmin"], p["rmax"], p["nbin"], p["tmax"], 8, p["skip"],
+                                  p["every"], p["ntimesteps"], p["primo"])
+    a, st = _run(gpu_engine, w, "tuned")
+    np.testing.assert_array_equal(a, ref)
+    assert st["kernel_used"] in (1, 3)
+    b, st2 = _run(gpu_engine, w, "tuned")
+    np.testing.assert_array_equal(b, ref)
+    assert st2["kernel_used"] == st["kernel_used"]
