@@ -524,7 +524,9 @@ struct Plan {
     int kind = 1;              // 0 = FP32+recheck, 1 = FP64
     bool cells = false;        // FP32 kernel in its cell-list form
     int nc[3] = {0, 0, 0}, blk[3] = {1, 1, 1}, nb[3] = {1, 1, 1};
-    double cell_fraction = 1.0;  // evaluated pairs / all pairs (estimate)
+    int reach = 1, cell_r = 4;   // neighbour reach in cells, first atoms per thread
+    double cell_fraction = 1.0;  // neighbourhood cells / all cells
+    double cell_time = 1e300;    // modelled time / the all-pairs kernel's
     bool wrapcheck = false;
     bool empty = false;        // accepted window empty: nothing can be counted
     Windows w;
@@ -532,69 +534,138 @@ struct Plan {
     std::vector<double> th;
 };
 
-// Cell-list grid for an orthorhombic box that does not change: cells of edge
-// >= rmax (1 + 1e-6), so two atoms at minimum-image distance <= rmax are in
-// neighbouring cells on every axis (periodically); at least 3 cells per axis.
-// The block of cells one CTA takes is chosen to minimise the evaluated pairs
-// per useful first-atom slot.
-bool cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl,
-               std::vector<std::array<int, 3>> *ranked = nullptr)
+// One cell-list configuration: cells of edge >= rmax (1 + 1e-6) / reach, so
+// two atoms at minimum-image distance <= rmax are at most `reach` cells apart
+// on every axis (periodically); at least 2 reach + 1 cells per axis.  A CTA
+// takes a block of bx*by*bz cells with r first atoms per thread.
+struct CellCand {
+    int reach = 1, r = 4;
+    int nc[3] = {0, 0, 0};
+    std::array<int, 3> blk{{1, 1, 1}};
+    double fraction = 1.0;  // neighbourhood cells / all cells
+    double cost = 1e300;    // evaluated first-slot x second-atom pairs / N^2
+    double time = 1e300;    // modelled time / the all-pairs kernel's
+};
+
+bool cell_eligible(const TrajDev &t, const gofr_params &p)
 {
     if (t.tric || !t.box_constant || p.nparts > 1) return false;
     if (!(p.rmax > 0.0)) return false;
-    if (cell_smem_bytes((int)(t.ntypes * (t.ntypes + 1)), (int)p.nbin, (int)t.ntypes) > 160 * 1024)
-        return false;  // large histograms use the global-memory form of the all-pairs kernel
+    // large histograms use the global-memory form of the all-pairs kernel
+    return cell_smem_bytes((int)(t.ntypes * (t.ntypes + 1)), (int)p.nbin, (int)t.ntypes) <=
+           160 * 1024;
+}
+
+bool cell_grid(const TrajDev &t, const gofr_params &p, int reach, int nc[3])
+{
     long long ncell = 1;
     for (int k = 0; k < 3; ++k) {
         const double L = 2.0 * t.h_box[3 + k];
-        const double nc = std::floor(L / (p.rmax * (1.0 + 1e-6)));
-        if (!(nc >= 3.0) || nc > 1024.0) return false;
-        pl.nc[k] = (int)nc;
-        ncell *= pl.nc[k];
+        const double n = std::floor(L * reach / (p.rmax * (1.0 + 1e-6)));
+        if (!(n >= 2.0 * reach + 1.0) || n > 1024.0) return false;
+        nc[k] = (int)n;
+        ncell *= nc[k];
     }
-    if (ncell > (1ll << 22)) return false;
-    const double per_cell = (double)t.N / (double)ncell;
-    const int TI = cell_block_atoms();
-    double best = 1e300;
-    std::vector<std::pair<double, std::array<int, 3>>> all;
-    for (int bx = 1; bx <= 4; ++bx)
-        for (int by = 1; by <= 4; ++by)
-            for (int bz = 1; bz <= 4; ++bz) {
-                if (bx > pl.nc[0] || by > pl.nc[1] || bz > pl.nc[2]) continue;
-                const int jy = std::min(by + 2, pl.nc[1]), jz = std::min(bz + 2, pl.nc[2]);
-                if (2 * jy * jz > cell_max_ranges() || by * bz > cell_max_ranges()) continue;
-                const double atoms = per_cell * bx * by * bz;
-                if (atoms > 0.9 * TI && bx * by * bz > 1) continue;
-                const double nbhd = (double)std::min(bx + 2, pl.nc[0]) * jy * jz;
-                const double slots = std::ceil(std::max(atoms, 1.0) / TI) * TI;
-                const double cost = nbhd * slots / std::max(atoms, 1e-9);
-                all.push_back({cost, {bx, by, bz}});
-                if (cost < best) {
-                    best = cost;
-                    pl.blk[0] = bx; pl.blk[1] = by; pl.blk[2] = bz;
-                    pl.cell_fraction = nbhd / (double)ncell;
+    return ncell <= (1ll << 22);
+}
+
+// Every configuration, fastest (modelled) first.  The cost counts, over all
+// blocks, the first-atom slots a block pays for (its atoms rounded up to
+// whole tiles of 256 r, with room for three standard deviations of density
+// fluctuation) times the atoms of its neighbourhood, relative to the N^2
+// pairs of the all-pairs kernel.  The time model weighs each evaluated pair
+// and each candidate (d <= rmax, binned in the warp flush): measured on the
+// 16k- and 131k-atom workloads, a candidate costs ~6.8 pair evaluations in
+// the all-pairs kernel and ~6.5 in the cell kernel, whose pairs cost ~1.1.
+std::vector<CellCand> cell_candidates(const TrajDev &t, const gofr_params &p)
+{
+    std::vector<CellCand> all;
+    if (!cell_eligible(t, p)) return all;
+    const double vbox = 8.0 * t.h_box[3] * t.h_box[4] * t.h_box[5];
+    const double f_all = std::min(1.0, 4.18879020478639 * p.rmax * p.rmax * p.rmax / vbox);
+    for (int m = 1; m <= 2; ++m) {
+        int nc[3];
+        if (!cell_grid(t, p, m, nc)) continue;
+        const double ncell = (double)nc[0] * nc[1] * nc[2];
+        const double per_cell = (double)t.N / ncell;
+        for (int bx = 1; bx <= 5; ++bx)
+            for (int by = 1; by <= 5; ++by)
+                for (int bz = 1; bz <= 5; ++bz) {
+                    if (bx > nc[0] || by > nc[1] || bz > nc[2]) continue;
+                    const int jy = std::min(by + 2 * m, nc[1]), jz = std::min(bz + 2 * m, nc[2]);
+                    if (2 * jy * jz > cell_max_ranges() || by * bz > cell_max_ranges()) continue;
+                    const double atoms = per_cell * bx * by * bz;
+                    const double nbhd = (double)std::min(bx + 2 * m, nc[0]) * jy * jz;
+                    for (int r = 2; r <= 4; ++r) {
+                        const int TI = cell_block_atoms(r);
+                        const double slots =
+                            std::ceil(std::max(atoms + 3.0 * std::sqrt(atoms), 1.0) / TI) * TI;
+                        CellCand c;
+                        c.reach = m;
+                        c.r = r;
+                        for (int k = 0; k < 3; ++k) c.nc[k] = nc[k];
+                        c.blk = {{bx, by, bz}};
+                        c.fraction = nbhd / ncell;
+                        const double blocks = (double)((nc[0] + bx - 1) / bx) *
+                                              ((nc[1] + by - 1) / by) * ((nc[2] + bz - 1) / bz);
+                        c.cost = blocks * slots * nbhd * per_cell / ((double)t.N * t.N);
+                        const double f_cell = std::min(1.0, f_all / std::max(c.fraction, 1e-9));
+                        c.time = c.cost * (1.1 + 6.5 * f_cell) / (1.0 + 6.8 * f_all);
+                        all.push_back(c);
+                    }
                 }
-            }
-    if (best >= 1e300) return false;
-    for (int k = 0; k < 3; ++k) pl.nb[k] = (pl.nc[k] + pl.blk[k] - 1) / pl.blk[k];
-    if (ranked) {
-        std::stable_sort(all.begin(), all.end(),
-                         [](const auto &a, const auto &b) { return a.first < b.first; });
-        ranked->clear();
-        for (auto &c : all) ranked->push_back(c.second);
     }
+    std::stable_sort(all.begin(), all.end(),
+                     [](const CellCand &a, const CellCand &b) { return a.time < b.time; });
+    return all;
+}
+
+void apply_cell(Plan &pl, const CellCand &c)
+{
+    pl.reach = c.reach;
+    pl.cell_r = c.r;
+    for (int k = 0; k < 3; ++k) {
+        pl.nc[k] = c.nc[k];
+        pl.blk[k] = c.blk[k];
+        pl.nb[k] = (c.nc[k] + c.blk[k] - 1) / c.blk[k];
+    }
+    pl.cell_fraction = c.fraction;
+    pl.cell_time = c.time;
+}
+
+// ANALISI_GB300_CELL_PLAN="reach,r,bx,by,bz" fixes the cell-list
+// configuration (for reproducible timings); it must be one the planner
+// accepts for the job, else the ranked choice stands.
+bool cell_override(const TrajDev &t, const gofr_params &p, CellCand &out)
+{
+    const char *env = std::getenv("ANALISI_GB300_CELL_PLAN");
+    if (!env) return false;
+    int v[5];
+    if (std::sscanf(env, "%d,%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3], &v[4]) != 5) return false;
+    for (const CellCand &c : cell_candidates(t, p))
+        if (c.reach == v[0] && c.r == v[1] && c.blk[0] == v[2] && c.blk[1] == v[3] &&
+            c.blk[2] == v[4]) {
+            out = c;
+            return true;
+        }
+    return false;
+}
+
+bool cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl)
+{
+    CellCand c;
+    if (!cell_override(t, p, c)) {
+        const std::vector<CellCand> all = cell_candidates(t, p);
+        if (all.empty()) return false;
+        c = all.front();
+    }
+    apply_cell(pl, c);
     return true;
 }
 
-void set_cell_block(Plan &pl, const std::array<int, 3> &b)
-{
-    for (int k = 0; k < 3; ++k) {
-        pl.blk[k] = b[k];
-        pl.nb[k] = (pl.nc[k] + b[k] - 1) / b[k];
-    }
-    pl.cell_fraction = (double)std::min(b[0] + 2, pl.nc[0]) * std::min(b[1] + 2, pl.nc[1]) *
-                       std::min(b[2] + 2, pl.nc[2]) / ((double)pl.nc[0] * pl.nc[1] * pl.nc[2]);
-}
+// AUTO takes the cell-list form when its modelled time is below this share of
+// the all-pairs kernel's (a margin for the model's error).
+constexpr double kCellAutoTime = 0.85;
 
 int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
 {
@@ -634,7 +705,7 @@ int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
     }
     if ((req == GOFR_KERNEL_CELL || req == GOFR_KERNEL_AUTO) && !pl.wrapcheck) {
         Plan c = pl;
-        if (cell_plan(t, p, c) && (req == GOFR_KERNEL_CELL || c.cell_fraction < 0.35)) {
+        if (cell_plan(t, p, c) && (req == GOFR_KERNEL_CELL || c.cell_time < kCellAutoTime)) {
             c.cells = true;
             pl = c;
         }
@@ -757,6 +828,8 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
         C.sid = t.d_sid;
         C.stype = t.d_stype;
         for (int k = 0; k < 3; ++k) { C.nc[k] = pl.nc[k]; C.b[k] = pl.blk[k]; C.nb[k] = pl.nb[k]; }
+        C.reach = pl.reach;
+        C.r = pl.cell_r;
         const int csmem = cell_smem_bytes(L.nch, L.nbin, L.ntypes);
         if (csmem > max_smem)
             return fail(ctx, GOFR_ERR_UNSUPPORTED, "cell-list histogram does not fit shared memory");
@@ -789,11 +862,13 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
 
 // ---------------------------------------------------------------------------
 // Autotuner: for GOFR_KERNEL_TUNED, times the all-pairs FP32 kernel and the
-// cell-list kernel with its best-ranked block shapes on a sample of the job
-// (its first origin and up to four lags) and keeps the fastest per key.
+// cell-list kernel in its best-estimated configurations (reach, atoms per
+// thread, block shape) on a sample of the job (its first origin and first
+// lags) and keeps the fastest per key.
 // ---------------------------------------------------------------------------
 struct TuneChoice {
     bool cells = false;
+    int reach = 1, r = 4;
     std::array<int, 3> blk{{1, 1, 1}};
 };
 
@@ -801,16 +876,21 @@ std::mutex g_tune_mutex;
 std::map<std::string, TuneChoice> g_tune;
 bool g_tune_loaded = false;
 
-std::string tune_key(const TrajDev &t, const gofr_params &p, const Plan &cellpl, bool eligible)
+std::string tune_key(const TrajDev &t, const gofr_params &p)
 {
     int lg = 0;
     while ((1ull << (lg + 1)) <= (unsigned long long)t.N) ++lg;
     std::ostringstream k;
     k << "n2^" << lg << "_bins" << p.nbin << "_types" << t.ntypes << (t.tric ? "_tric" : "_ortho");
-    if (eligible) k << "_cells" << cellpl.nc[0] << "x" << cellpl.nc[1] << "x" << cellpl.nc[2];
+    int nc[3];
+    if (cell_eligible(t, p) && cell_grid(t, p, 2, nc))
+        k << "_halfcells" << nc[0] << "x" << nc[1] << "x" << nc[2];
+    else if (cell_eligible(t, p) && cell_grid(t, p, 1, nc))
+        k << "_cells" << nc[0] << "x" << nc[1] << "x" << nc[2];
     return k.str();
 }
 
+// Cache file lines: key cells reach r bx by bz (other lines are skipped).
 void tune_load_file()
 {
     if (g_tune_loaded) return;
@@ -818,11 +898,16 @@ void tune_load_file()
     const char *path = std::getenv("ANALISI_GB300_TUNE_CACHE");
     if (!path) return;
     std::ifstream in(path);
-    std::string key;
-    int cells, b0, b1, b2;
-    while (in >> key >> cells >> b0 >> b1 >> b2) {
+    std::string line;
+    while (std::getline(in, line)) {
+        std::istringstream ls(line);
+        std::string key;
+        int cells, m, r, b0, b1, b2;
+        if (!(ls >> key >> cells >> m >> r >> b0 >> b1 >> b2)) continue;
         TuneChoice c;
         c.cells = cells != 0;
+        c.reach = m;
+        c.r = r;
         c.blk = {{b0, b1, b2}};
         g_tune[key] = c;
     }
@@ -833,8 +918,21 @@ void tune_store_file(const std::string &key, const TuneChoice &c)
     const char *path = std::getenv("ANALISI_GB300_TUNE_CACHE");
     if (!path) return;
     std::ofstream out(path, std::ios::app);
-    out << key << " " << (c.cells ? 1 : 0) << " " << c.blk[0] << " " << c.blk[1] << " " << c.blk[2]
-        << "\n";
+    out << key << " " << (c.cells ? 1 : 0) << " " << c.reach << " " << c.r << " " << c.blk[0]
+        << " " << c.blk[1] << " " << c.blk[2] << "\n";
+}
+
+// ANALISI_GB300_TUNE_LOG=path appends each timed configuration of the tuner.
+void tune_log(const std::string &key, const char *what, const CellCand *c, double ms)
+{
+    const char *path = std::getenv("ANALISI_GB300_TUNE_LOG");
+    if (!path) return;
+    std::ofstream out(path, std::ios::app);
+    out << key << " " << what;
+    if (c)
+        out << " reach=" << c->reach << " r=" << c->r << " blk=" << c->blk[0] << "x" << c->blk[1]
+            << "x" << c->blk[2] << " cost=" << c->cost << " model=" << c->time;
+    out << " ms=" << ms << "\n";
 }
 
 int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const RunShape &rs,
@@ -866,49 +964,67 @@ double tune_time(gofr_ctx *ctx, const TrajDev &t, const gofr_params &q, const Pl
 int tune_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
 {
     if (pl.kind != 0 || pl.wrapcheck || pl.empty) return GOFR_OK;  // nothing to choose
-    Plan cellpl = pl;
-    std::vector<std::array<int, 3>> ranked;
-    const bool eligible = cell_plan(t, p, cellpl, &ranked);
-    if (!eligible) {
+    const std::vector<CellCand> all = cell_candidates(t, p);
+    if (all.empty()) {
         pl.cells = false;
         return GOFR_OK;
     }
-    const std::string key = tune_key(t, p, cellpl, eligible);
+    const std::string key = tune_key(t, p);
+    auto apply = [&](const TuneChoice &c) {
+        pl.cells = false;
+        if (!c.cells) return;
+        for (const CellCand &cc : all)
+            if (cc.reach == c.reach && cc.r == c.r && cc.blk == c.blk) {
+                apply_cell(pl, cc);
+                pl.cells = true;
+                return;
+            }
+    };
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         tune_load_file();
         auto it = g_tune.find(key);
         if (it != g_tune.end()) {
-            if (it->second.cells) {
-                pl = cellpl;
-                pl.cells = true;
-                set_cell_block(pl, it->second.blk);
-            } else {
-                pl.cells = false;
-            }
+            apply(it->second);
             return GOFR_OK;
         }
     }
-    // sample of the job: its first origin, up to four lags
+    // sample of the job: its first origin and the first lags, at least four
+    // and enough for ~1.5e10 pairs (the device full several times over)
+    const unsigned leff = (p.ntimesteps < p.tmax || p.tmax == 0) ? p.ntimesteps : p.tmax;
+    const double want = std::ceil(1.5e10 / ((double)t.N * (double)t.N));
     gofr_params q = p;
     q.kernel = GOFR_KERNEL_AUTO;
     q.nparts = 1;
-    q.tmax = std::min<unsigned>(p.tmax ? p.tmax : p.ntimesteps, 4);
+    q.tmax = (unsigned)std::min<double>(leff, std::max(4.0, want));
     q.ntimesteps = std::max<unsigned>(q.tmax, 1);
     q.skip = q.ntimesteps;
     Plan base = pl;
     base.cells = false;
     double best_ms = tune_time(ctx, t, q, base);
+    tune_log(key, "all-pairs", nullptr, best_ms);
+    // the four cheapest estimates, and the cheapest of each reach
+    std::vector<const CellCand *> tries;
+    for (size_t c = 0; c < all.size() && tries.size() < 4; ++c) tries.push_back(&all[c]);
+    for (int m = 1; m <= 2; ++m)
+        for (const CellCand &c : all)
+            if (c.reach == m) {
+                if (std::find(tries.begin(), tries.end(), &c) == tries.end()) tries.push_back(&c);
+                break;
+            }
     TuneChoice choice;
-    for (size_t c = 0; c < ranked.size() && c < 3; ++c) {
-        Plan cp = cellpl;
+    for (const CellCand *c : tries) {
+        Plan cp = pl;
         cp.cells = true;
-        set_cell_block(cp, ranked[c]);
+        apply_cell(cp, *c);
         const double ms = tune_time(ctx, t, q, cp);
+        tune_log(key, "cells", c, ms);
         if (ms > 0 && (best_ms < 0 || ms < best_ms)) {
             best_ms = ms;
             choice.cells = true;
-            choice.blk = ranked[c];
+            choice.reach = c->reach;
+            choice.r = c->r;
+            choice.blk = c->blk;
         }
     }
     {
@@ -916,13 +1032,7 @@ int tune_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
         g_tune[key] = choice;
         tune_store_file(key, choice);
     }
-    if (choice.cells) {
-        pl = cellpl;
-        pl.cells = true;
-        set_cell_block(pl, choice.blk);
-    } else {
-        pl.cells = false;
-    }
+    apply(choice);
     return GOFR_OK;
 }
 

@@ -27,12 +27,11 @@ namespace gofr {
 namespace cells {
 
 constexpr int NT = 256;
-constexpr int R = 4;          // first atoms per thread
-constexpr int TI = NT * R;
 constexpr int TJ = 1024;      // second atoms per shared-memory tile
 constexpr int SLOTS = 16;
 constexpr int QCAP = 1024;
-constexpr int MAXR = 64;      // max contiguous ranges of a neighbourhood (checked on host)
+constexpr int MAXR = 128;     // max contiguous ranges of a neighbourhood (checked on host)
+constexpr int FLUSH_ILP = 2;  // slots binned per round of a warp flush
 
 typedef unsigned long long f2;
 __device__ __forceinline__ f2 f2pk(float a, float b)
@@ -202,16 +201,23 @@ __device__ int build_ranges(const int *start, int ncx, int ncy, int ncz, int x0,
     return n;
 }
 
-// flat index q of a range list -> sorted atom index
+// flat index q of a range list -> sorted atom index (binary search of the
+// prefix table: the last range r with pre[r] <= q)
 __device__ __forceinline__ int flat_to_atom(const Range *rg, const int *pre, int nr, int q)
 {
-    int r = 0;
-    while (r + 1 < nr && pre[r + 1] <= q) ++r;
-    return rg[r].begin + (q - pre[r]);
+    int lo = 0, hi = nr - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pre[mid] <= q) lo = mid;
+        else hi = mid - 1;
+    }
+    return rg[lo].begin + (q - pre[lo]);
 }
 
+template <int R>
 __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
 {
+    constexpr int TI = NT * R;
     extern __shared__ __align__(128) unsigned char smem[];
     const PairLaunch &P = C.pair;
     float *jx = reinterpret_cast<float *>(smem);                 // [3][TJ]
@@ -274,11 +280,12 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
             const int *st_o = C.start + fo * (size_t)(ncell + 1);
             const int *st_l = C.start + fl * (size_t)(ncell + 1);
             nir = build_ranges(st_o, C.nc[0], C.nc[1], C.nc[2], cx0, cnx, cy0, cny, cz0, cnz, irg);
-            const int jnx = min(cnx + 2, C.nc[0]), jny = min(cny + 2, C.nc[1]),
-                      jnz = min(cnz + 2, C.nc[2]);
-            const int jx0 = jnx == C.nc[0] ? 0 : cx0 - 1;
-            const int jy0 = jny == C.nc[1] ? 0 : cy0 - 1;
-            const int jz0 = jnz == C.nc[2] ? 0 : cz0 - 1;
+            const int m = C.reach;
+            const int jnx = min(cnx + 2 * m, C.nc[0]), jny = min(cny + 2 * m, C.nc[1]),
+                      jnz = min(cnz + 2 * m, C.nc[2]);
+            const int jx0 = jnx == C.nc[0] ? 0 : cx0 - m;
+            const int jy0 = jny == C.nc[1] ? 0 : cy0 - m;
+            const int jz0 = jnz == C.nc[2] ? 0 : cz0 - m;
             njr = build_ranges(st_l, C.nc[0], C.nc[1], C.nc[2], jx0, jnx, jy0, jny, jz0, jnz, jrg);
             ipre[0] = 0;
             for (int r = 0; r < nir; ++r) ipre[r + 1] = ipre[r] + (irg[r].end - irg[r].begin);
@@ -356,43 +363,61 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
                 }
                 __syncthreads();
 
+                // Bins every slot of this warp's lanes, two slots per round
+                // so that their shared-memory load chains overlap.
                 auto warp_flush = [&]() {
                     const int maxc = __reduce_max_sync(0xffffffffu, (unsigned)cnt);
-                    for (int qq = 0; qq < maxc; ++qq) {
-                        if (qq < cnt) {
-                            const uint2 e = my_slots[qq * NT];
-                            const float d2 = __uint_as_float(e.x);
-                            const int r = e.y & 3;
-                            const int jj = (e.y >> 2) & 0x1fff;
-                            int t_i = ti[0], ia = iid[0];
+                    for (int q0 = 0; q0 < maxc; q0 += FLUSH_ILP) {
+                        uint2 e[FLUSH_ILP];
+                        bool v[FLUSH_ILP];
+#pragma unroll
+                        for (int u = 0; u < FLUSH_ILP; ++u) {
+                            v[u] = q0 + u < cnt;
+                            e[u] = v[u] ? my_slots[(q0 + u) * NT] : make_uint2(0x7f800000u, 0u);
+                        }
+                        int ch[FLUSH_ILP], bi[FLUSH_ILP], ia[FLUSH_ILP], ja[FLUSH_ILP];
+                        bool ok[FLUSH_ILP], need[FLUSH_ILP];
+#pragma unroll
+                        for (int u = 0; u < FLUSH_ILP; ++u) {
+                            const float d2 = __uint_as_float(e[u].x);
+                            const int r = e[u].y & 3;  // R <= 4
+                            const int jj = (e[u].y >> 2) & 0x1fff;
+                            int t_i = ti[0], a_ = iid[0];
 #pragma unroll
                             for (int rr = 1; rr < R; ++rr) {
                                 t_i = (r == rr) ? ti[rr] : t_i;
-                                ia = (r == rr) ? iid[rr] : ia;
+                                a_ = (r == rr) ? iid[rr] : a_;
                             }
-                            const int ja = jid[jj];
-                            const int ch = chtab[t_i * P.ntypes + jt[jj]] + (ia == ja ? half : 0);
-                            bool need = false;
-                            if (d2 >= P.lo_f) {
-                                const float rr_ = __fsqrt_rn(d2);
-                                int bi = __float2int_rd(__fmul_rn(__fsub_rn(rr_, P.rmin_f), P.inv_dr_f));
-                                bi = min(max(bi, 0), P.nbin - 1);
-                                const float2 w = win[bi];
-                                if (d2 >= w.x && d2 <= w.y) atomicAdd(hist + ch * P.nbin + bi, 1u);
-                                else need = true;
-                            }
-                            if (need) {
+                            ia[u] = a_;
+                            ja[u] = jid[jj];
+                            ch[u] = chtab[t_i * P.ntypes + jt[jj]] + (ia[u] == ja[u] ? half : 0);
+                            const int b_ = __float2int_rd(
+                                __fmul_rn(__fsub_rn(sqrt_guess(d2), P.rmin_f), P.inv_dr_f));
+                            bi[u] = min(max(b_, 0), P.nbin - 1);
+                            const float2 w = win[bi[u]];
+                            const bool test = v[u] && d2 >= P.lo_f;
+                            const bool inw = d2 >= w.x && d2 <= w.y;
+                            ok[u] = test && inw;
+                            need[u] = test && !inw;
+                        }
+#pragma unroll
+                        for (int u = 0; u < FLUSH_ILP; ++u) {
+                            if (ok[u]) atomicAdd(hist + ch[u] * P.nbin + bi[u], 1u);
+                            if (need[u]) {
                                 ++n_rech;
                                 const int slot = atomicAdd(&rqn, 1);
                                 if (slot < QCAP) {
-                                    rq[slot] = make_uint4((unsigned)ia, (unsigned)ja, (unsigned)ch, 0u);
+                                    rq[slot] = make_uint4((unsigned)ia[u], (unsigned)ja[u],
+                                                          (unsigned)ch[u], 0u);
                                 } else {
-                                    const double *xi64 = P.pos64 + (fo * P.N + ia) * 3;
-                                    const double *xj64 = P.pos64 + (fl * P.N + ja) * 3;
-                                    const double d2d = ref_d2<false>(xi64[0], xi64[1], xi64[2], xj64[0],
-                                                                     xj64[1], xj64[2], P.box64 + fo * 9, P.err);
-                                    const int bb = ref_bin(d2d, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
-                                    if (bb >= 0) atomicAdd(hist + ch * P.nbin + bb, 1u);
+                                    const double *xi64 = P.pos64 + (fo * P.N + ia[u]) * 3;
+                                    const double *xj64 = P.pos64 + (fl * P.N + ja[u]) * 3;
+                                    const double d2d =
+                                        ref_d2<false>(xi64[0], xi64[1], xi64[2], xj64[0], xj64[1],
+                                                      xj64[2], P.box64 + fo * 9, P.err);
+                                    const int bb =
+                                        ref_bin(d2d, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
+                                    if (bb >= 0) atomicAdd(hist + ch[u] * P.nbin + bb, 1u);
                                 }
                             }
                         }
@@ -470,7 +495,7 @@ int cell_smem_bytes(int nch, int nbin, int ntypes)
     return (int)((b + 127) / 128 * 128);
 }
 
-int cell_block_atoms() { return cells::TI; }
+int cell_block_atoms(int r) { return cells::NT * r; }
 int cell_max_ranges() { return cells::MAXR; }
 
 int launch_cell_build(const double *pos64, const float *pos32, const unsigned char *types8,
@@ -498,23 +523,34 @@ int launch_cell_build(const double *pos64, const float *pos32, const unsigned ch
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-int launch_cell_pairs(const CellLaunch &C, int num_sms, cudaStream_t s)
+template <int R>
+static int launch_cell_r(const CellLaunch &C, int num_sms, cudaStream_t s)
 {
     using namespace cells;
-    if (C.pair.n_items <= 0) return 0;
     const int smem = cell_smem_bytes(C.pair.nch, C.pair.nbin, C.pair.ntypes);
-    if (cudaFuncSetAttribute(k_pairs_cell, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+    if (cudaFuncSetAttribute(k_pairs_cell<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
         cudaSuccess)
         return -1;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairs_cell, NT, smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairs_cell<R>, NT, smem) !=
         cudaSuccess)
         return -1;
     if (per_sm < 1) return -2;
     long long grid = (long long)num_sms * per_sm;
     if (grid > C.pair.n_items) grid = C.pair.n_items;
-    k_pairs_cell<<<(unsigned)grid, NT, smem, s>>>(C);
+    k_pairs_cell<R><<<(unsigned)grid, NT, smem, s>>>(C);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_cell_pairs(const CellLaunch &C, int num_sms, cudaStream_t s)
+{
+    if (C.pair.n_items <= 0) return 0;
+    switch (C.r) {
+    case 2: return launch_cell_r<2>(C, num_sms, s);
+    case 3: return launch_cell_r<3>(C, num_sms, s);
+    case 4: return launch_cell_r<4>(C, num_sms, s);
+    default: return -3;
+    }
 }
 
 }  // namespace gofr

@@ -70,6 +70,18 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity
     return false;
 }
 
+// Square root for the bin guess of a candidate only.  The certified window
+// test that follows decides whether the pair is counted in the guessed bin,
+// so the hardware approximation (a few ulp) is enough: a guess that is wrong
+// near a bin edge fails the window test and the pair goes to the FP64
+// recheck, exactly as a pair inside a window margin does.
+__device__ __forceinline__ float sqrt_guess(float x)
+{
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // ---------------------------------------------------------------------------
 // FP64 restatement of the reference pair arithmetic.
 // Every operation is an explicitly rounded IEEE intrinsic, so nvcc cannot

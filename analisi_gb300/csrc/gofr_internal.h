@@ -74,10 +74,12 @@ struct CellLaunch {
     int nc[3];                     // cells per axis
     int b[3];                      // cells per block per axis
     int nb[3];                     // blocks per axis
+    int reach;                     // neighbour cells per side (cell edge >= rmax / reach)
+    int r;                         // first atoms per thread (2, 3 or 4)
 };
 
 int cell_smem_bytes(int nch, int nbin, int ntypes);
-int cell_block_atoms();
+int cell_block_atoms(int r);
 int cell_max_ranges();
 int launch_cell_build(const double *pos64, const float *pos32, const unsigned char *types8,
                       size_t T, size_t N, const double *box_internal, const int *nc,

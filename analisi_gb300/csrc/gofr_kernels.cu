@@ -419,7 +419,7 @@ __device__ __forceinline__ bool f32_item(const PairLaunch &P, const F32Views &V,
                     const int ch = V.chtab[t_i * P.ntypes + btp[jj]] + (ia == ja ? half : 0);
                     bool need = WCHK && (e.y >> 31);
                     if (!need && d2 >= P.lo_f) {
-                        const float rr_ = __fsqrt_rn(d2);
+                        const float rr_ = sqrt_guess(d2);
                         int bi = __float2int_rd(__fmul_rn(__fsub_rn(rr_, P.rmin_f), P.inv_dr_f));
                         bi = min(max(bi, 0), P.nbin - 1);
                         const float2 w = V.win[bi];

@@ -8,15 +8,17 @@ nbin=400, tmax=200, skip=4), reset(1800), i.e. 450 origins x 200 lags x N^2
 ordered pairs = 2.42e13 pair evaluations.  Seeded synthetic data
 (analisi_gb300.workloads.c2), no dataset.
 
-One step = one Gofrt::calculate over a window of 25 consecutive origins
-(reset(100), calculate(primo)) x all 200 lags: step s uses primo=100*(s mod 18),
-so 18 steps are exactly the full reset(1800) calculation, split the way the
-reference's block-average driver splits a trajectory.
+One step = one Gofrt::calculate over a window of 50 consecutive origins
+(reset(200), calculate(primo)) x all 200 lags (2.68e12 ordered pairs; the
+lags of a calculate are min(reset length, tmax), so the window must be at
+least tmax frames long): step s uses primo=200*(s mod 9), so 9 steps are
+exactly the full reset(1800) calculation, split the way the reference's
+block-average driver splits a trajectory.
 
   value   pair throughput with the frames resident in HBM (device-timed with
           CUDA events on the engine's stream, L2 flushed between steps)
   e2e     the same metric through the C ABI with host buffers: every step
-          uploads its 300-frame window from pinned host memory
+          uploads its 400-frame window from pinned host memory
           (gofr_set_frames) and reads the counts back (gofr_run)
   roofline  FP32-issue bound: 16 FP32 lane operations per ordered pair
           (orthorhombic), against the FP32 lane-op peak measured on this GPU
@@ -42,7 +44,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "g(r,t) Gpairs/s on 1 GB300: FP32+FP64-edge-recheck vs plain FP64, exact counts"
 UNIT = "Gpairs/s"
-ORIGINS_PER_STEP = 25
+ORIGINS_PER_STEP = 50
+STEP_WINDOWS = 9  # windows of ORIGINS_PER_STEP origins in reset(1800)
 OPS_PER_PAIR = 16  # orthorhombic FP32 pair: 3 sub + 3x(ffma, fadd, ffma) + fmul + 2 ffma + cmp
 
 
@@ -59,6 +62,8 @@ def parse():
                     help="c2: the headline line (default); batch / cells: only that measurement")
     ap.add_argument("--batch-origins", type=int, default=20,
                     help="origins per trajectory of the batched measurement")
+    ap.add_argument("--kernel", default="auto", choices=["auto", "f32", "cell", "tuned"],
+                    help="pair kernel of the headline line (auto: what a user gets)")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the batched (64 trajectories) and cell-list (131k atoms) lines")
     ap.add_argument("--lags", type=int, default=200,
@@ -72,17 +77,17 @@ def dist_info():
 
 
 def step_window(s, rank=0):
-    """primo of step s: 18 windows of 100 origins-frames cover reset(1800)."""
-    return 100 * ((s + rank * 7) % 18)
+    """primo of step s: 9 windows of 200 origin-frames cover reset(1800)."""
+    return 200 * ((s + rank * 4) % STEP_WINDOWS)
 
 
 def workload_config(extra=None):
     cfg = {"workload": "c2_n16384_t2000_ortho", "natoms": 16384, "types": [16352, 16, 16],
            "box": "cubic L=54.72 (density 0.1)", "frames": 2000, "sigma": 0.08,
            "rmin": 0.0, "rmax": 12.0, "nbin": 400, "tmax": 200, "skip": 4, "every": 1,
-           "reset": 1800, "step": "calculate over 25 origins (reset(100), primo=100*(s%18)) "
-                                   "x 200 lags; 18 steps = the full reset(1800)",
-           "l2": "flushed between timed steps (256 MiB write); per-step inputs ~60 MB < L2"}
+           "reset": 1800, "step": "calculate over 50 origins (reset(200), primo=200*(s%9)) "
+                                   "x 200 lags = 2.68e12 pairs; 9 steps = the full reset(1800)",
+           "l2": "flushed between timed steps (256 MiB write); per-step inputs ~79 MB < L2"}
     if extra:
         cfg.update(extra)
     return cfg
@@ -148,7 +153,7 @@ def run_reference(args):
     val = pairs * len(times) / sum(times) / 1e9
     from oracle.oracle import host_info
     hi = host_info()
-    sample = (f"each step: 1 origin (primo=100*(s%18)) x {n_lags} lags = {pairs:.3g} pairs "
+    sample = (f"each step: 1 origin (primo=200*(s%9)) x {n_lags} lags = {pairs:.3g} pairs "
               f"on {threads} threads of {hi['cpu']} ({hi['arch']})")
     out = {"metric": METRIC, "value": round(val, 4), "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup,
@@ -219,9 +224,16 @@ class Clocks:
                 "samples": len(rows)}
 
 
-def traffic_from_profiles():
-    """dram bytes per launch of the FP32 pair kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_pairs_f32_c2_n16384.md")
+KERNEL_NAMES = {1: "k_pairs_f32 (all pairs)", 2: "k_pairs_f64 (all pairs)",
+                3: "k_pairs_cell (cell lists)"}
+PROFILE_OF = {1: "k_pairs_f32_c2_n16384.md", 3: "k_pairs_cell_c2_n16384.md"}
+
+
+def traffic_from_profiles(kernel_used):
+    """dram bytes per launch of the pair kernel from the committed ncu summary."""
+    if kernel_used not in PROFILE_OF:
+        return None
+    path = os.path.join(ROOT, "profiles", PROFILE_OF[kernel_used])
     try:
         for line in open(path):
             m = re.search(r"traffic_bytes_per_launch:\s*([\d.eE+]+)", line)
@@ -256,29 +268,61 @@ def bench_batch(engine, workloads, device, origins=20, reps=5):
         ms.append(e.stats()["kernel_ms"])
     st = e.stats()
     batch_rate = st["pairs"] / (sum(ms) / len(ms)) / 1e6
-    seq_ms, seq_pairs, same = 0.0, 0, True
-    best_single = 0.0
+    # the same trajectories one by one: with the batch's kernel (all pairs), and
+    # with the kernel a single run picks by itself (cell lists where they pay)
+    seq = {}
+    same = True
     e2 = engine.Engine(device)
-    for k, (m, t) in enumerate(zip(mem, trajs)):
-        e2.set_frames(m["positions"], m["boxes"], m["type_ids"], m["ntypes"])
-        P = t["params"]
-        c = e2.run(P.rmin, P.rmax, P.nbin, P.tmax, P.skip, P.every, P.ntimesteps, P.primo)
-        s2 = e2.stats()
-        seq_ms += s2["kernel_ms"]
-        seq_pairs += s2["pairs"]
-        best_single = max(best_single, s2["pairs"] / s2["kernel_ms"] / 1e6)
-        same &= bool(np.array_equal(c, outs[k]))
+    for kern in ("f32", "auto"):
+        ms_sum, pairs_sum, best = 0.0, 0, 0.0
+        for k, (m, t) in enumerate(zip(mem, trajs)):
+            e2.set_frames(m["positions"], m["boxes"], m["type_ids"], m["ntypes"])
+            P = t["params"]
+            for _ in range(2):  # the first run of a trajectory builds its cell lists
+                c = e2.run(P.rmin, P.rmax, P.nbin, P.tmax, P.skip, P.every, P.ntimesteps,
+                           P.primo, kernel=kern)
+            s2 = e2.stats()
+            ms_sum += s2["kernel_ms"]
+            pairs_sum += s2["pairs"]
+            best = max(best, s2["pairs"] / s2["kernel_ms"] / 1e6)
+            same &= bool(np.array_equal(c, outs[k]))
+        seq[kern] = (pairs_sum / ms_sum / 1e6, best)
     e.close()
     e2.close()
-    seq_rate = seq_pairs / seq_ms / 1e6
     return {"workload": "64 trajectories, N log-uniform 256..16384, T 100..1000, 1-4 types, "
                         f"300 bins on [0,10], {origins} origins x all lags each",
             "pairs": st["pairs"], "value": round(batch_rate, 2), "unit": UNIT,
-            "sequential_same_trajectories": round(seq_rate, 2),
-            "best_single_trajectory": round(best_single, 2),
-            "ratio_vs_sequential": round(batch_rate / seq_rate, 3),
-            "ratio_vs_best_single": round(batch_rate / best_single, 3),
+            "kernel": "k_pairs_batch (all pairs, one persistent launch)",
+            "sequential_same_kernel": round(seq["f32"][0], 2),
+            "best_single_same_kernel": round(seq["f32"][1], 2),
+            "ratio_vs_sequential": round(batch_rate / seq["f32"][0], 3),
+            "ratio_vs_best_single": round(batch_rate / seq["f32"][1], 3),
+            "sequential_auto_kernel": round(seq["auto"][0], 2),
+            "best_single_auto_kernel": round(seq["auto"][1], 2),
             "counts_identical_to_single_runs": same, "cuda_graph": True}
+
+
+def bench_allpairs(eng, prm, args, flush, steps=2):
+    """The same steps through the all-pairs FP32 kernel (for comparison when the
+    headline line used the cell-list form)."""
+    import numpy as np
+    import torch
+    from analisi_gb300 import engine
+    pairs, ms = 0, 0.0
+    for s in range(steps + 1):
+        p = prm[(args.warmup + s) % STEP_WINDOWS]
+        q = engine.make_params(p.rmin, p.rmax, p.nbin, p.tmax, p.skip, p.every, p.ntimesteps,
+                               p.primo, kernel="f32")
+        out = np.zeros(eng.output_size(q), dtype=np.uint64)
+        flush.zero_()
+        torch.cuda.synchronize()
+        eng.run_params(q, out)
+        st = eng.stats()
+        if s > 0:
+            pairs += st["pairs"]
+            ms += st["kernel_ms"]
+    return {"value": round(pairs / ms / 1e6, 3), "unit": UNIT, "steps": steps,
+            "kernel": "k_pairs_f32 (all pairs)"}
 
 
 def bench_cells(engine, workloads, device):
@@ -322,7 +366,8 @@ def run_gpu(args):
     step_n = ORIGINS_PER_STEP * p["skip"]
     lags = min(args.lags, p["tmax"])
     prm = [engine.make_params(p["rmin"], p["rmax"], p["nbin"], lags, p["skip"], p["every"],
-                              step_n, step_window(s, rank)) for s in range(18)]
+                              step_n, step_window(s, rank), kernel=args.kernel)
+           for s in range(STEP_WINDOWS)]
     nout = eng.output_size(prm[0])
     out = np.zeros(nout, dtype=np.uint64)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
@@ -334,23 +379,26 @@ def run_gpu(args):
 
     # warm-up
     for s in range(args.warmup):
-        eng.run_params(prm[s % 18], out)
+        eng.run_params(prm[s % STEP_WINDOWS], out)
     st0 = eng.stats()
     launches0 = st0["launches"]
-    kernel_ms, total_ms, cands, rech, pairs = [], [], 0, 0, 0
+    kernel_ms, total_ms, cands, rech, pairs, evaluated = [], [], 0, 0, 0, 0
+    kernels_used = set()
     barrier()
     os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
     with Clocks(os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv")) as clk:
         for s in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
-            eng.run_params(prm[(args.warmup + s) % 18], out)
+            eng.run_params(prm[(args.warmup + s) % STEP_WINDOWS], out)
             st = eng.stats()
             kernel_ms.append(st["kernel_ms"])
             total_ms.append(st["total_ms"])
             cands += st["candidates"]
             rech += st["rechecks"]
             pairs += st["pairs"]
+            evaluated += st["evaluated"]
+            kernels_used.add(int(st["kernel_used"]))
     barrier()
     launches = eng.stats()["launches"] - launches0
     dev_s = sum(total_ms) / 1e3
@@ -371,7 +419,7 @@ def run_gpu(args):
         pp, pb = pinned_pos.numpy(), pinned_box.numpy()
         e2 = engine.Engine(local)
         pe = [engine.make_params(p["rmin"], p["rmax"], p["nbin"], lags, p["skip"],
-                                 p["every"], step_n, 0) for _ in range(1)]
+                                 p["every"], step_n, 0, kernel=args.kernel) for _ in range(1)]
         times = []
         h2d = win_frames * N * 24 + win_frames * 48 + N * 4
         for s in range(args.warmup + args.steps):
@@ -401,20 +449,20 @@ def run_gpu(args):
     # FP64 comparison kernel on a sample (1 origin x 10 lags), same engine
     f64 = None
     if rank == 0 and not args.no_f64:
-        pf = engine.make_params(p["rmin"], p["rmax"], p["nbin"], 10, p["skip"], p["every"],
-                                4, 0, kernel="f64")
+        pf = engine.make_params(p["rmin"], p["rmax"], p["nbin"], 10, 10, p["every"],
+                                10, 0, kernel="f64")
         o64 = np.zeros(eng.output_size(pf), dtype=np.uint64)
         eng.run_params(pf, o64)
         st = eng.stats()
-        pf32 = engine.make_params(p["rmin"], p["rmax"], p["nbin"], 10, p["skip"], p["every"],
-                                  4, 0, kernel="f32")
+        pf32 = engine.make_params(p["rmin"], p["rmax"], p["nbin"], 10, 10, p["every"],
+                                  10, 0, kernel="f32")
         o32 = np.zeros_like(o64)
         eng.run_params(pf32, o32)
         st32 = eng.stats()
         f64 = {"gpairs_per_s_f64": round(st["pairs"] / st["kernel_ms"] / 1e6, 3),
                "gpairs_per_s_f32_same_sample": round(st32["pairs"] / st32["kernel_ms"] / 1e6, 3),
                "counts_identical": bool(np.array_equal(o64, o32)),
-               "sample": "1 origin x 10 lags (1.07e9 pairs)"}
+               "sample": "1 origin x 10 lags (2.68e9 pairs)"}
 
     if rank != 0:
         if world > 1:
@@ -422,15 +470,21 @@ def run_gpu(args):
         return 0
 
     fp32_peak, satom_peak = engine.measure_peaks(local)
-    achieved = pairs_per_launch * OPS_PER_PAIR / kernel_avg_s / 1e12
+    kernel_used = max(kernels_used) if kernels_used else 0
+    evaluated_per_launch = evaluated / args.steps
+    achieved = evaluated_per_launch * OPS_PER_PAIR / kernel_avg_s / 1e12
     peak = fp32_peak / 1e12
-    traffic = traffic_from_profiles()
+    traffic = traffic_from_profiles(kernel_used)
     roof = {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(peak, 3),
             "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
             "traffic": traffic,
-            "notes": "FP32 lane operations (one FADD/FMUL/FFMA = 1) at 16 per ordered pair; "
-                     "peak = FFMA issue rate measured on this GPU (gofr_measure_peaks, burst); "
-                     "traffic = ncu dram bytes per launch (profiles/)",
+            "notes": "FP32 lane operations (one FADD/FMUL/FFMA = 1) at 16 per evaluated "
+                     "ordered pair (all N^2 pairs for the all-pairs kernel, the cell "
+                     "neighbourhoods' pairs for the cell-list kernel); peak = FFMA issue rate "
+                     "measured on this GPU (gofr_measure_peaks, burst); traffic = ncu dram "
+                     "bytes per launch (profiles/)",
+            "kernel": KERNEL_NAMES.get(kernel_used, str(kernel_used)),
+            "evaluated_pairs_per_launch": int(evaluated_per_launch),
             "smem_atomic_peak_per_s": satom_peak,
             "atomics_needed_per_s": round(cands / (sum(kernel_ms) / 1e3), 1)}
     cpu = None
@@ -442,6 +496,8 @@ def run_gpu(args):
     extra = {}
     if not args.no_extra:
         del w
+        if kernel_used != 1:
+            extra["allpairs_f32"] = bench_allpairs(eng, prm, args, flush)
         extra["batch64"] = bench_batch(engine, workloads, local, args.batch_origins)
         extra["cells131k"] = bench_cells(engine, workloads, local)
     res = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
@@ -450,6 +506,9 @@ def run_gpu(args):
            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64-recheck (u64 counts)",
            "data": "synthetic (seeded random walk, analisi_gb300.workloads.c2)",
            "config": workload_config({"pairs_per_step": int(pairs_per_launch), "lags": lags,
+                                      "kernel": KERNEL_NAMES.get(kernel_used, str(kernel_used)),
+                                      "kernel_request": args.kernel,
+                                      "evaluated_frac": round(evaluated / pairs, 6),
                                       "candidates_frac": round(cands / pairs, 6),
                                       "recheck_frac": rech / pairs}),
            "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,

@@ -28,8 +28,20 @@ def _run(eng, w, kernel):
     return c, eng.stats()
 
 
+# Cell-list configurations "reach,r,bx,by,bz" forced through
+# ANALISI_GB300_CELL_PLAN (None = the planner's choice): cells of edge
+# >= rmax (reach 1) and >= rmax/2 (reach 2), 2/3/4 first atoms per thread,
+# single cells and blocks whose neighbourhood wraps the box.
+PLANS = [None, "1,4,1,1,1", "1,2,2,1,1", "2,2,1,1,1", "2,3,2,1,3", "2,4,3,3,3"]
+
+
+@pytest.mark.parametrize("plan", PLANS, ids=[str(p) for p in PLANS])
 @pytest.mark.parametrize("case", CASES, ids=[str(c[0]) for c in CASES])
-def test_cells_match_oracle_and_all_pairs(gpu_engine, oracle_mod, case):
+def test_cells_match_oracle_and_all_pairs(gpu_engine, oracle_mod, case, plan, monkeypatch):
+    if plan is None:
+        monkeypatch.delenv("ANALISI_GB300_CELL_PLAN", raising=False)
+    else:
+        monkeypatch.setenv("ANALISI_GB300_CELL_PLAN", plan)
     seed, N, T, L, sigma, counts, params = case
     w = workloads.small_case(seed, N, T, L, sigma, counts, **params)
     if seed == 62:  # shifted, non-cubic box
@@ -42,7 +54,8 @@ def test_cells_match_oracle_and_all_pairs(gpu_engine, oracle_mod, case):
                                   p["every"], p["ntimesteps"], p["primo"])
     cell, st = _run(gpu_engine, w, "cell")
     assert st["kernel_used"] == 3
-    assert st["evaluated"] < st["pairs"]
+    # the planner may take the whole box as one block for so few atoms
+    assert st["evaluated"] <= st["pairs"] if plan is None else st["evaluated"] < st["pairs"]
     np.testing.assert_array_equal(cell, ref)
     allp, _ = _run(gpu_engine, w, "f32")
     np.testing.assert_array_equal(allp, ref)
