@@ -61,9 +61,9 @@ struct TrajDev {
     bool box_constant = true;   // every frame has the same box
     // cell lists (built on first use for a grid, kept while the frames stay)
     int cell_nc[3] = {0, 0, 0};
-    int *d_cstart = nullptr, *d_sid = nullptr;
+    int *d_cstart = nullptr;
+    unsigned *d_sidt = nullptr;
     float *d_spos = nullptr;
-    unsigned char *d_stype = nullptr;
 };
 
 }  // namespace
@@ -168,12 +168,11 @@ void free_traj(TrajDev &t)
     cudaFree(t.types);
     cudaFree(t.types8);
     cudaFree(t.d_cstart);
-    cudaFree(t.d_sid);
+    cudaFree(t.d_sidt);
     cudaFree(t.d_spos);
-    cudaFree(t.d_stype);
     t.pos64 = nullptr; t.pos32 = nullptr; t.box64 = nullptr; t.box32 = nullptr; t.types = nullptr;
     t.types8 = nullptr;
-    t.d_cstart = nullptr; t.d_sid = nullptr; t.d_spos = nullptr; t.d_stype = nullptr;
+    t.d_cstart = nullptr; t.d_sidt = nullptr; t.d_spos = nullptr;
     t.cell_nc[0] = t.cell_nc[1] = t.cell_nc[2] = 0;
 }
 
@@ -341,6 +340,48 @@ Bound error_bound(const TrajDev &t)
         double eq = b.e[k] / s.Lmin[k] + (D[k] / s.Lmin[k] + 1.0) * std::ldexp(1.0, -22);
         b.eta = std::max(b.eta, eq);
     }
+    return b;
+}
+
+// Per-axis error bound of the cell-list kernel's FP32 differences, for an
+// orthorhombic box that is the same in every frame (u = 2^-24, v = 2^-53,
+// per axis: xlo, L, L32 = fl32(L), c = fl64(xlo + L/2)).
+//   w = fl64(x - n L), n = floor(fl64(fl64(x - xlo) / L)):   |w - (x - nL)| <= v |w|
+//     |w - c| <= Mw = L/2 + 3 v (X + L) + v (|xlo| + L), X >= |x - xlo|
+//     (fl64 of the quotient may move n by one next to an integer)
+//   a = fl32(fl64(w - c)):                   |a - (w - c)| <= (u + 2v) Mw = d3
+//   b = fl32(a_j + s L32), s in {-1, 0, 1}:  |b - (a_j + s L32)| <= u (|a| + L32) = d4
+//   a_i - b = d*_K + s (L - L32) + (w/a roundings of i and j), K the image
+//     n_i - n_j + s, d*_K = x_i - x_j - K L exactly
+//   dx = fl32(a_i - b):  |dx - (a_i - b)| <= u |a_i - b| <= u (2 |a| + L32)
+// plus the reference's own FP64 rounding of its difference and of kmax wrap
+// steps (as in error_bound).  d2 is then formed as in the all-pairs kernel
+// (one multiply, two FMAs), so Efun applies with these e.
+Bound error_bound_cells(const TrajDev &t)
+{
+    Bound b{};
+    const double u = std::ldexp(1.0, -24), v = std::ldexp(1.0, -53);
+    const BoxStats &s = t.bs;
+    for (int k = 0; k < 3; ++k) {
+        const double L = s.Lmax[k], xlo = t.h_box[k];
+        const double c = xlo + 0.5 * L;
+        const double X = t.M[k] + std::fabs(t.shift[k] - xlo);
+        const double Mw = 0.5 * L + 3.0 * v * (X + L) + v * (std::fabs(xlo) + L);
+        const double d1 = v * (std::fabs(c) + Mw);
+        const double d3 = (u + 2.0 * v) * Mw;
+        const double A = Mw * (1.0 + 2.0 * u) + d3;
+        const double L32 = L + s.eL[k];
+        const double d4 = u * (A + L32);
+        const double ea = s.eL[k] + 2.0 * d1 + 2.0 * d3 + d4;
+        const double esub = u * (2.0 * A + L32 + d4);
+        const double D = 2.0 * t.M[k] * (1.0 + std::ldexp(1.0, -40));
+        const double kmax = std::floor(D / s.Lmin[k] + 0.5) + 1.0;
+        const double eref = v * D + kmax * v * (D + s.Lmax[k]);
+        b.e[k] = (ea + esub + eref) * (1.0 + std::ldexp(1.0, -20));
+        b.kmax[k] = kmax;
+    }
+    b.enorm = std::sqrt(b.e[0] * b.e[0] + b.e[1] * b.e[1] + b.e[2] * b.e[2]);
+    b.eta = 0.0;  // no wrap quotients: the cell path needs no wrap check
     return b;
 }
 
@@ -551,6 +592,7 @@ bool cell_eligible(const TrajDev &t, const gofr_params &p)
 {
     if (t.tric || !t.box_constant || p.nparts > 1) return false;
     if (!(p.rmax > 0.0)) return false;
+    if (t.N >= (1u << 24)) return false;  // sorted slots pack type << 24 | atom id
     // large histograms use the global-memory form of the all-pairs kernel
     return cell_smem_bytes((int)(t.ntypes * (t.ntypes + 1)), (int)p.nbin, (int)t.ntypes) <=
            160 * 1024;
@@ -576,7 +618,8 @@ bool cell_grid(const TrajDev &t, const gofr_params &p, int reach, int nc[3])
 // pairs of the all-pairs kernel.  The time model weighs each evaluated pair
 // and each candidate (d <= rmax, binned in the warp flush): measured on the
 // 16k- and 131k-atom workloads, a candidate costs ~6.8 pair evaluations in
-// the all-pairs kernel and ~6.5 in the cell kernel, whose pairs cost ~1.1.
+// the all-pairs kernel and ~6.5 in the cell kernel, whose pairs (no wrap
+// arithmetic) cost ~0.62 of an all-pairs evaluation.
 std::vector<CellCand> cell_candidates(const TrajDev &t, const gofr_params &p)
 {
     std::vector<CellCand> all;
@@ -591,11 +634,12 @@ std::vector<CellCand> cell_candidates(const TrajDev &t, const gofr_params &p)
         for (int bx = 1; bx <= 5; ++bx)
             for (int by = 1; by <= 5; ++by)
                 for (int bz = 1; bz <= 5; ++bz) {
-                    if (bx > nc[0] || by > nc[1] || bz > nc[2]) continue;
-                    const int jy = std::min(by + 2 * m, nc[1]), jz = std::min(bz + 2 * m, nc[2]);
+                    // each neighbourhood cell once: b + 2 reach <= nc per axis
+                    if (bx + 2 * m > nc[0] || by + 2 * m > nc[1] || bz + 2 * m > nc[2]) continue;
+                    const int jy = by + 2 * m, jz = bz + 2 * m;
                     if (2 * jy * jz > cell_max_ranges() || by * bz > cell_max_ranges()) continue;
                     const double atoms = per_cell * bx * by * bz;
-                    const double nbhd = (double)std::min(bx + 2 * m, nc[0]) * jy * jz;
+                    const double nbhd = (double)(bx + 2 * m) * jy * jz;
                     for (int r = 2; r <= 4; ++r) {
                         const int TI = cell_block_atoms(r);
                         const double slots =
@@ -610,7 +654,7 @@ std::vector<CellCand> cell_candidates(const TrajDev &t, const gofr_params &p)
                                               ((nc[1] + by - 1) / by) * ((nc[2] + bz - 1) / bz);
                         c.cost = blocks * slots * nbhd * per_cell / ((double)t.N * t.N);
                         const double f_cell = std::min(1.0, f_all / std::max(c.fraction, 1e-9));
-                        c.time = c.cost * (1.1 + 6.5 * f_cell) / (1.0 + 6.8 * f_all);
+                        c.time = c.cost * (0.62 + 6.5 * f_cell) / (1.0 + 6.8 * f_all);
                         all.push_back(c);
                     }
                 }
@@ -651,6 +695,26 @@ bool cell_override(const TrajDev &t, const gofr_params &p, CellCand &out)
     return false;
 }
 
+// Turns an FP32 plan (thresholds set) into the cell-list form of configuration
+// c, with the cell kernel's own bound and windows.  False when the minimum
+// image of the candidates is not certain without a per-pair wrap test.
+bool make_cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl, const CellCand &c)
+{
+    if (pl.kind != 0 || pl.th.empty()) return false;
+    Plan q = pl;
+    apply_cell(q, c);
+    q.b = error_bound_cells(t);
+    certify(q.b, q.th.data(), p.nbin, q.w);
+    const double emax = std::max(q.b.e[0], std::max(q.b.e[1], q.b.e[2]));
+    const double reach = std::sqrt((double)q.w.hi_f) * (1.0 + std::ldexp(1.0, -20)) +
+                         2.0 * emax + 1e-9;
+    if (!(t.bs.lh_min > reach)) return false;
+    q.cells = true;
+    q.wrapcheck = false;
+    pl = q;
+    return true;
+}
+
 bool cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl)
 {
     CellCand c;
@@ -659,15 +723,15 @@ bool cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl)
         if (all.empty()) return false;
         c = all.front();
     }
-    apply_cell(pl, c);
-    return true;
+    return make_cell_plan(t, p, pl, c);
 }
 
 // AUTO takes the cell-list form when its modelled time is below this share of
 // the all-pairs kernel's (a margin for the model's error).
 constexpr double kCellAutoTime = 0.85;
 
-int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
+int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl,
+              bool allow_cells = true)
 {
     const int req = p.kernel;
     if (req != GOFR_KERNEL_AUTO && req != GOFR_KERNEL_F32_RECHECK && req != GOFR_KERNEL_F64 &&
@@ -676,7 +740,7 @@ int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
     if (req == GOFR_KERNEL_TUNED) {
         gofr_params q = p;
         q.kernel = GOFR_KERNEL_AUTO;
-        return make_plan(ctx, t, q, pl);
+        return make_plan(ctx, t, q, pl, allow_cells);
     }
     const bool reg = regular_bins(p.rmin, p.rmax, p.nbin);
     if (reg) {
@@ -703,12 +767,10 @@ int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
         return fail(ctx, GOFR_ERR_UNSUPPORTED,
                     "coordinates too far outside the box for a certified FP32 wrap");
     }
-    if ((req == GOFR_KERNEL_CELL || req == GOFR_KERNEL_AUTO) && !pl.wrapcheck) {
+    if (allow_cells && (req == GOFR_KERNEL_CELL || req == GOFR_KERNEL_AUTO) && !pl.wrapcheck) {
         Plan c = pl;
-        if (cell_plan(t, p, c) && (req == GOFR_KERNEL_CELL || c.cell_time < kCellAutoTime)) {
-            c.cells = true;
+        if (cell_plan(t, p, c) && (req == GOFR_KERNEL_CELL || c.cell_time < kCellAutoTime))
             pl = c;
-        }
     }
     if (req == GOFR_KERNEL_CELL && !pl.cells)
         return fail(ctx, GOFR_ERR_UNSUPPORTED,
@@ -792,23 +854,24 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
     if (pl.cells && !ghist) {
         TrajDev &tm = const_cast<TrajDev &>(t);
         if (tm.cell_nc[0] != pl.nc[0] || tm.cell_nc[1] != pl.nc[1] || tm.cell_nc[2] != pl.nc[2]) {
-            cudaFree(tm.d_cstart); cudaFree(tm.d_sid); cudaFree(tm.d_spos); cudaFree(tm.d_stype);
-            tm.d_cstart = nullptr; tm.d_sid = nullptr; tm.d_spos = nullptr; tm.d_stype = nullptr;
+            cudaFree(tm.d_cstart); cudaFree(tm.d_sidt); cudaFree(tm.d_spos);
+            tm.d_cstart = nullptr; tm.d_sidt = nullptr; tm.d_spos = nullptr;
             tm.cell_nc[0] = tm.cell_nc[1] = tm.cell_nc[2] = 0;
             const size_t ncell = (size_t)pl.nc[0] * pl.nc[1] * pl.nc[2];
             const size_t NP = padded_natoms(t.N);
             int *cell_of = nullptr, *rank_of = nullptr, *count = nullptr;
             CK(cudaMalloc(&tm.d_cstart, t.T * (ncell + 1) * sizeof(int)));
-            CK(cudaMalloc(&tm.d_sid, t.T * NP * sizeof(int)));
+            CK(cudaMalloc(&tm.d_sidt, t.T * NP * sizeof(unsigned)));
             CK(cudaMalloc(&tm.d_spos, t.T * 3 * NP * sizeof(float)));
-            CK(cudaMalloc(&tm.d_stype, t.T * NP));
             CK(cudaMalloc(&cell_of, t.T * t.N * sizeof(int)));
             CK(cudaMalloc(&rank_of, t.T * t.N * sizeof(int)));
             CK(cudaMalloc(&count, t.T * (ncell + 1) * sizeof(int)));
             ctx->launches += 3;
-            const int brc = launch_cell_build(t.pos64, t.pos32, t.types8, t.T, t.N, &t.h_box[0],
+            double centre[3];
+            for (int k = 0; k < 3; ++k) centre[k] = t.h_box[k] + t.h_box[3 + k];  // xlo + L/2
+            const int brc = launch_cell_build(t.pos64, t.types8, t.T, t.N, &t.h_box[0], centre,
                                               pl.nc, cell_of, rank_of, count, tm.d_cstart,
-                                              tm.d_spos, tm.d_sid, tm.d_stype, ctx->stream);
+                                              tm.d_spos, tm.d_sidt, ctx->stream);
             cudaStreamSynchronize(ctx->stream);
             cudaFree(cell_of);
             cudaFree(rank_of);
@@ -825,8 +888,7 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
         C.pair.n_items = (long long)L.n_lags * pl.nb[0] * pl.nb[1] * pl.nb[2] * L.n_orig;
         C.start = t.d_cstart;
         C.spos = t.d_spos;
-        C.sid = t.d_sid;
-        C.stype = t.d_stype;
+        C.sidt = t.d_sidt;
         for (int k = 0; k < 3; ++k) { C.nc[k] = pl.nc[k]; C.b[k] = pl.blk[k]; C.nb[k] = pl.nb[k]; }
         C.reach = pl.reach;
         C.r = pl.cell_r;
@@ -970,13 +1032,15 @@ int tune_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
         return GOFR_OK;
     }
     const std::string key = tune_key(t, p);
+    const Plan base_pl = pl;
     auto apply = [&](const TuneChoice &c) {
+        pl = base_pl;
         pl.cells = false;
         if (!c.cells) return;
         for (const CellCand &cc : all)
             if (cc.reach == c.reach && cc.r == c.r && cc.blk == c.blk) {
-                apply_cell(pl, cc);
-                pl.cells = true;
+                Plan q = base_pl;
+                if (make_cell_plan(t, p, q, cc)) pl = q;
                 return;
             }
     };
@@ -999,7 +1063,7 @@ int tune_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
     q.tmax = (unsigned)std::min<double>(leff, std::max(4.0, want));
     q.ntimesteps = std::max<unsigned>(q.tmax, 1);
     q.skip = q.ntimesteps;
-    Plan base = pl;
+    Plan base = base_pl;
     base.cells = false;
     double best_ms = tune_time(ctx, t, q, base);
     tune_log(key, "all-pairs", nullptr, best_ms);
@@ -1014,9 +1078,8 @@ int tune_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
             }
     TuneChoice choice;
     for (const CellCand *c : tries) {
-        Plan cp = pl;
-        cp.cells = true;
-        apply_cell(cp, *c);
+        Plan cp = base_pl;
+        if (!make_cell_plan(t, p, cp, *c)) continue;
         const double ms = tune_time(ctx, t, q, cp);
         tune_log(key, "cells", c, ms);
         if (ms > 0 && (best_ms < 0 || ms < best_ms)) {
@@ -1047,7 +1110,8 @@ int run_common(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_d
     int rc = shape_of(ctx, t, *p, rs);
     if (rc) return rc;
     Plan pl;
-    rc = make_plan(ctx, t, *p, pl);
+    // the tuner starts from the all-pairs plan and decides on cells itself
+    rc = make_plan(ctx, t, *p, pl, p->kernel != GOFR_KERNEL_TUNED);
     if (rc) return rc;
     if (p->kernel == GOFR_KERNEL_TUNED && p->nparts <= 1) {
         rc = tune_plan(ctx, t, *p, pl);
@@ -1121,7 +1185,7 @@ int build_batch(gofr_ctx *ctx)
         p.nparts = 1;
         int rc = shape_of(ctx, t, p, shapes[k]);
         if (rc) return rc;
-        rc = make_plan(ctx, t, p, plans[k]);
+        rc = make_plan(ctx, t, p, plans[k], false);  // the batch kernel is all-pairs
         if (rc) return rc;
         total += (unsigned long long)shapes[k].n_lags * shapes[k].n_orig * t.N * t.N;
     }

@@ -10,12 +10,22 @@
 // goes through exactly the same certified FP32 test and FP64 recheck as the
 // all-pairs kernel, so the counts are identical.
 //
-// Layout per frame: atoms sorted by cell (x fastest), FP32 SoA x|y|z (the
-// same values as the all-pairs frames), original atom ids, u8 types, and the
-// cell start offsets.  A work item is (lag, block of bx*by*bz cells, origin):
-// the block's atoms at the origin frame against the atoms of the block's
-// neighbourhood ((bx+2)(by+2)(bz+2) cells, fewer where that wraps the whole
-// box) at the lagged frame, streamed through shared memory.
+// Cells have edge >= rmax / reach (reach 1 or 2), so such a pair lies at most
+// `reach` cells apart on every axis.  Layout per frame: atoms sorted by cell
+// (x fastest); FP32 SoA x|y|z of the coordinates wrapped into the box in FP64
+// (x - n L, n = floor((x - xlo) / L)) and rounded about the box centre; a
+// u32 word type << 24 | original atom id; and the cell start offsets.  A work
+// item is (lag, origin, block of bx*by*bz cells): the block's atoms at the
+// origin frame against the atoms of the block's neighbourhood
+// ((bx+2 reach)(by+2 reach)(bz+2 reach) cells, never more than the box holds,
+// so every cell appears once) at the lagged frame.  A neighbour cell reached
+// across the box boundary is the periodic image of that cell: its atoms are
+// shifted by +-fl32(L) on that axis when they enter shared memory, so the
+// pair arithmetic is a plain FP32 difference and d2 (6 operations per two
+// pairs as f32x2), the minimum image being the image the neighbourhood
+// selects.  The host certifies these FP32 values with their own error bound
+// (gofr_capi.cu, error_bound_cells), then every candidate goes through the
+// same window test and FP64 recheck as in the all-pairs kernel.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -63,19 +73,11 @@ __device__ __forceinline__ f2 f2fma(f2 a, f2 b, f2 c)
     return r;
 }
 
-// Orthorhombic minimum-image d2 of (i, j0) and (i, j1), the same operations
-// as the all-pairs kernel's pair2 (so FP32 values and bounds are identical).
-__device__ __forceinline__ f2 pair2o(f2 xi, f2 yi, f2 zi, f2 xj, f2 yj, f2 zj, const f2 *invL,
-                                     const f2 *negL)
+// d2 of (i, j0) and (i, j1) for second atoms already in the first atom's
+// image: three differences, then one multiply and two FMAs, as f32x2.
+__device__ __forceinline__ f2 pair2s(f2 xi, f2 yi, f2 zi, f2 xj, f2 yj, f2 zj)
 {
-    const f2 MAG = f2pk(12582912.0f, 12582912.0f);
-    f2 dx = f2sub(xi, xj), dy = f2sub(yi, yj), dz = f2sub(zi, zj);
-    const f2 kx = f2sub(f2fma(dx, invL[0], MAG), MAG);
-    const f2 ky = f2sub(f2fma(dy, invL[1], MAG), MAG);
-    const f2 kz = f2sub(f2fma(dz, invL[2], MAG), MAG);
-    dx = f2fma(kx, negL[0], dx);
-    dy = f2fma(ky, negL[1], dy);
-    dz = f2fma(kz, negL[2], dz);
+    const f2 dx = f2sub(xi, xj), dy = f2sub(yi, yj), dz = f2sub(zi, zj);
     f2 d2 = f2mul(dx, dx);
     d2 = f2fma(dy, dy, d2);
     d2 = f2fma(dz, dz, d2);
@@ -101,7 +103,8 @@ __global__ void k_cell_assign(const double *__restrict__ pos, size_t T, size_t N
          g += (size_t)gridDim.x * blockDim.x) {
         const size_t f = g / N;
         const double *p = pos + g * 3;
-        double u[3] = {(p[0] - xlo) / Lx, (p[1] - ylo) / Ly, (p[2] - zlo) / Lz};
+        double u[3] = {__ddiv_rn(__dsub_rn(p[0], xlo), Lx), __ddiv_rn(__dsub_rn(p[1], ylo), Ly),
+                       __ddiv_rn(__dsub_rn(p[2], zlo), Lz)};
         const int nc[3] = {ncx, ncy, ncz};
         int c[3];
 #pragma unroll
@@ -146,23 +149,31 @@ __global__ void k_cell_scan(const int *__restrict__ count, int *__restrict__ sta
     }
 }
 
-__global__ void k_cell_scatter(const float *__restrict__ pos32, const unsigned char *__restrict__ types8,
-                               size_t T, size_t N, size_t NP, int ncell,
+// Sorted copy of every frame.  Coordinates: w = x - n L with n = floor((x -
+// xlo) / L) (the n of the cell assignment), one FMA in FP64, then
+// fl32(fl64(w - c)) with c the box centre.
+__global__ void k_cell_scatter(const double *__restrict__ pos64,
+                               const unsigned char *__restrict__ types8, size_t T, size_t N,
+                               size_t NP, int ncell, double xlo, double ylo, double zlo, double Lx,
+                               double Ly, double Lz, double cx, double cy, double cz,
                                const int *__restrict__ cell_of, const int *__restrict__ rank_of,
                                const int *__restrict__ start, float *__restrict__ spos,
-                               int *__restrict__ sid, unsigned char *__restrict__ stype)
+                               unsigned *__restrict__ sidt)
 {
+    const double lo[3] = {xlo, ylo, zlo}, L[3] = {Lx, Ly, Lz}, c[3] = {cx, cy, cz};
     for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < T * N;
          g += (size_t)gridDim.x * blockDim.x) {
         const size_t f = g / N, a = g - f * N;
         const size_t d = (size_t)start[f * (size_t)(ncell + 1) + cell_of[g]] + rank_of[g];
-        const float *src = pos32 + f * 3 * NP;
+        const double *p = pos64 + g * 3;
         float *dst = spos + f * 3 * NP;
-        dst[d] = src[a];
-        dst[NP + d] = src[NP + a];
-        dst[2 * NP + d] = src[2 * NP + a];
-        sid[f * NP + d] = (int)a;
-        stype[f * NP + d] = types8[a];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double n = floor(__ddiv_rn(__dsub_rn(p[k], lo[k]), L[k]));
+            const double w = __fma_rn(-n, L[k], p[k]);
+            dst[k * NP + d] = __double2float_rn(__dsub_rn(w, c[k]));
+        }
+        sidt[f * NP + d] = ((unsigned)types8[a] << 24) | (unsigned)a;
     }
 }
 
@@ -171,39 +182,44 @@ __global__ void k_cell_scatter(const float *__restrict__ pos32, const unsigned c
 // ---------------------------------------------------------------------------
 struct Range {
     int begin, end;   // sorted atom indices [begin, end)
+    int shift;        // image of the cells: (sx+1) | (sy+1) << 2 | (sz+1) << 4, s in {-1,0,1}
 };
 
-// Rows of contiguous atom ranges making up a set of cells.
-// ys, zs: the y and z cell coordinates to visit; x cells [x0, x0+nx) wrapped.
+__device__ __forceinline__ int image_of(int c, int n) { return c < 0 ? -1 : (c >= n ? 1 : 0); }
+
+// Rows of contiguous atom ranges making up a set of cells, with the periodic
+// image each row segment is reached in.  Cells [x0, x0+nx) x [y0, y0+ny) x
+// [z0, z0+nz) in unwrapped coordinates, nx <= ncx, ny <= ncy, nz <= ncz (each
+// cell at most once).
 __device__ int build_ranges(const int *start, int ncx, int ncy, int ncz, int x0, int nx, int y0,
                             int ny, int z0, int nz, Range *out)
 {
     int n = 0;
     for (int dz = 0; dz < nz; ++dz) {
-        const int cz = wrapi(z0 + dz, ncz);
+        const int uz = z0 + dz, cz = wrapi(uz, ncz);
         for (int dy = 0; dy < ny; ++dy) {
-            const int cy = wrapi(y0 + dy, ncy);
+            const int uy = y0 + dy, cy = wrapi(uy, ncy);
             const int rowbase = (cz * ncy + cy) * ncx;
-            if (nx >= ncx) {
-                out[n++] = {start[rowbase], start[rowbase + ncx]};
+            const int yz = (image_of(uy, ncy) + 1) << 2 | (image_of(uz, ncz) + 1) << 4;
+            const int a = wrapi(x0, ncx);
+            const int b = a + nx;  // exclusive, may pass the row end
+            // the first segment starts at x0 (image of x0), a wrapped second
+            // segment is one image further
+            const int sx0 = image_of(x0, ncx);
+            if (b <= ncx) {
+                out[n++] = {start[rowbase + a], start[rowbase + b], (sx0 + 1) | yz};
             } else {
-                const int a = wrapi(x0, ncx);
-                const int b = a + nx;  // exclusive, may pass the row end
-                if (b <= ncx) {
-                    out[n++] = {start[rowbase + a], start[rowbase + b]};
-                } else {
-                    out[n++] = {start[rowbase + a], start[rowbase + ncx]};
-                    out[n++] = {start[rowbase], start[rowbase + (b - ncx)]};
-                }
+                out[n++] = {start[rowbase + a], start[rowbase + ncx], (sx0 + 1) | yz};
+                out[n++] = {start[rowbase], start[rowbase + (b - ncx)], (sx0 + 2) | yz};
             }
         }
     }
     return n;
 }
 
-// flat index q of a range list -> sorted atom index (binary search of the
-// prefix table: the last range r with pre[r] <= q)
-__device__ __forceinline__ int flat_to_atom(const Range *rg, const int *pre, int nr, int q)
+// flat index q of a range list -> range (binary search of the prefix table:
+// the last range r with pre[r] <= q); the atom is rg[r].begin + q - pre[r]
+__device__ __forceinline__ int range_of(const int *pre, int nr, int q)
 {
     int lo = 0, hi = nr - 1;
     while (lo < hi) {
@@ -211,19 +227,35 @@ __device__ __forceinline__ int flat_to_atom(const Range *rg, const int *pre, int
         if (pre[mid] <= q) lo = mid;
         else hi = mid - 1;
     }
-    return rg[lo].begin + (q - pre[lo]);
+    return lo;
 }
 
+// 4-byte asynchronous global -> shared copy (no register staging).
+__device__ __forceinline__ void cp_async4(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Work items are (lag, origin, block of cells), block fastest, handed to the
+// CTAs round-robin: the CTAs running at one time share a few frames, which
+// stay in L2.  Each item streams its neighbourhood atoms through two
+// shared-memory tiles, the next one copied asynchronously while the current
+// one is evaluated.
 template <int R>
 __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
 {
     constexpr int TI = NT * R;
     extern __shared__ __align__(128) unsigned char smem[];
     const PairLaunch &P = C.pair;
-    float *jx = reinterpret_cast<float *>(smem);                 // [3][TJ]
-    int *jid = reinterpret_cast<int *>(jx + 3 * TJ);              // [TJ]
-    unsigned char *jt = reinterpret_cast<unsigned char *>(jid + TJ);  // [TJ]
-    uint2 *slots = reinterpret_cast<uint2 *>(jt + TJ);            // [SLOTS][NT]
+    unsigned *jbuf = reinterpret_cast<unsigned *>(smem);          // [2][x|y|z|id-type][TJ]
+    uint2 *slots = reinterpret_cast<uint2 *>(jbuf + 2 * 4 * TJ);  // [SLOTS][NT]
     uint4 *rq = reinterpret_cast<uint4 *>(slots + SLOTS * NT);    // [QCAP]
     float2 *win = reinterpret_cast<float2 *>(rq + QCAP);          // [nbin]
     unsigned *hist = reinterpret_cast<unsigned *>(win + P.nbin);  // [nch][nbin]
@@ -244,32 +276,26 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
     const int nbx = C.nb[0], nby = C.nb[1], nbz = C.nb[2];
     const long long nblocks = (long long)nbx * nby * nbz;
     const long long per_lag = nblocks * P.n_orig;
-    const long long per = (P.n_items + gridDim.x - 1) / gridDim.x;
-    const long long it0 = (long long)blockIdx.x * per;
-    const long long it1 = min(it0 + per, P.n_items);
     const long long NP = P.NP;
     const int ncell = C.nc[0] * C.nc[1] * C.nc[2];
     const float hi_f = P.hi_f;
-    f2 invL[3], negL[3];
+    float L32[3];
     int cur_lag = -1;
     long long pairs_since = 0;
     unsigned long long n_cand = 0, n_rech = 0, n_eval = 0;
     uint2 *const my_slots = slots + tid;
 
-    for (long long item = it0; item < it1; ++item) {
+    for (long long item = blockIdx.x; item < P.n_items; item += gridDim.x) {
         const int lag_idx = (int)(item / per_lag);
         const long long rem = item - (long long)lag_idx * per_lag;
-        const int blk = (int)(rem / P.n_orig);
-        const int k = (int)(rem - (long long)blk * P.n_orig);
+        const int k = (int)(rem / nblocks);
+        const int blk = (int)(rem - (long long)k * nblocks);
         const long long fo = P.primo + (long long)k * P.skip;
         const long long fl = fo + (long long)lag_idx * P.every;
         {
-            const Box32 b = P.box32[fo];
+            const Box32 b = P.box32[fo];  // the box is the same in every frame
 #pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                invL[a] = f2pk(b.invL[a], b.invL[a]);
-                negL[a] = f2pk(-b.L[a], -b.L[a]);
-            }
+            for (int a = 0; a < 3; ++a) L32[a] = b.L[a];
         }
         const int bz = blk / (nbx * nby), by = (blk / nbx) % nby, bx = blk % nbx;
         const int cx0 = bx * C.b[0], cy0 = by * C.b[1], cz0 = bz * C.b[2];
@@ -280,13 +306,10 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
             const int *st_o = C.start + fo * (size_t)(ncell + 1);
             const int *st_l = C.start + fl * (size_t)(ncell + 1);
             nir = build_ranges(st_o, C.nc[0], C.nc[1], C.nc[2], cx0, cnx, cy0, cny, cz0, cnz, irg);
+            // b + 2 reach <= nc on every axis (host plan): each cell once
             const int m = C.reach;
-            const int jnx = min(cnx + 2 * m, C.nc[0]), jny = min(cny + 2 * m, C.nc[1]),
-                      jnz = min(cnz + 2 * m, C.nc[2]);
-            const int jx0 = jnx == C.nc[0] ? 0 : cx0 - m;
-            const int jy0 = jny == C.nc[1] ? 0 : cy0 - m;
-            const int jz0 = jnz == C.nc[2] ? 0 : cz0 - m;
-            njr = build_ranges(st_l, C.nc[0], C.nc[1], C.nc[2], jx0, jnx, jy0, jny, jz0, jnz, jrg);
+            njr = build_ranges(st_l, C.nc[0], C.nc[1], C.nc[2], cx0 - m, cnx + 2 * m, cy0 - m,
+                               cny + 2 * m, cz0 - m, cnz + 2 * m, jrg);
             ipre[0] = 0;
             for (int r = 0; r < nir; ++r) ipre[r + 1] = ipre[r] + (irg[r].end - irg[r].begin);
             jpre[0] = 0;
@@ -318,10 +341,56 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
         n_eval += (tid == 0) ? (unsigned long long)n_i * n_j : 0ull;
         const float *fo32 = C.spos + fo * 3 * NP;
         const float *fl32 = C.spos + fl * 3 * NP;
-        const int *fo_id = C.sid + fo * NP;
-        const int *fl_id = C.sid + fl * NP;
-        const unsigned char *fo_t = C.stype + fo * NP;
-        const unsigned char *fl_t = C.stype + fl * NP;
+        const unsigned *fo_idt = C.sidt + fo * NP;
+        const unsigned *fl_idt = C.sidt + fl * NP;
+        const int ntile = (n_j + TJ - 1) / TJ;
+
+        // Copies tile t of the neighbourhood into buffer t & 1 (all threads;
+        // thread tid takes elements tid + k NT, k < TJ / NT) and returns the
+        // image codes of this thread's elements, 6 bits each.
+        auto load_tile = [&](int t) -> unsigned {
+            const int jbase = t * TJ;
+            const int tj = min(TJ, n_j - jbase);
+            unsigned *dst = jbuf + (t & 1) * 4 * TJ;
+            unsigned codes = 0u;
+#pragma unroll
+            for (int e = 0; e < TJ / NT; ++e) {
+                const int q = tid + e * NT;
+                if (q < tj) {
+                    const int r = range_of(jpre, njr, jbase + q);
+                    const int s = jrg[r].begin + (jbase + q - jpre[r]);
+                    codes |= (unsigned)jrg[r].shift << (6 * e);
+                    cp_async4(dst + q, fl32 + s);
+                    cp_async4(dst + TJ + q, fl32 + NP + s);
+                    cp_async4(dst + 2 * TJ + q, fl32 + 2 * NP + s);
+                    cp_async4(dst + 3 * TJ + q, fl_idt + s);
+                } else if (q < ((tj + 3) & ~3)) {
+                    // no atom: NaN never passes d2 <= hi_f
+                    dst[q] = dst[TJ + q] = dst[2 * TJ + q] = 0x7fc00000u;
+                    dst[3 * TJ + q] = 0xffffffffu;
+                }
+            }
+            cp_async_commit();
+            return codes;
+        };
+        // Moves this thread's elements of tile t (copies complete) to the
+        // image of their cell: x += s fl32(L), one FP32 rounding.
+        auto shift_tile = [&](int t, unsigned codes) {
+            const int tj = min(TJ, n_j - t * TJ);
+            float *xs = reinterpret_cast<float *>(jbuf + (t & 1) * 4 * TJ);
+#pragma unroll
+            for (int e = 0; e < TJ / NT; ++e) {
+                const int q = tid + e * NT;
+                const unsigned c = (codes >> (6 * e)) & 63u;
+                if (q < tj && c != 21u) {  // 21: image (0, 0, 0)
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const int sa = (int)((c >> (2 * a)) & 3u) - 1;
+                        if (sa) xs[a * TJ + q] = __fadd_rn(xs[a * TJ + q], sa > 0 ? L32[a] : -L32[a]);
+                    }
+                }
+            }
+        };
 
         for (int ibase = 0; ibase < n_i; ibase += TI) {
             f2 xi[R], yi[R], zi[R];
@@ -331,10 +400,12 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
                 const int q = ibase + r * NT + tid;
                 float x, y, z;
                 if (q < n_i) {
-                    const int s = flat_to_atom(irg, ipre, nir, q);
+                    const int rr = range_of(ipre, nir, q);
+                    const int s = irg[rr].begin + (q - ipre[rr]);  // block cells: image (0,0,0)
                     x = fo32[s]; y = fo32[NP + s]; z = fo32[2 * NP + s];
-                    ti[r] = fo_t[s];
-                    iid[r] = fo_id[s];
+                    const unsigned v = fo_idt[s];
+                    ti[r] = (int)(v >> 24);
+                    iid[r] = (int)(v & 0xffffffu);
                 } else {
                     x = y = z = __int_as_float(0x7fc00000);
                     ti[r] = 0;
@@ -343,25 +414,21 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
                 xi[r] = f2pk(x, x); yi[r] = f2pk(y, y); zi[r] = f2pk(z, z);
             }
             int cnt = 0;
-            for (int jbase = 0; jbase < n_j; jbase += TJ) {
-                const int tj = min(TJ, n_j - jbase);
-                __syncthreads();  // previous tile consumed
-                for (int q = tid; q < TJ; q += NT) {
-                    if (q < tj) {
-                        const int s = flat_to_atom(jrg, jpre, njr, jbase + q);
-                        jx[q] = fl32[s];
-                        jx[TJ + q] = fl32[NP + s];
-                        jx[2 * TJ + q] = fl32[2 * NP + s];
-                        jid[q] = fl_id[s];
-                        jt[q] = fl_t[s];
-                    } else if (q < ((tj + 3) & ~3)) {
-                        const float nan = __int_as_float(0x7fc00000);
-                        jx[q] = nan; jx[TJ + q] = nan; jx[2 * TJ + q] = nan;
-                        jid[q] = -2;
-                        jt[q] = 0;
-                    }
+            unsigned codes = load_tile(0);
+            for (int t = 0; t < ntile; ++t) {
+                const int tj = min(TJ, n_j - t * TJ);
+                unsigned next = 0u;
+                if (t + 1 < ntile) {
+                    next = load_tile(t + 1);
+                    cp_async_wait<1>();
+                } else {
+                    cp_async_wait<0>();
                 }
-                __syncthreads();
+                shift_tile(t, codes);
+                codes = next;
+                __syncthreads();  // tile t in shared memory for every thread
+                const float *jx = reinterpret_cast<const float *>(jbuf + (t & 1) * 4 * TJ);
+                const unsigned *jidt = jbuf + (t & 1) * 4 * TJ + 3 * TJ;
 
                 // Bins every slot of this warp's lanes, two slots per round
                 // so that their shared-memory load chains overlap.
@@ -388,9 +455,11 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
                                 t_i = (r == rr) ? ti[rr] : t_i;
                                 a_ = (r == rr) ? iid[rr] : a_;
                             }
+                            const unsigned jv = jidt[jj];
                             ia[u] = a_;
-                            ja[u] = jid[jj];
-                            ch[u] = chtab[t_i * P.ntypes + jt[jj]] + (ia[u] == ja[u] ? half : 0);
+                            ja[u] = (int)(jv & 0xffffffu);
+                            ch[u] = chtab[t_i * P.ntypes + (int)(jv >> 24)] +
+                                    (ia[u] == ja[u] ? half : 0);
                             const int b_ = __float2int_rd(
                                 __fmul_rn(__fsub_rn(sqrt_guess(d2), P.rmin_f), P.inv_dr_f));
                             bi[u] = min(max(b_, 0), P.nbin - 1);
@@ -435,8 +504,8 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
                     const f2 za = f2pk(Z.x, Z.y), zb = f2pk(Z.z, Z.w);
 #pragma unroll
                     for (int r = 0; r < R; ++r) {
-                        const f2 da = pair2o(xi[r], yi[r], zi[r], xa, ya, za, invL, negL);
-                        const f2 db = pair2o(xi[r], yi[r], zi[r], xb, yb, zb, invL, negL);
+                        const f2 da = pair2s(xi[r], yi[r], zi[r], xa, ya, za);
+                        const f2 db = pair2s(xi[r], yi[r], zi[r], xb, yb, zb);
                         float d0, d1, d2v, d3;
                         f2up(da, d0, d1);
                         f2up(db, d2v, d3);
@@ -449,6 +518,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
                     }
                 }
                 if (__any_sync(0xffffffffu, cnt > 0)) warp_flush();
+                __syncthreads();  // every thread done with buffer t & 1
             }
         }
         // end of item: FP64 recheck queue of this item's frames, all threads together
@@ -490,7 +560,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
 int cell_smem_bytes(int nch, int nbin, int ntypes)
 {
     using namespace cells;
-    size_t b = (size_t)3 * TJ * 4 + TJ * 4 + TJ + (size_t)SLOTS * NT * 8 + (size_t)QCAP * 16 +
+    size_t b = (size_t)2 * 4 * TJ * 4 + (size_t)SLOTS * NT * 8 + (size_t)QCAP * 16 +
                (size_t)nbin * 8 + (size_t)nch * nbin * 4 + (size_t)ntypes * ntypes * 2;
     return (int)((b + 127) / 128 * 128);
 }
@@ -498,28 +568,29 @@ int cell_smem_bytes(int nch, int nbin, int ntypes)
 int cell_block_atoms(int r) { return cells::NT * r; }
 int cell_max_ranges() { return cells::MAXR; }
 
-int launch_cell_build(const double *pos64, const float *pos32, const unsigned char *types8,
-                      size_t T, size_t N, const double *box_internal, const int *nc,
-                      int *cell_of, int *rank_of, int *count, int *start, float *spos, int *sid,
-                      unsigned char *stype, cudaStream_t s)
+int launch_cell_build(const double *pos64, const unsigned char *types8, size_t T, size_t N,
+                      const double *box_internal, const double *centre, const int *nc,
+                      int *cell_of, int *rank_of, int *count, int *start, float *spos,
+                      unsigned *sidt, cudaStream_t s)
 {
     using namespace cells;
     const int ncell = nc[0] * nc[1] * nc[2];
     if (cudaMemsetAsync(count, 0, T * (size_t)(ncell + 1) * sizeof(int), s) != cudaSuccess)
         return -1;
     const size_t NP = padded_natoms(N);
-    // padding of the sorted frames: NaN coordinates, id -1
+    // padding of the sorted frames: NaN coordinates (never read as atoms)
     if (cudaMemsetAsync(spos, 0xff, T * 3 * NP * sizeof(float), s) != cudaSuccess) return -1;
     const size_t total = T * N;
     int blocks = (int)((total + NT - 1) / NT);
     if (blocks > 152 * 16) blocks = 152 * 16;
+    const double Lx = 2.0 * box_internal[3], Ly = 2.0 * box_internal[4], Lz = 2.0 * box_internal[5];
     k_cell_assign<<<blocks, NT, 0, s>>>(pos64, T, N, box_internal[0], box_internal[1],
-                                        box_internal[2], 2.0 * box_internal[3],
-                                        2.0 * box_internal[4], 2.0 * box_internal[5], nc[0], nc[1],
-                                        nc[2], cell_of, rank_of, count);
+                                        box_internal[2], Lx, Ly, Lz, nc[0], nc[1], nc[2], cell_of,
+                                        rank_of, count);
     k_cell_scan<<<(unsigned)T, NT, 0, s>>>(count, start, ncell);
-    k_cell_scatter<<<blocks, NT, 0, s>>>(pos32, types8, T, N, NP, ncell, cell_of, rank_of, start,
-                                         spos, sid, stype);
+    k_cell_scatter<<<blocks, NT, 0, s>>>(pos64, types8, T, N, NP, ncell, box_internal[0],
+                                         box_internal[1], box_internal[2], Lx, Ly, Lz, centre[0],
+                                         centre[1], centre[2], cell_of, rank_of, start, spos, sidt);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

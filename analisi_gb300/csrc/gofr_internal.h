@@ -69,8 +69,7 @@ struct CellLaunch {
     PairLaunch pair;
     const int *start;              // [T][ncell+1] sorted-atom offset of each cell
     const float *spos;             // [T][3][NP] FP32 frames sorted by cell
-    const int *sid;                // [T][NP] original atom id of each sorted slot
-    const unsigned char *stype;    // [T][NP] type id of each sorted slot
+    const unsigned *sidt;          // [T][NP] type << 24 | original atom id of each sorted slot
     int nc[3];                     // cells per axis
     int b[3];                      // cells per block per axis
     int nb[3];                     // blocks per axis
@@ -81,10 +80,10 @@ struct CellLaunch {
 int cell_smem_bytes(int nch, int nbin, int ntypes);
 int cell_block_atoms(int r);
 int cell_max_ranges();
-int launch_cell_build(const double *pos64, const float *pos32, const unsigned char *types8,
-                      size_t T, size_t N, const double *box_internal, const int *nc,
-                      int *cell_of, int *rank_of, int *count, int *start, float *spos, int *sid,
-                      unsigned char *stype, cudaStream_t s);
+int launch_cell_build(const double *pos64, const unsigned char *types8, size_t T, size_t N,
+                      const double *box_internal, const double *centre, const int *nc,
+                      int *cell_of, int *rank_of, int *count, int *start, float *spos,
+                      unsigned *sidt, cudaStream_t s);
 int launch_cell_pairs(const CellLaunch &C, int num_sms, cudaStream_t s);
 
 // Launch configuration helpers implemented in gofr_kernels.cu.

@@ -61,6 +61,35 @@ def test_cells_match_oracle_and_all_pairs(gpu_engine, oracle_mod, case, plan, mo
     np.testing.assert_array_equal(allp, ref)
 
 
+@pytest.mark.parametrize("plan", [None, "1,3,1,1,1", "2,2,1,2,1", "2,4,2,2,2"],
+                         ids=["auto", "1,3,1,1,1", "2,2,1,2,1", "2,4,2,2,2"])
+def test_cells_far_unwrapped_coordinates(gpu_engine, oracle_mod, plan, monkeypatch):
+    """Atoms several box lengths outside the cell (the reference iterates its
+    minimum image), a box not at the origin and the all-wrapped neighbour
+    images: the cell path wraps every coordinate into the box first and must
+    still count exactly what the oracle counts."""
+    if plan is None:
+        monkeypatch.delenv("ANALISI_GB300_CELL_PLAN", raising=False)
+    else:
+        monkeypatch.setenv("ANALISI_GB300_CELL_PLAN", plan)
+    w = workloads.small_case(65, 2400, 7, 26.0, 0.4, [1500, 900], rmin=0.3, rmax=5.0, nbin=45,
+                             tmax=3, skip=2, every=1, ntimesteps=4, primo=0)
+    rng = np.random.default_rng(650)
+    L = 26.0
+    w["positions"] = w["positions"] + L * rng.integers(-4, 5, size=(1, 2400, 3))
+    w["boxes"] = w["boxes"].copy()
+    w["boxes"][:, 0:3] += np.array([-7.5, 3.25, 11.0])
+    w["positions"] = w["positions"] + np.array([-7.5, 3.25, 11.0])
+    p = w["params"]
+    ref = oracle_mod.gofrt_counts(w["positions"], w["boxes"], w["type_ids"], w["ntypes"],
+                                  p["rmin"], p["rmax"], p["nbin"], p["tmax"], 8, p["skip"],
+                                  p["every"], p["ntimesteps"], p["primo"])
+    assert ref.sum() > 0
+    cell, st = _run(gpu_engine, w, "cell")
+    assert st["kernel_used"] == 3
+    np.testing.assert_array_equal(cell, ref)
+
+
 def test_cell_kernel_refuses_small_box(gpu_engine):
     from analisi_gb300 import engine
     w = workloads.small_case(64, 200, 6, 10.0, 0.1, [200], rmin=0.0, rmax=4.0, nbin=10, tmax=2,
