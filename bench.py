@@ -16,13 +16,20 @@ exactly the full reset(1800) calculation, split the way the reference's
 block-average driver splits a trajectory.
 
   value   pair throughput with the frames resident in HBM (device-timed with
-          CUDA events on the engine's stream, L2 flushed between steps)
+          CUDA events on the engine's stream, L2 flushed between steps).
+          Pairs are the reference's: N^2 ordered pairs per (lag, origin).
+          The engine's default (auto) plan may take the cell-list kernel,
+          which evaluates only the pairs of neighbouring cells (the others
+          are provably beyond rmax); the counts are identical, so the value
+          is the all-pairs-equivalent rate, and config.evaluated_frac says
+          what share of the pairs was evaluated
   e2e     the same metric through the C ABI with host buffers: every step
           uploads its 400-frame window from pinned host memory
           (gofr_set_frames) and reads the counts back (gofr_run)
-  roofline  FP32-issue bound: 16 FP32 lane operations per ordered pair
-          (orthorhombic), against the FP32 lane-op peak measured on this GPU
-          by gofr_measure_peaks
+  roofline  FP32-issue bound of the pair kernel used: 16 FP32 lane operations
+          per ordered pair for the all-pairs kernel (orthorhombic minimum
+          image), 7 per evaluated pair for the cell-list kernel, against the
+          FP32 lane-op peak measured on this GPU by gofr_measure_peaks
   cpu_baseline  the C restatement of the reference (oracle/gofr_oracle.c,
           same fork/join thread split as the reference) on this host's cores,
           on a bounded sample of the same workload
@@ -47,6 +54,7 @@ UNIT = "Gpairs/s"
 ORIGINS_PER_STEP = 50
 STEP_WINDOWS = 9  # windows of ORIGINS_PER_STEP origins in reset(1800)
 OPS_PER_PAIR = 16  # orthorhombic FP32 pair: 3 sub + 3x(ffma, fadd, ffma) + fmul + 2 ffma + cmp
+OPS_PER_PAIR_CELL = 7  # cell-list pair, images pre-shifted: 3 sub + fmul + 2 ffma + cmp
 
 
 def parse():
@@ -472,17 +480,21 @@ def run_gpu(args):
     fp32_peak, satom_peak = engine.measure_peaks(local)
     kernel_used = max(kernels_used) if kernels_used else 0
     evaluated_per_launch = evaluated / args.steps
-    achieved = evaluated_per_launch * OPS_PER_PAIR / kernel_avg_s / 1e12
+    ops_per_pair = OPS_PER_PAIR_CELL if kernel_used == 3 else OPS_PER_PAIR
+    achieved = evaluated_per_launch * ops_per_pair / kernel_avg_s / 1e12
     peak = fp32_peak / 1e12
     traffic = traffic_from_profiles(kernel_used)
     roof = {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(peak, 3),
             "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
             "traffic": traffic,
-            "notes": "FP32 lane operations (one FADD/FMUL/FFMA = 1) at 16 per evaluated "
-                     "ordered pair (all N^2 pairs for the all-pairs kernel, the cell "
-                     "neighbourhoods' pairs for the cell-list kernel); peak = FFMA issue rate "
-                     "measured on this GPU (gofr_measure_peaks, burst); traffic = ncu dram "
-                     "bytes per launch (profiles/)",
+            "notes": "FP32 lane operations (one FADD/FMUL/FFMA = 1) per evaluated ordered "
+                     "pair: 16 for the all-pairs kernel (minimum image per pair, all N^2 "
+                     "pairs), 7 for the cell-list kernel (images shifted once per tile "
+                     "element; the pairs of the cell neighbourhoods); the binning of the "
+                     "candidates (d <= rmax) is not counted; peak = FFMA issue rate measured "
+                     "on this GPU (gofr_measure_peaks, burst); traffic = ncu dram bytes per "
+                     "launch (profiles/)",
+            "ops_per_evaluated_pair": ops_per_pair,
             "kernel": KERNEL_NAMES.get(kernel_used, str(kernel_used)),
             "evaluated_pairs_per_launch": int(evaluated_per_launch),
             "smem_atomic_peak_per_s": satom_peak,

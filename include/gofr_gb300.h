@@ -55,16 +55,21 @@ enum gofr_box_kind {
 };
 
 enum gofr_kernel {
-    GOFR_KERNEL_AUTO = 0,        /* FP32 bulk + FP64 edge recheck when certifiable, else FP64 */
-    GOFR_KERNEL_F32_RECHECK = 1, /* force the FP32 + recheck kernel (error if not certifiable) */
+    GOFR_KERNEL_AUTO = 0,        /* FP32 bulk + FP64 edge recheck when certifiable, else FP64;
+                                    the cell-list form when its modelled time is lower */
+    GOFR_KERNEL_F32_RECHECK = 1, /* force the all-pairs FP32 + recheck kernel (error if not
+                                    certifiable) */
     GOFR_KERNEL_F64 = 2,         /* plain FP64 kernel: reference arithmetic for every pair */
-    GOFR_KERNEL_CELL = 3,        /* cell-list FP32 + recheck kernel (large N) */
+    GOFR_KERNEL_CELL = 3,        /* cell-list FP32 + recheck kernel (error if not eligible);
+                                    ANALISI_GB300_CELL_PLAN="reach,r,bx,by,bz" pins its
+                                    configuration when that one is eligible */
     GOFR_KERNEL_TUNED = 4        /* AUTO, but the all-pairs / cell-list form and the cell
-                                    block shape are picked by timing them on a sample of
+                                    configuration are picked by timing them on a sample of
                                     the job; the choice is remembered per key
                                     (log2 N, nbin, ntypes, box kind, cell grid) in the
                                     process and, when the environment variable
-                                    ANALISI_GB300_TUNE_CACHE names a file, across runs */
+                                    ANALISI_GB300_TUNE_CACHE names a file, across runs
+                                    (ANALISI_GB300_TUNE_LOG: a file for every timing) */
 };
 
 /* Parameters of one Gofrt::calculate (lib/include/gofrt.h:37-45 constructor
