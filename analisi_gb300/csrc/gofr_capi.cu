@@ -64,6 +64,10 @@ struct TrajDev {
     int *d_cstart = nullptr;
     unsigned *d_sidt = nullptr;
     float *d_spos = nullptr;
+    // MSD: atoms sorted by type, type starts, optional centres of mass
+    std::vector<int> h_perm, h_tbegin;
+    int *d_perm = nullptr, *d_tbegin = nullptr;
+    double *d_cm = nullptr;          // [T][ntypes][3]
 };
 
 }  // namespace
@@ -82,6 +86,8 @@ struct gofr_ctx {
     size_t cap_chtab = 0;
     unsigned *d_err = nullptr;
     unsigned long long *d_stats = nullptr;
+    double *d_msd_partial = nullptr, *d_msd_out = nullptr;
+    size_t cap_msd_partial = 0, cap_msd_out = 0;
     double *d_minmax = nullptr;
     unsigned *d_nonfinite = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -170,6 +176,10 @@ void free_traj(TrajDev &t)
     cudaFree(t.d_cstart);
     cudaFree(t.d_sidt);
     cudaFree(t.d_spos);
+    cudaFree(t.d_perm);
+    cudaFree(t.d_tbegin);
+    cudaFree(t.d_cm);
+    t.d_perm = nullptr; t.d_tbegin = nullptr; t.d_cm = nullptr;
     t.pos64 = nullptr; t.pos32 = nullptr; t.box64 = nullptr; t.box32 = nullptr; t.types = nullptr;
     t.types8 = nullptr;
     t.d_cstart = nullptr; t.d_sidt = nullptr; t.d_spos = nullptr;
@@ -513,6 +523,21 @@ int upload_traj(gofr_ctx *ctx, TrajDev &t, const double *positions, const double
                        ctx->stream));
     CK(cudaMemcpyAsync(t.types, type_ids, natoms * sizeof(int), cudaMemcpyHostToDevice,
                        ctx->stream));
+    // atoms sorted by type (stable), for the per-type sums of the MSD
+    t.h_tbegin.assign(ntypes + 1, 0);
+    for (size_t a = 0; a < natoms; ++a) t.h_tbegin[type_ids[a] + 1]++;
+    for (unsigned k = 0; k < ntypes; ++k) t.h_tbegin[k + 1] += t.h_tbegin[k];
+    t.h_perm.resize(natoms);
+    {
+        std::vector<int> fill(t.h_tbegin.begin(), t.h_tbegin.end() - 1);
+        for (size_t a = 0; a < natoms; ++a) t.h_perm[fill[type_ids[a]]++] = (int)a;
+    }
+    CK(cudaMalloc(&t.d_perm, natoms * sizeof(int)));
+    CK(cudaMalloc(&t.d_tbegin, (ntypes + 1) * sizeof(int)));
+    CK(cudaMemcpyAsync(t.d_perm, t.h_perm.data(), natoms * sizeof(int), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(t.d_tbegin, t.h_tbegin.data(), (ntypes + 1) * sizeof(int),
+                       cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemsetAsync(ctx->d_nonfinite, 0, sizeof(unsigned), ctx->stream));
     ++ctx->launches;
     if (launch_minmax(t.pos64, nframes * natoms, ctx->d_minmax, ctx->d_nonfinite, ctx->stream))
@@ -1392,6 +1417,8 @@ void gofr_ctx_destroy(gofr_ctx *ctx)
         cudaFree(ctx->d_stats);
         cudaFree(ctx->d_minmax);
         cudaFree(ctx->d_nonfinite);
+        cudaFree(ctx->d_msd_partial);
+        cudaFree(ctx->d_msd_out);
         for (auto &e : ctx->ev)
             if (e) cudaEventDestroy(e);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1782,6 +1809,99 @@ int gofr_batch_run(gofr_ctx *ctx, int use_graph, unsigned long long *counts_host
     if (rc) return rc;
     std::memcpy(counts_host, B.h_stage, ctx->batch_total * sizeof(unsigned long long));
     return GOFR_OK;
+}
+
+int gofr_set_centres(gofr_ctx *ctx, const double *centres, size_t nframes, unsigned ntypes)
+{
+    if (!ctx) return GOFR_ERR_ARG;
+    if (!centres) return fail(ctx, GOFR_ERR_ARG, "null centres");
+    if (ctx->trajs.size() != 1) return fail(ctx, GOFR_ERR_STATE, "no frames uploaded");
+    TrajDev &t = ctx->trajs[0];
+    if (nframes != t.T || ntypes != t.ntypes)
+        return fail(ctx, GOFR_ERR_ARG, "centres are [%zu][%u][3], the frames need [%zu][%u][3]",
+                    nframes, ntypes, t.T, t.ntypes);
+    DevGuard g(ctx->device);
+    cudaFree(t.d_cm);
+    t.d_cm = nullptr;
+    const size_t n = nframes * ntypes * 3;
+    CK(cudaMalloc(&t.d_cm, n * sizeof(double)));
+    CK(cudaMemcpyAsync(t.d_cm, centres, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return GOFR_OK;
+}
+
+int gofr_msd_output_size(const gofr_ctx *ctx_c, const gofr_msd_params *p, size_t *n)
+{
+    gofr_ctx *ctx = const_cast<gofr_ctx *>(ctx_c);
+    if (!ctx || !p || !n) return GOFR_ERR_ARG;
+    if (ctx->trajs.size() != 1) return fail(ctx, GOFR_ERR_STATE, "no frames uploaded");
+    const unsigned leff = (p->ntimesteps < p->tmax || p->tmax == 0) ? p->ntimesteps : p->tmax;
+    *n = (size_t)leff * (p->center_of_mass ? 2 : 1) * ctx->trajs[0].ntypes;
+    return GOFR_OK;
+}
+
+// MSD<T>::calc_init + calc_single_th (lib/src/msd.cpp:57-118) on the resident frames.
+int gofr_msd_run(gofr_ctx *ctx, const gofr_msd_params *p, double *out_host)
+{
+    if (!ctx) return GOFR_ERR_ARG;
+    if (!p) return fail(ctx, GOFR_ERR_ARG, "null params");
+    if (ctx->trajs.size() != 1) return fail(ctx, GOFR_ERR_STATE, "no frames uploaded");
+    const TrajDev &t = ctx->trajs[0];
+    const unsigned skip = p->skip ? p->skip : 1;
+    const unsigned leff = (p->ntimesteps < p->tmax || p->tmax == 0) ? p->ntimesteps : p->tmax;
+    if ((unsigned long long)leff + p->ntimesteps + p->primo > (unsigned long long)t.T)
+        return fail(ctx, GOFR_ERR_RANGE,
+                    "trajectory is too short for this kind of calculation. Select a different "
+                    "starting timestep or lower the size of the average or the lenght of the "
+                    "time lag");
+    if ((p->center_of_mass || p->in_center_of_mass_frame) && !t.d_cm)
+        return fail(ctx, GOFR_ERR_STATE,
+                    "the centre-of-mass options need the per-type centres (gofr_set_centres)");
+    const int fk = (p->center_of_mass ? 2 : 1) * (int)t.ntypes;
+    const size_t nout = (size_t)leff * fk;
+    const unsigned n_orig = (p->ntimesteps + skip - 1) / skip;
+    DevGuard g(ctx->device);
+    std::memset(&ctx->stats, 0, sizeof ctx->stats);
+    if (nout == 0) return GOFR_OK;
+    if (n_orig == 0) {  // no origin: the reference leaves its zeroed buffer
+        std::memset(out_host, 0, nout * sizeof(double));
+        return GOFR_OK;
+    }
+    int rc = ensure(ctx, ctx->d_msd_partial, ctx->cap_msd_partial, nout * n_orig);
+    if (rc) return rc;
+    rc = ensure(ctx, ctx->d_msd_out, ctx->cap_msd_out, nout);
+    if (rc) return rc;
+    MsdLaunch M{};
+    M.pos64 = t.pos64;
+    M.cm = t.d_cm;
+    M.perm = t.d_perm;
+    M.tbegin = t.d_tbegin;
+    M.partial = ctx->d_msd_partial;
+    M.N = (int)t.N;
+    M.ntypes = (int)t.ntypes;
+    M.leff = (int)leff;
+    M.n_orig = (int)n_orig;
+    M.skip = (int)skip;
+    M.primo = (long long)p->primo;
+    M.cm_msd = p->center_of_mass ? 1 : 0;
+    M.cm_self = p->in_center_of_mass_frame ? 1 : 0;
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_stats, 0, ST_COUNT * sizeof(unsigned long long), ctx->stream));
+    CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+    ctx->launches += 2;
+    if (launch_msd(M, ctx->d_msd_out, ctx->num_sms, ctx->stream))
+        return fail(ctx, GOFR_ERR_CUDA, "MSD kernel launch failed: %s",
+                    cudaGetErrorString(cudaGetLastError()));
+    CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+    CK(cudaMemcpyAsync(out_host, ctx->d_msd_out, nout * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+    // one squared displacement per (lag, origin, atom)
+    ctx->stats.pairs = (unsigned long long)leff * n_orig * t.N;
+    ctx->stats.evaluated = ctx->stats.pairs;
+    ctx->stats.kernel_used = -1;
+    return gofr_sync(ctx);
 }
 
 }  // extern "C"

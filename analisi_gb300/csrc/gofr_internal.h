@@ -80,6 +80,19 @@ struct CellLaunch {
 int cell_smem_bytes(int nch, int nbin, int ntypes);
 int cell_block_atoms(int r);
 int cell_max_ranges();
+// Mean square displacement (gofr_msd.cu)
+struct MsdLaunch {
+    const double *pos64;    // [T][N][3]
+    const double *cm;       // [T][ntypes][3] centres of mass (or null)
+    const int *perm;        // [N] atom ids sorted by type (stable)
+    const int *tbegin;      // [ntypes + 1] start of each type in perm
+    double *partial;        // [leff][n_orig][f_cm * ntypes] sums over atoms
+    int N, ntypes, leff, n_orig, skip;
+    long long primo;
+    int cm_msd, cm_self;
+};
+int launch_msd(const MsdLaunch &M, double *out_device, int num_sms, cudaStream_t s);
+
 int launch_cell_build(const double *pos64, const unsigned char *types8, size_t T, size_t N,
                       const double *box_internal, const double *centre, const int *nc,
                       int *cell_of, int *rank_of, int *count, int *start, float *spos,

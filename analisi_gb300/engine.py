@@ -26,7 +26,8 @@ EXPORTED = [
     "gofr_output_size", "gofr_run", "gofr_run_device", "gofr_sync", "gofr_get_stats",
     "gofr_counts_to_buffer", "gofr_bin_thresholds", "gofr_batch_set",
     "gofr_batch_output_layout", "gofr_batch_run", "gofr_measure_peaks",
-    "gofr_run_f64_noalloc", "gofr_run_windows",
+    "gofr_run_f64_noalloc", "gofr_run_windows", "gofr_set_centres", "gofr_msd_output_size",
+    "gofr_msd_run",
 ]
 
 
@@ -45,6 +46,12 @@ class Params(ctypes.Structure):
                 ("tmax", ctypes.c_uint), ("skip", ctypes.c_uint), ("every", ctypes.c_uint),
                 ("ntimesteps", ctypes.c_uint), ("primo", ctypes.c_ulonglong),
                 ("kernel", ctypes.c_int), ("nparts", ctypes.c_uint)]
+
+
+class MsdParams(ctypes.Structure):
+    _fields_ = [("skip", ctypes.c_uint), ("tmax", ctypes.c_uint), ("ntimesteps", ctypes.c_uint),
+                ("primo", ctypes.c_ulonglong), ("center_of_mass", ctypes.c_int),
+                ("in_center_of_mass_frame", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -104,6 +111,10 @@ def load_library(path=None):
     L.gofr_batch_run.argtypes = [vp, ctypes.c_int, up]
     L.gofr_measure_peaks.argtypes = [ctypes.c_int, dp, dp]
     L.gofr_run_windows.argtypes = [vp, ctypes.POINTER(Params), ctypes.c_uint, up, up]
+    L.gofr_set_centres.argtypes = [vp, dp, ctypes.c_size_t, ctypes.c_uint]
+    L.gofr_msd_output_size.argtypes = [vp, ctypes.POINTER(MsdParams),
+                                       ctypes.POINTER(ctypes.c_size_t)]
+    L.gofr_msd_run.argtypes = [vp, ctypes.POINTER(MsdParams), dp]
     L.gofr_run_f64_noalloc.argtypes = [vp, vp, ctypes.c_int, vp, ctypes.c_uint, ctypes.c_size_t,
                                        ctypes.c_size_t, ctypes.POINTER(Params), vp, vp,
                                        ctypes.c_char_p, ctypes.c_size_t]
@@ -217,6 +228,24 @@ class Engine:
             self._ctx, _dp(pos), _dp(bx), BOX_TRICLINIC if triclinic else BOX_ORTHO,
             ty.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), int(ntypes), N, T))
         self.ntypes, self.natoms, self.nframes = int(ntypes), N, T
+
+    def set_centres(self, centres):
+        """Per-frame per-type centres of mass [T][ntypes][3] (for the MSD
+        centre-of-mass options)."""
+        cm = np.ascontiguousarray(centres, dtype=np.float64)
+        self._check(self.L.gofr_set_centres(self._ctx, _dp(cm), cm.shape[0], cm.shape[1]))
+
+    def msd(self, skip=1, tmax=0, ntimesteps=0, primo=0, center_of_mass=False,
+            in_center_of_mass_frame=False):
+        """MSD::calculate(primo) after reset(ntimesteps): [leff][f_cm][ntypes] f64."""
+        p = MsdParams(int(skip), int(tmax), int(ntimesteps), int(primo), int(bool(center_of_mass)),
+                      int(bool(in_center_of_mass_frame)))
+        n = ctypes.c_size_t()
+        self._check(self.L.gofr_msd_output_size(self._ctx, ctypes.byref(p), ctypes.byref(n)))
+        out = np.zeros(max(n.value, 1))
+        self._check(self.L.gofr_msd_run(self._ctx, ctypes.byref(p), _dp(out)))
+        leff = ntimesteps if (ntimesteps < tmax or tmax == 0) else tmax
+        return out[:n.value].reshape(leff, 2 if center_of_mass else 1, self.ntypes)
 
     def output_size(self, params):
         n = ctypes.c_size_t()

@@ -1,6 +1,7 @@
 // Python module `pyanalisi` of analisi_gb300: the reference's Gofrt path API
-// (pyanalisi/src/pyanalisi.cpp:67-82 for Gofrt, :487-532 for Trajectory and
-// BoxFormat) with the GB300 engine behind it.
+// (pyanalisi/src/pyanalisi.cpp:67-82 for Gofrt, :124-152 for
+// MeanSquareDisplacement, :487-532 for Trajectory and BoxFormat) with the
+// GB300 engine behind it.
 //
 //   import pyanalisi        # analisi_gb300/_build on sys.path
 //   t = pyanalisi.Trajectory(pos, vel, types, box, pyanalisi.BoxFormat.CellVectors, False, False)
@@ -17,12 +18,14 @@
 
 #include "gofrt.h"
 #include "lammps_file.h"
+#include "msd.h"
 #include "trajectory.h"
 
 namespace py = pybind11;
 using analisi_gb300::BoxFormat;
 using analisi_gb300::Trajectory;
 using GofrtT = analisi_gb300::Gofrt<double, Trajectory>;
+using MsdT = analisi_gb300::MeanSquareDisplacement<Trajectory>;
 
 namespace {
 
@@ -140,6 +143,9 @@ save rotation matrix if triclinic format is used and a rotation is needed)doc")
             if (r.empty()) return py::array_t<double>();
             return copy3(r.data(), t.get_ntimesteps(), 3, 3);
         })
+        .def("get_centres_copy", [](Trajectory &t) {
+            return copy3(t.centres_data(), t.get_ntimesteps(), t.get_ntypes(), 3);
+        }, "per-frame, per-type centres of mass (the reference's positions_cm)")
         .def("get_type", &Trajectory::get_type, "get the type used for the internal representation")
         .def("get_type_ids", [](Trajectory &t) {
             py::array_t<int> out(t.get_natoms());
@@ -195,6 +201,45 @@ time skip, every time, debug flag)doc")
                                    py::format_descriptor<double>::format(), g.get_shape().size(),
                                    g.get_shape(), g.get_stride());
         });
+
+    py::class_<MsdT>(m, "MeanSquareDisplacement", py::buffer_protocol())
+        .def(py::init<Trajectory *, unsigned int, unsigned int, unsigned int, bool, bool, bool>(),
+             py::arg("trajectory"), py::arg("skip") = 1, py::arg("tmax") = 0,
+             py::arg("nthreads") = 0, py::arg("center_of_mass") = false,
+             py::arg("in_center_of_mass_frame") = false, py::arg("debug") = false,
+             py::keep_alive<1, 2>(),
+             R"doc(mean square displacement on the GPU
+
+Parameters
+----------
+Trajectory instance
+time skip for the average computation
+max time
+number of threads (no effect: the GPU computes every lag)
+calculate center of mass MSD
+calculate for each atomic specie the atomic msd in the center of mass reference system of that specie
+debug flag)doc")
+        .def("reset", &MsdT::reset)
+        .def("getNumberOfExtraTimestepsNeeded", &MsdT::nExtraTimesteps)
+        .def("calculate", [](MsdT &m, size_t primo) {
+            py::gil_scoped_release release;
+            m.calculate(primo);
+        })
+        .def("last_stats", [](MsdT &m) {
+            gofr_stats s = m.last_stats();
+            py::dict d;
+            d["displacements"] = s.pairs;
+            d["kernel_ms"] = s.kernel_ms;
+            d["total_ms"] = s.total_ms;
+            return d;
+        })
+        .def_buffer([](MsdT &m) -> py::buffer_info {
+            return py::buffer_info(m.access_vdata(), sizeof(double),
+                                   py::format_descriptor<double>::format(), m.get_shape().size(),
+                                   m.get_shape(), m.get_stride());
+        })
+        .def("__enter__", [](MsdT &m) -> MsdT & { return m; }, py::return_value_policy::reference)
+        .def("__exit__", [](MsdT &, py::object, py::object, py::object) {});
 
     m.def("read_lammps_binary", [](const std::string &path) {
         analisi_gb300::LammpsFrames f = analisi_gb300::read_lammps_binary(path);

@@ -253,6 +253,25 @@ Trajectory::Trajectory(const double *positions, const double *velocities, const 
     type_ids_.resize(natoms);
     for (size_t a = 0; a < natoms; ++a)
         type_ids_[a] = static_cast<int>(idmap[static_cast<unsigned>(types[a])]);
+    // Per-frame, per-type centres of mass of the caller's positions (before
+    // any rotation or wrapping), running mean over the atoms of each type in
+    // atom order, as lib/src/trajectory_numpy.cpp:182,201-222.
+    {
+        const size_t nt = types_sorted_.size();
+        centres_.assign(nframes * nt * 3, 0.0);
+        std::vector<int> cont(nt);
+        for (size_t t = 0; t < nframes; ++t) {
+            std::fill(cont.begin(), cont.end(), 0);
+            for (size_t a = 0; a < natoms; ++a) {
+                const int k = type_ids_[a];
+                cont[k]++;
+                for (int c = 0; c < 3; ++c) {
+                    double &m = centres_[(t * nt + k) * 3 + c];
+                    m += (positions[(t * natoms + a) * 3 + c] - m) / double(cont[k]);
+                }
+            }
+        }
+    }
     if (wrap_pbc)
         for (size_t t = 0; t < nframes; ++t) wrap_frame(t);
     static uint64_t counter = 0;

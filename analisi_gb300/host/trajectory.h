@@ -63,6 +63,8 @@ public:
         return positions_.data() + (t * natoms_ + atom) * 3;
     }
     const int *type_ids() const { return type_ids_.data(); }
+    // [T][ntypes][3] centres of mass of each type (the reference's positions_cm)
+    const double *centres_data() const { return centres_.data(); }
     // [nframes][3][3] rotation applied to positions (only for non-diagonal
     // cell vectors with save_rotation_matrix), else empty.
     const std::vector<double> &rotation_matrix() const { return rotation_; }
@@ -79,7 +81,7 @@ private:
 
     size_t nframes_ = 0, natoms_ = 0, box_stride_ = 6;
     bool triclinic_ = false, wrap_ = false;
-    std::vector<double> positions_, velocities_, boxes_, rotation_;
+    std::vector<double> positions_, velocities_, boxes_, rotation_, centres_;
     std::vector<int> type_ids_;
     std::vector<unsigned int> types_sorted_;
     uint64_t version_ = 0;

@@ -237,6 +237,46 @@ int gofr_batch_output_layout(const gofr_ctx *ctx, unsigned k, size_t *offset, si
  * [leff][nch][nbin] counts (gofr_batch_output_layout gives the offsets). */
 int gofr_batch_run(gofr_ctx *ctx, int use_graph, unsigned long long *counts_host);
 
+/* ------------------------------------------------------------------------
+ * Mean square displacement on the resident frames (the reference's
+ * MSD<T>, lib/include/msd.h:25-58, lib/src/msd.cpp:24-118).
+ * ------------------------------------------------------------------------ */
+
+/* MSD(t, skip, tmax, nthreads, calcola_msd_centro_di_massa,
+ * calcola_msd_nel_sistema_del_centro_di_massa, debug) + reset(ntimesteps) +
+ * calculate(primo). */
+typedef struct gofr_msd_params {
+    unsigned skip;                 /* origin stride (0 means 1) */
+    unsigned tmax;                 /* lmax: lags 0..leff-1, leff = min(ntimesteps, tmax) (0: ntimesteps) */
+    unsigned ntimesteps;           /* reset(n): origins primo + k skip, k skip < n */
+    unsigned long long primo;      /* calculate(primo) */
+    int center_of_mass;            /* also the MSD of each type's centre of mass (f_cm = 2) */
+    int in_center_of_mass_frame;   /* atomic displacements minus their type's centre-of-mass
+                                      displacement */
+} gofr_msd_params;
+
+/* Per-frame, per-type centres of mass [nframes][ntypes][3] FP64 as the
+ * reference's Trajectory_numpy::calc_cm_pos_vel computes them
+ * (lib/src/trajectory_numpy.cpp:201-222: running mean over the atoms of each
+ * type of the caller's positions); needed only for the two centre-of-mass
+ * options.  nframes and ntypes must match the uploaded frames. */
+int gofr_set_centres(gofr_ctx *ctx, const double *centres, size_t nframes, unsigned ntypes);
+
+/* Number of doubles of the MSD result: leff * (center_of_mass ? 2 : 1) * ntypes. */
+int gofr_msd_output_size(const gofr_ctx *ctx, const gofr_msd_params *p, size_t *n);
+
+/* Runs MSD::calculate(primo) on the resident frames (positions as they are,
+ * no minimum image, like the reference's positions<false>) and writes the
+ * result [leff][f_cm][ntypes] to out_host (double).  Element (t, 0, k) is the
+ * mean over origins and atoms of type k of |x(o) - x(o+t)|^2 (optionally
+ * minus the type's centre-of-mass displacement); (t, 1, k) the mean over
+ * origins of the centre-of-mass |cm_k(o) - cm_k(o+t)|^2.  Each squared
+ * displacement is the reference's FP64 value; the means are FP64 sums in a
+ * fixed order divided by the count, where the reference keeps a running mean:
+ * the two agree to rounding (relative ~1e-13 for 1e7 terms).  Errors as
+ * lib/src/msd.cpp:57-68 (GOFR_ERR_RANGE: trajectory too short). */
+int gofr_msd_run(gofr_ctx *ctx, const gofr_msd_params *p, double *out_host);
+
 #ifdef __cplusplus
 }
 #endif

@@ -24,6 +24,8 @@
  *   lib/include/basetrajectory.h:94-105   lammps_to_internal
  *   lib/include/basetrajectory.h:145-161  pbc_wrap
  *   lib/include/calculatemultithread.h:50-78,80-104,106-162  split + loops
+ *   lib/src/msd.cpp:37-118            MSD reset / calc_init / calc_single_th
+ *   lib/src/trajectory_numpy.cpp:201-222  calc_cm_pos_vel  (centres of mass)
  */
 #include <math.h>
 #include <stdint.h>
@@ -249,4 +251,85 @@ void oracle_fold_buffer(const uint64_t *counts, size_t data_length, unsigned nth
         }
         out[i] = acc;
     }
+}
+
+/*
+ * Per-frame, per-type centres of mass: running mean over the atoms of each
+ * type, in atom order, of the given positions (Trajectory_numpy::calc_cm_pos_vel,
+ * lib/src/trajectory_numpy.cpp:201-222).  cm: [T][ntypes][3].
+ */
+void oracle_centres(const double *pos, const int *type_ids, unsigned ntypes, size_t natoms,
+                    size_t nframes, double *cm)
+{
+    unsigned *cont = (unsigned *)calloc(ntypes ? ntypes : 1, sizeof(unsigned));
+    for (size_t f = 0; f < nframes; ++f) {
+        for (unsigned k = 0; k < ntypes; ++k) {
+            cont[k] = 0;
+            for (int c = 0; c < 3; ++c) cm[(f * ntypes + k) * 3 + c] = 0.0;
+        }
+        for (size_t a = 0; a < natoms; ++a) {
+            const unsigned k = (unsigned)type_ids[a];
+            cont[k]++;
+            for (int c = 0; c < 3; ++c) {
+                double *m = &cm[(f * ntypes + k) * 3 + c];
+                *m += (pos[(f * natoms + a) * 3 + c] - *m) / (double)cont[k];
+            }
+        }
+    }
+    free(cont);
+}
+
+/*
+ * MSD<T>::calc_single_th for every lag (lib/src/msd.cpp:70-118): per lag t and
+ * type, the running mean over origins imedia = 0, skip, ... < ntimesteps and
+ * atoms (in that order) of pow(dx,2)+pow(dy,2)+pow(dz,2), dx = x(primo+imedia)
+ * - x(primo+imedia+t) [- (cm(o) - cm(o+t)) with cm_self]; with cm_msd also the
+ * running mean over origins of the centres' own squared displacement.  The
+ * reference splits lags over threads (PARALLEL_SPLIT_TIME); each lag's value
+ * does not depend on that split.  out: [leff][f_cm][ntypes].  Returns -1 when
+ * leff + ntimesteps + primo > nframes (msd.cpp:57-60).
+ */
+int oracle_msd(const double *pos, const double *cm, const int *type_ids, unsigned ntypes,
+               size_t natoms, size_t nframes, unsigned skip, unsigned tmax, unsigned ntimesteps,
+               size_t primo, int cm_msd, int cm_self, double *out)
+{
+    const size_t leff = (ntimesteps < tmax || tmax == 0) ? ntimesteps : tmax;
+    const size_t f_cm = cm_msd ? 2 : 1;
+    if (skip == 0) skip = 1;
+    if (leff + ntimesteps + primo > nframes) return -1;
+    uint64_t *cont = (uint64_t *)calloc(ntypes * f_cm + 1, sizeof(uint64_t));
+    for (size_t t = 0; t < leff; ++t) {
+        double *v = out + t * ntypes * f_cm;
+        for (size_t i = 0; i < ntypes * f_cm; ++i) {
+            v[i] = 0.0;
+            cont[i] = 0;
+        }
+        for (size_t im = 0; im < ntimesteps; im += skip) {
+            const size_t fo = primo + im, fl = primo + im + t;
+            for (size_t a = 0; a < natoms; ++a) {
+                const unsigned k = (unsigned)type_ids[a];
+                const double *xo = pos + (fo * natoms + a) * 3;
+                const double *xl = pos + (fl * natoms + a) * 3;
+                double d[3];
+                for (int c = 0; c < 3; ++c) {
+                    d[c] = xo[c] - xl[c];
+                    if (cm_self)
+                        d[c] = d[c] - (cm[(fo * ntypes + k) * 3 + c] - cm[(fl * ntypes + k) * 3 + c]);
+                }
+                const double delta = (pow(d[0], 2) + pow(d[1], 2) + pow(d[2], 2)) - v[k];
+                v[k] += delta / (double)(++cont[k]);
+            }
+            if (cm_msd) {
+                for (unsigned k = 0; k < ntypes; ++k) {
+                    const double *co = cm + (fo * ntypes + k) * 3;
+                    const double *cl = cm + (fl * ntypes + k) * 3;
+                    const double delta = (pow(co[0] - cl[0], 2) + pow(co[1] - cl[1], 2) +
+                                          pow(co[2] - cl[2], 2)) - v[ntypes + k];
+                    v[ntypes + k] += delta / (double)(++cont[ntypes + k]);
+                }
+            }
+        }
+    }
+    free(cont);
+    return 0;
 }

@@ -64,6 +64,12 @@ def lib():
         L.oracle_incr.restype = ctypes.c_double
         L.oracle_fold_buffer.argtypes = [up, ctypes.c_size_t, ctypes.c_uint, ctypes.c_double, dp]
         L.oracle_fold_buffer.restype = None
+        L.oracle_centres.argtypes = [dp, ip, ctypes.c_uint, ctypes.c_size_t, ctypes.c_size_t, dp]
+        L.oracle_centres.restype = None
+        L.oracle_msd.argtypes = [dp, dp, ip, ctypes.c_uint, ctypes.c_size_t, ctypes.c_size_t,
+                                 ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.c_size_t,
+                                 ctypes.c_int, ctypes.c_int, dp]
+        L.oracle_msd.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -129,6 +135,40 @@ def gofrt_counts(pos, boxes, type_ids, ntypes, rmin, rmax, nbin, tmax, nthreads,
     if rc != 0:
         raise MemoryError("oracle allocation failed")
     return out if per_thread else out.sum(axis=0)
+
+
+def centres(pos, type_ids, ntypes):
+    """Per-frame per-type centres of mass [T][ntypes][3] (running mean over the
+    atoms of each type, as the reference's calc_cm_pos_vel)."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    type_ids = np.ascontiguousarray(type_ids, dtype=np.int32)
+    T, N = pos.shape[0], pos.shape[1]
+    cm = np.zeros((T, ntypes, 3))
+    lib().oracle_centres(_dp(pos), type_ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                         int(ntypes), N, T, _dp(cm))
+    return cm
+
+
+def msd(pos, type_ids, ntypes, skip, tmax, ntimesteps, primo, cm_msd=False, cm_self=False,
+        cm=None):
+    """The reference MSD::calculate result [leff][f_cm][ntypes] (running means)."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    type_ids = np.ascontiguousarray(type_ids, dtype=np.int32)
+    T, N = pos.shape[0], pos.shape[1]
+    if cm is None:
+        cm = centres(pos, type_ids, ntypes)
+    cm = np.ascontiguousarray(cm, dtype=np.float64)
+    leff = ntimesteps if (ntimesteps < tmax or tmax == 0) else tmax
+    fcm = 2 if cm_msd else 1
+    out = np.zeros((leff, fcm, ntypes))
+    rc = lib().oracle_msd(_dp(pos), _dp(cm), type_ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                          int(ntypes), N, T, int(skip), int(tmax), int(ntimesteps), int(primo),
+                          int(bool(cm_msd)), int(bool(cm_self)), _dp(out))
+    if rc == -1:
+        raise RuntimeError("trajectory is too short for this kind of calculation. Select a "
+                           "different starting timestep or lower the size of the average or "
+                           "the lenght of the time lag")
+    return out
 
 
 def incr(ntimesteps, skip):

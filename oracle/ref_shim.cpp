@@ -1,18 +1,19 @@
-// Reduced Python binding of the reference's own Gofrt path.
+// Reduced Python binding of the reference's own Gofrt path (and its MSD).
 //
 // TEST INFRASTRUCTURE ONLY.  This file is compiled together with the
-// reference's unmodified sources lib/src/gofrt.cpp, lib/src/basetrajectory.cpp
-// and lib/src/trajectory_numpy.cpp (see oracle/build_ref.sh) into
-// oracle/_ref/pyanalisi_ref*.so.  It exposes exactly the three classes the
-// Gofrt path needs, with the constructor and method signatures of the full
-// reference binding (pyanalisi/src/pyanalisi.cpp:67-82 for Gofrt,
-// :487-527 for Trajectory, :528-532 for BoxFormat), so that fixtures can be
-// generated by the reference itself and the C restatement in
-// oracle/gofr_oracle.c can be pinned against it.
+// reference's unmodified sources lib/src/gofrt.cpp, lib/src/msd.cpp,
+// lib/src/basetrajectory.cpp and lib/src/trajectory_numpy.cpp (see
+// oracle/build_ref.sh) into oracle/_ref/pyanalisi_ref*.so.  It exposes the
+// classes these paths need, with the constructor and method signatures of the
+// full reference binding (pyanalisi/src/pyanalisi.cpp:67-82 for Gofrt,
+// :124-152 for MeanSquareDisplacement, :487-527 for Trajectory, :528-532 for
+// BoxFormat), so that fixtures can be generated by the reference itself and
+// the C restatement in oracle/gofr_oracle.c can be pinned against it.
 #include <pybind11/pybind11.h>
 #include <pybind11/numpy.h>
 #include "trajectory_numpy.h"
 #include "gofrt.h"
+#include "msd.h"
 
 namespace py = pybind11;
 
@@ -36,6 +37,10 @@ PYBIND11_MODULE(pyanalisi_ref, m) {
             size_t nt = t.get_ntimesteps(), st = t.get_box_stride();
             return py::array_t<double>({nt, st}, t.box<false>(0));
         })
+        .def("internal_centres", [](Trajectory_numpy &t) {
+            size_t nt = t.get_ntimesteps(), ny = t.get_ntypes();
+            return py::array_t<double>({nt, ny, (size_t)3}, t.positions_cm<false>(0, 0));
+        })
         .def("internal_type_ids", [](Trajectory_numpy &t) {
             size_t na = t.get_natoms();
             py::array_t<int> a(na);
@@ -55,6 +60,18 @@ PYBIND11_MODULE(pyanalisi_ref, m) {
         .def("calculate", &G::calculate)
         .def("get_columns_description", &G::get_columns_description)
         .def_buffer([](G &g) -> py::buffer_info {
+            return py::buffer_info(g.access_vdata(), sizeof(double),
+                                   py::format_descriptor<double>::format(),
+                                   g.get_shape().size(), g.get_shape(), g.get_stride());
+        });
+    using MSDT = MSD<Trajectory_numpy>;
+    py::class_<MSDT>(m, "MeanSquareDisplacement", py::buffer_protocol())
+        .def(py::init<Trajectory_numpy *, unsigned int, unsigned int, unsigned int, bool, bool,
+                      bool>())
+        .def("reset", &MSDT::reset)
+        .def("getNumberOfExtraTimestepsNeeded", &MSDT::nExtraTimesteps)
+        .def("calculate", &MSDT::calculate)
+        .def_buffer([](MSDT &g) -> py::buffer_info {
             return py::buffer_info(g.access_vdata(), sizeof(double),
                                    py::format_descriptor<double>::format(),
                                    g.get_shape().size(), g.get_shape(), g.get_stride());

@@ -22,3 +22,17 @@ def load(name):
 def incr(meta):
     n, skip = meta["ntimesteps"], meta["skip"] or 1
     return 1.0 / (n // skip) if n // skip > 0 else 1.0
+
+
+GOLDEN_MSD = os.path.join(GOLDEN, "msd")
+
+
+def msd_names():
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN_MSD, "*.npz")))
+
+
+def load_msd(name):
+    z = np.load(os.path.join(GOLDEN_MSD, name + ".npz"))
+    d = {k: z[k] for k in z.files if k != "meta"}
+    d["meta"] = json.loads(str(z["meta"]))
+    return d

@@ -72,3 +72,16 @@ def test_argument_errors_match_reference(pa, bad, msg):
         vel = np.zeros((3, 4, 3))
     with pytest.raises(RuntimeError, match=msg.replace("(", r"\(").replace(")", r"\)")):
         pa.Trajectory(pos, vel, types, box, pa.BoxFormat.LammpsOrtho, False, False)
+
+
+@pytest.mark.parametrize("name", gu.msd_names())
+def test_centres_of_mass_match_reference(pa, name):
+    """Per-type centres of mass, from the caller's positions before wrapping or
+    rotation, bit for bit (the reference's positions_cm)."""
+    g = gu.load_msd(name)
+    m = g["meta"]
+    t = pa.Trajectory(g["positions"], np.zeros_like(g["positions"]), g["types"], g["box"],
+                      getattr(pa.BoxFormat, m["box_format"]), m["wrap"], False)
+    assert np.array_equal(t.get_positions_copy(), g["internal_positions"])
+    assert np.array_equal(t.get_type_ids(), g["internal_type_ids"])
+    assert np.array_equal(t.get_centres_copy(), g["internal_centres"])
