@@ -333,6 +333,42 @@ def bench_allpairs(eng, prm, args, flush, steps=2):
             "kernel": "k_pairs_f32 (all pairs)"}
 
 
+def bench_msd(eng, w, p, reps=3):
+    """MeanSquareDisplacement on the same resident 16k-atom frames, the job of
+    the g(r,t) headline (reset(1800), tmax=200, skip=4: 450 origins x 200 lags
+    x 16384 atoms = 1.47e9 squared displacements), both centre-of-mass options
+    on; checked against the oracle's running means on a sub-sample, and the
+    oracle (one thread) timed on a bounded sample of the same job."""
+    import numpy as np
+    from oracle import oracle
+    N = w["positions"].shape[1]
+    nt = w["ntypes"]
+    cm = oracle.centres(w["positions"], w["type_ids"], nt)
+    eng.set_centres(cm)
+    eng.msd(p["skip"], p["tmax"], 1800, 0, True, True)
+    ms = []
+    for _ in range(reps):
+        eng.msd(p["skip"], p["tmax"], 1800, 0, True, True)
+        ms.append(eng.stats()["kernel_ms"])
+    disp = 200 * 450 * N
+    rate = disp / (sum(ms) / len(ms)) / 1e6
+    # sub-sample check: 20 lags x 10 origins
+    sub_gpu = eng.msd(p["skip"], 20, 40, 0, True, True)
+    t0 = time.perf_counter()
+    sub_ref = oracle.msd(w["positions"], w["type_ids"], nt, p["skip"], 20, 40, 0, True, True,
+                         cm=cm)
+    dt = time.perf_counter() - t0
+    rel = float(np.max(np.abs(sub_gpu - sub_ref) / np.maximum(np.abs(sub_ref), 1e-300)))
+    cpu_rate = 20 * 10 * N / dt / 1e9
+    return {"workload": "c2 frames: reset(1800), tmax=200, skip=4, both centre-of-mass options",
+            "displacements": disp, "ms": round(sum(ms) / len(ms), 3),
+            "value": round(rate, 2), "unit": "G squared displacements/s",
+            "fp64_ops_per_displacement": 12,
+            "max_rel_diff_vs_oracle_sample": rel,
+            "cpu_oracle_1thread": {"value": round(cpu_rate, 4), "unit": "G squared displacements/s",
+                                   "sample": "20 lags x 10 origins", "seconds": round(dt, 3)}}
+
+
 def bench_cells(engine, workloads, device):
     """131072 atoms, 4 types, 250 bins on [0,10]: the cell-list kernel on a sample
     (10 origins x 50 lags), its counts checked against the all-pairs FP32 kernel on
@@ -507,6 +543,7 @@ def run_gpu(args):
     clocks = clk.summary(local)
     extra = {}
     if not args.no_extra:
+        extra["msd"] = bench_msd(eng, w, p)
         del w
         if kernel_used != 1:
             extra["allpairs_f32"] = bench_allpairs(eng, prm, args, flush)
