@@ -65,7 +65,7 @@ struct TrajDev {
     unsigned *d_sidt = nullptr;
     float *d_spos = nullptr;
     // MSD: atoms sorted by type, type starts, optional centres of mass
-    std::vector<int> h_perm, h_tbegin;
+    std::vector<int> h_perm, h_tbegin, h_types;
     int *d_perm = nullptr, *d_tbegin = nullptr;
     double *d_cm = nullptr;          // [T][ntypes][3]
 };
@@ -88,6 +88,11 @@ struct gofr_ctx {
     unsigned long long *d_stats = nullptr;
     double *d_msd_partial = nullptr, *d_msd_out = nullptr;
     size_t cap_msd_partial = 0, cap_msd_out = 0;
+    // neighbour lists
+    unsigned long long *d_nl_list = nullptr, *d_nl_meta = nullptr;
+    double *d_nl_rpos = nullptr, *d_nl_cut2 = nullptr;
+    int *d_nl_full = nullptr;
+    size_t cap_nl_list = 0, cap_nl_meta = 0, cap_nl_rpos = 0, cap_nl_cut2 = 0, cap_nl_full = 0;
     double *d_minmax = nullptr;
     unsigned *d_nonfinite = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -523,6 +528,7 @@ int upload_traj(gofr_ctx *ctx, TrajDev &t, const double *positions, const double
                        ctx->stream));
     CK(cudaMemcpyAsync(t.types, type_ids, natoms * sizeof(int), cudaMemcpyHostToDevice,
                        ctx->stream));
+    t.h_types.assign(type_ids, type_ids + natoms);
     // atoms sorted by type (stable), for the per-type sums of the MSD
     t.h_tbegin.assign(ntypes + 1, 0);
     for (size_t a = 0; a < natoms; ++a) t.h_tbegin[type_ids[a] + 1]++;
@@ -1419,6 +1425,11 @@ void gofr_ctx_destroy(gofr_ctx *ctx)
         cudaFree(ctx->d_nonfinite);
         cudaFree(ctx->d_msd_partial);
         cudaFree(ctx->d_msd_out);
+        cudaFree(ctx->d_nl_list);
+        cudaFree(ctx->d_nl_meta);
+        cudaFree(ctx->d_nl_rpos);
+        cudaFree(ctx->d_nl_cut2);
+        cudaFree(ctx->d_nl_full);
         for (auto &e : ctx->ev)
             if (e) cudaEventDestroy(e);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1902,6 +1913,143 @@ int gofr_msd_run(gofr_ctx *ctx, const gofr_msd_params *p, double *out_host)
     ctx->stats.evaluated = ctx->stats.pairs;
     ctx->stats.kernel_used = -1;
     return gofr_sync(ctx);
+}
+
+int gofr_neigh_layout(const gofr_ctx *ctx_c, const gofr_neigh_spec *spec, unsigned nspec,
+                      size_t *list_len, size_t *rpos_len)
+{
+    gofr_ctx *ctx = const_cast<gofr_ctx *>(ctx_c);
+    if (!ctx || !list_len || !rpos_len || (nspec && !spec)) return GOFR_ERR_ARG;
+    if (ctx->trajs.size() != 1) return fail(ctx, GOFR_ERR_STATE, "no frames uploaded");
+    const TrajDev &t = ctx->trajs[0];
+    if (nspec != t.ntypes)
+        return fail(ctx, GOFR_ERR_ARG,
+                    "In neighbours list you must specify parameters for each atomic type");
+    unsigned long long tot = 0;
+    for (unsigned k = 0; k < nspec; ++k) tot += spec[k].nneigh;
+    *list_len = t.N * (size_t)(tot + nspec);
+    *rpos_len = t.N * (size_t)4 * tot;
+    return GOFR_OK;
+}
+
+// Neighbours::update_neigh(timestep, sort) (lib/src/neighbour.cpp:9-79).
+int gofr_neigh_run(gofr_ctx *ctx, const gofr_neigh_spec *spec, unsigned nspec, size_t timestep,
+                   int sort, unsigned long long *list_host, double *rpos_host)
+{
+    size_t list_len = 0, rpos_len = 0;
+    int rc = gofr_neigh_layout(ctx, spec, nspec, &list_len, &rpos_len);
+    if (rc) return rc;
+    const TrajDev &t = ctx->trajs[0];
+    if (timestep >= t.T)
+        return fail(ctx, GOFR_ERR_ARG, "timestep %zu outside the %zu frames", timestep, t.T);
+    if (nspec > (unsigned)NEIGH_MAXT)
+        return fail(ctx, GOFR_ERR_UNSUPPORTED, "neighbour lists support at most %d types",
+                    NEIGH_MAXT);
+    if (t.N > (size_t)INT32_MAX / 2) return fail(ctx, GOFR_ERR_UNSUPPORTED, "too many atoms");
+    if ((list_len && !list_host) || (rpos_len && !rpos_host))
+        return fail(ctx, GOFR_ERR_ARG, "null output");
+    DevGuard g(ctx->device);
+    // meta: nneigh[nt], loff[nt], roff[nt], flags (u32 in a u64), first_err
+    const unsigned nt = nspec;
+    std::vector<unsigned long long> meta(3 * nt + 2, 0ull);
+    std::vector<double> cut2(nt);
+    unsigned long long lo = 0, ro = 0;
+    for (unsigned k = 0; k < nt; ++k) {
+        meta[k] = spec[k].nneigh;
+        meta[nt + k] = lo;
+        meta[2 * nt + k] = ro;
+        lo += (spec[k].nneigh + 1) * (unsigned long long)t.N;
+        ro += spec[k].nneigh * (unsigned long long)t.N * 4;
+        cut2[k] = spec[k].cut2;
+    }
+    meta[3 * nt + 1] = ~0ull;
+    rc = ensure(ctx, ctx->d_nl_meta, ctx->cap_nl_meta, meta.size());
+    if (!rc) rc = ensure(ctx, ctx->d_nl_cut2, ctx->cap_nl_cut2, std::max<size_t>(nt, 1));
+    if (!rc) rc = ensure(ctx, ctx->d_nl_list, ctx->cap_nl_list, std::max<size_t>(list_len, 1));
+    if (!rc) rc = ensure(ctx, ctx->d_nl_rpos, ctx->cap_nl_rpos, std::max<size_t>(rpos_len, 1));
+    if (!rc) rc = ensure(ctx, ctx->d_nl_full, ctx->cap_nl_full, std::max<size_t>(t.N * nt, 1));
+    if (rc) return rc;
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_nl_meta, meta.data(), meta.size() * 8, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_nl_cut2, cut2.data(), nt * sizeof(double), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    if (list_len) CK(cudaMemsetAsync(ctx->d_nl_list, 0, list_len * 8, ctx->stream));
+    if (rpos_len) CK(cudaMemsetAsync(ctx->d_nl_rpos, 0, rpos_len * 8, ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), ctx->stream));
+    CK(cudaMemsetAsync(ctx->d_stats, 0, ST_COUNT * sizeof(unsigned long long), ctx->stream));
+    NeighLaunch L{};
+    L.pos64 = t.pos64;
+    L.box64 = t.box64;
+    L.types = t.types;
+    L.nneigh = ctx->d_nl_meta;
+    L.loff = ctx->d_nl_meta + nt;
+    L.roff = ctx->d_nl_meta + 2 * nt;
+    L.cut2 = ctx->d_nl_cut2;
+    L.list = ctx->d_nl_list;
+    L.rpos = ctx->d_nl_rpos;
+    L.full = ctx->d_nl_full;
+    L.flags = reinterpret_cast<unsigned *>(ctx->d_nl_meta + 3 * nt);
+    L.first_err = ctx->d_nl_meta + 3 * nt + 1;
+    L.err = ctx->d_err;
+    L.N = (int)t.N;
+    L.ntypes = (int)nt;
+    L.timestep = (long long)timestep;
+    L.tric = t.tric;
+    std::memset(&ctx->stats, 0, sizeof ctx->stats);
+    CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+    ++ctx->launches;
+    if (launch_neigh_build(L, ctx->num_sms, ctx->stream))
+        return fail(ctx, GOFR_ERR_CUDA, "neighbour-list kernel launch failed: %s",
+                    cudaGetErrorString(cudaGetLastError()));
+    unsigned long long tail[2] = {0ull, 0ull};
+    CK(cudaMemcpyAsync(tail, ctx->d_nl_meta + 3 * nt, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (tail[0] & 1ull) {  // some list is full: look for the reference's overflow
+        ++ctx->launches;
+        if (launch_neigh_check(L, ctx->num_sms, ctx->stream))
+            return fail(ctx, GOFR_ERR_CUDA, "neighbour-list check launch failed: %s",
+                        cudaGetErrorString(cudaGetLastError()));
+        CK(cudaMemcpyAsync(tail, ctx->d_nl_meta + 3 * nt, 16, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
+    const bool overflow = tail[1] != ~0ull;
+    if (!overflow && sort) {
+        ++ctx->launches;
+        if (launch_neigh_sort(L, ctx->num_sms, ctx->stream))
+            return fail(ctx, GOFR_ERR_CUDA, "neighbour-list sort launch failed: %s",
+                        cudaGetErrorString(cudaGetLastError()));
+    }
+    CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+    if (list_len)
+        CK(cudaMemcpyAsync(list_host, ctx->d_nl_list, list_len * 8, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+    if (rpos_len)
+        CK(cudaMemcpyAsync(rpos_host, ctx->d_nl_rpos, rpos_len * 8, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+    CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+    ctx->stats.pairs = (unsigned long long)t.N * t.N;
+    ctx->stats.evaluated = ctx->stats.pairs;
+    ctx->stats.kernel_used = -1;
+    rc = gofr_sync(ctx);
+    if (rc) return rc;
+    if (overflow) {
+        // the reference's message: sizes of the two lists when the pair came
+        const unsigned long long i = tail[1] / t.N, j = tail[1] % t.N;
+        const unsigned ti = (unsigned)t.h_types[i], tj = (unsigned)t.h_types[j];
+        auto before = [&](unsigned long long a, unsigned k, unsigned long long lim) {
+            const unsigned long long *l = list_host + meta[nt + k] + a * (spec[k].nneigh + 1);
+            unsigned long long n = 0;
+            for (unsigned long long q = 0; q < l[0]; ++q) n += l[1 + q] < lim ? 1 : 0;
+            return n;
+        };
+        return fail(ctx, GOFR_ERR_NEIGH_FULL,
+                    "Too many neighbours in shell! (iatom=%llu jatom=%llu ni=%llu nj=%llu "
+                    "itype=%u jtype=%u)",
+                    i, j, before(i, tj, j), before(j, ti, i), ti, tj);
+    }
+    return GOFR_OK;
 }
 
 }  // extern "C"

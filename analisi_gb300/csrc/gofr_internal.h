@@ -93,6 +93,29 @@ struct MsdLaunch {
 };
 int launch_msd(const MsdLaunch &M, double *out_device, int num_sms, cudaStream_t s);
 
+// Neighbour lists (gofr_neigh.cu)
+constexpr int NEIGH_MAXT = 32;
+struct NeighLaunch {
+    const double *pos64;                  // [T][N][3]
+    const double *box64;                  // [T][9] internal boxes
+    const int *types;                     // [N] dense type ids
+    const unsigned long long *nneigh;     // [ntypes] list capacities
+    const unsigned long long *loff, *roff;  // [ntypes] offsets in list / rpos
+    const double *cut2;                   // [ntypes] cutoffs^2
+    unsigned long long *list;             // the reference's list array
+    double *rpos;                         // the reference's rpos array
+    int *full;                            // [N][ntypes] neighbour that filled a list (N: not full)
+    unsigned *flags;                      // bit 0: some list is full
+    unsigned long long *first_err;        // min i*N + j over overflowing pairs
+    unsigned *err;                        // error word (minimum-image iteration cap)
+    int N, ntypes;
+    long long timestep;
+    int tric;
+};
+int launch_neigh_build(const NeighLaunch &L, int num_sms, cudaStream_t s);
+int launch_neigh_check(const NeighLaunch &L, int num_sms, cudaStream_t s);
+int launch_neigh_sort(const NeighLaunch &L, int num_sms, cudaStream_t s);
+
 int launch_cell_build(const double *pos64, const unsigned char *types8, size_t T, size_t N,
                       const double *box_internal, const double *centre, const int *nc,
                       int *cell_of, int *rank_of, int *count, int *start, float *spos,

@@ -1,0 +1,197 @@
+// Neighbour lists of one resident frame (the reference's
+// Neighbours<T,double>::update_neigh, lib/src/neighbour.cpp:9-79).
+//
+// The reference visits the pairs i < j once and appends each pair within
+// either type's cutoff to both atoms' lists, so every list ends up in
+// ascending neighbour index.  Here one warp builds one atom's lists: its lanes
+// take 32 consecutive candidates at a time, compute the reference's FP64
+// minimum-image vector for the ordered pair (lower index first, negated for
+// the higher-index atom, as the reference stores -x), and the counted entries
+// of each neighbour type are placed by a ballot prefix, which keeps the
+// ascending order.  Overflow follows the reference's rule exactly: a pair
+// (i < j) within either cutoff is an error when, at that point of the
+// reference's loop, i's list of j's type or j's list of i's type is full;
+// with full[a][k] = the neighbour index that filled a's list of type k, that
+// is full[i][t_j] < j or full[j][t_i] < i, checked by a second pass (only
+// when some list is full) that keeps the first such pair in loop order.  The
+// optional sort by distance is a stable insertion sort per list.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gofr_device.cuh"
+#include "gofr_internal.h"
+
+namespace gofr {
+namespace neigh {
+
+constexpr int NT = 256;
+constexpr int WARPS = NT / 32;
+
+// x = minimum image of x_i - x_j (i < j), d2 as the reference
+template <bool TRI>
+__device__ __forceinline__ double pair_vec(const NeighLaunch &L, const double *frame,
+                                           const double *box, int i, int j, double x[3])
+{
+    const double *pi = frame + (size_t)i * 3, *pj = frame + (size_t)j * 3;
+    x[0] = __dsub_rn(pi[0], pj[0]);
+    x[1] = __dsub_rn(pi[1], pj[1]);
+    x[2] = __dsub_rn(pi[2], pj[2]);
+    ref_min_image<TRI>(x[0], x[1], x[2], box, L.err);
+    double s = __dmul_rn(x[0], x[0]);
+    s = __dadd_rn(s, __dmul_rn(x[1], x[1]));
+    s = __dadd_rn(s, __dmul_rn(x[2], x[2]));
+    return s;
+}
+
+template <bool TRI>
+__global__ void __launch_bounds__(NT) k_neigh_build(const NeighLaunch L)
+{
+    __shared__ unsigned long long cnt[WARPS][NEIGH_MAXT];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const double *frame = L.pos64 + (size_t)L.timestep * L.N * 3;
+    const double *box = L.box64 + (size_t)L.timestep * 9;
+    const unsigned lt = (1u << lane) - 1u;
+    for (long long a0 = (long long)blockIdx.x * WARPS; a0 < L.N; a0 += (long long)gridDim.x * WARPS) {
+        const int a = (int)(a0 + w);
+        if (a >= L.N) continue;  // warp-uniform
+        const int ta = L.types[a];
+        for (int k = lane; k < L.ntypes; k += 32) {
+            cnt[w][k] = 0ull;
+            // a list of capacity 0 is full before its first neighbour
+            L.full[(size_t)a * L.ntypes + k] = L.nneigh[k] == 0 ? -1 : L.N;
+        }
+        __syncwarp();
+        for (int b0 = 0; b0 < L.N; b0 += 32) {
+            const int b = b0 + lane;
+            const bool valid = b < L.N && b != a;
+            int tb = 0;
+            double x[3] = {0.0, 0.0, 0.0}, d2 = 0.0;
+            bool counted = false;
+            if (valid) {
+                tb = L.types[b];
+                const int i = a < b ? a : b, j = a < b ? b : a;
+                d2 = pair_vec<TRI>(L, frame, box, i, j, x);
+                if (a > b) { x[0] = -x[0]; x[1] = -x[1]; x[2] = -x[2]; }
+                counted = d2 <= L.cut2[tb];
+            }
+            for (int k = 0; k < L.ntypes; ++k) {
+                const unsigned m = __ballot_sync(0xffffffffu, counted && tb == k);
+                if (!m) continue;
+                const unsigned long long base = cnt[w][k];
+                const unsigned long long nk = L.nneigh[k];
+                if (counted && tb == k) {
+                    const unsigned long long pos = base + __popc(m & lt);
+                    if (pos < nk) {
+                        L.list[L.loff[k] + (size_t)a * (nk + 1) + 1 + pos] = (unsigned long long)b;
+                        double *r = L.rpos + L.roff[k] + ((size_t)a * nk + pos) * 4;
+                        r[0] = __dsqrt_rn(d2);
+                        r[1] = x[0];
+                        r[2] = x[1];
+                        r[3] = x[2];
+                    }
+                    if (pos + 1 == nk) L.full[(size_t)a * L.ntypes + k] = b;
+                }
+                __syncwarp();
+                if (lane == 0) cnt[w][k] = base + __popc(m);
+                __syncwarp();
+            }
+        }
+        for (int k = lane; k < L.ntypes; k += 32) {
+            const unsigned long long c = cnt[w][k], nk = L.nneigh[k];
+            L.list[L.loff[k] + (size_t)a * (nk + 1)] = c < nk ? c : nk;
+            if (c >= nk) atomicOr(L.flags, 1u);  // some list is full: run the check
+        }
+        __syncwarp();
+    }
+}
+
+// first pair (i < j) in the reference's loop order that finds a full list
+template <bool TRI>
+__global__ void __launch_bounds__(NT) k_neigh_check(const NeighLaunch L)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const double *frame = L.pos64 + (size_t)L.timestep * L.N * 3;
+    const double *box = L.box64 + (size_t)L.timestep * 9;
+    for (long long a0 = (long long)blockIdx.x * WARPS; a0 < L.N; a0 += (long long)gridDim.x * WARPS) {
+        const int i = (int)(a0 + w);
+        if (i >= L.N) continue;
+        const int ti = L.types[i];
+        for (int j = i + 1 + lane; j < L.N; j += 32) {
+            const int tj = L.types[j];
+            double x[3];
+            const double d2 = pair_vec<TRI>(L, frame, box, i, j, x);
+            if (!(d2 <= L.cut2[tj] || d2 <= L.cut2[ti])) continue;
+            if (L.full[(size_t)i * L.ntypes + tj] < j || L.full[(size_t)j * L.ntypes + ti] < i)
+                atomicMin(L.first_err, (unsigned long long)i * (unsigned long long)L.N + j);
+        }
+    }
+}
+
+// stable insertion sort of every list by distance
+__global__ void k_neigh_sort(const NeighLaunch L)
+{
+    const long long n = (long long)L.N * L.ntypes;
+    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
+         g += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(g / L.N), a = (int)(g - (long long)k * L.N);
+        const unsigned long long nk = L.nneigh[k];
+        unsigned long long *l = L.list + L.loff[k] + (size_t)a * (nk + 1);
+        double *r = L.rpos + L.roff[k] + (size_t)a * nk * 4;
+        const unsigned long long cntk = l[0];
+        for (unsigned long long s = 1; s < cntk; ++s) {
+            const double e0 = r[4 * s], e1 = r[4 * s + 1], e2 = r[4 * s + 2], e3 = r[4 * s + 3];
+            const unsigned long long id = l[1 + s];
+            unsigned long long q = s;
+            while (q > 0 && e0 < r[4 * (q - 1)]) {
+                r[4 * q] = r[4 * (q - 1)];
+                r[4 * q + 1] = r[4 * (q - 1) + 1];
+                r[4 * q + 2] = r[4 * (q - 1) + 2];
+                r[4 * q + 3] = r[4 * (q - 1) + 3];
+                l[1 + q] = l[q];
+                --q;
+            }
+            r[4 * q] = e0;
+            r[4 * q + 1] = e1;
+            r[4 * q + 2] = e2;
+            r[4 * q + 3] = e3;
+            l[1 + q] = id;
+        }
+    }
+}
+
+}  // namespace neigh
+
+int launch_neigh_build(const NeighLaunch &L, int num_sms, cudaStream_t s)
+{
+    using namespace neigh;
+    long long grid = (L.N + WARPS - 1) / WARPS;
+    if (grid > (long long)num_sms * 16) grid = (long long)num_sms * 16;
+    if (grid < 1) return 0;
+    if (L.tric) k_neigh_build<true><<<(unsigned)grid, NT, 0, s>>>(L);
+    else k_neigh_build<false><<<(unsigned)grid, NT, 0, s>>>(L);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_neigh_check(const NeighLaunch &L, int num_sms, cudaStream_t s)
+{
+    using namespace neigh;
+    long long grid = (L.N + WARPS - 1) / WARPS;
+    if (grid > (long long)num_sms * 16) grid = (long long)num_sms * 16;
+    if (grid < 1) return 0;
+    if (L.tric) k_neigh_check<true><<<(unsigned)grid, NT, 0, s>>>(L);
+    else k_neigh_check<false><<<(unsigned)grid, NT, 0, s>>>(L);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_neigh_sort(const NeighLaunch &L, int num_sms, cudaStream_t s)
+{
+    using namespace neigh;
+    long long n = (long long)L.N * L.ntypes;
+    long long grid = (n + NT - 1) / NT;
+    if (grid > (long long)num_sms * 8) grid = (long long)num_sms * 8;
+    if (grid < 1) return 0;
+    k_neigh_sort<<<(unsigned)grid, NT, 0, s>>>(L);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace gofr

@@ -16,6 +16,7 @@ GOFR_OK = 0
 STATUS = {
     -1: "GOFR_ERR_ARG", -2: "GOFR_ERR_RANGE", -3: "GOFR_ERR_CUDA", -4: "GOFR_ERR_NOMEM",
     -5: "GOFR_ERR_STATE", -6: "GOFR_ERR_DEVICE", -7: "GOFR_ERR_UNSUPPORTED",
+    -8: "GOFR_ERR_NEIGH_FULL",
 }
 BOX_ORTHO, BOX_TRICLINIC = 0, 1
 KERNELS = {"auto": 0, "f32": 1, "f64": 2, "cell": 3, "tuned": 4}
@@ -27,8 +28,47 @@ EXPORTED = [
     "gofr_counts_to_buffer", "gofr_bin_thresholds", "gofr_batch_set",
     "gofr_batch_output_layout", "gofr_batch_run", "gofr_measure_peaks",
     "gofr_run_f64_noalloc", "gofr_run_windows", "gofr_set_centres", "gofr_msd_output_size",
-    "gofr_msd_run",
+    "gofr_msd_run", "gofr_neigh_layout", "gofr_neigh_run",
 ]
+
+
+class NeighLists:
+    """The reference's neighbour-list arrays (lib/include/neighbour.h:68-96)
+    with its accessors: size, indices, {r, x, y, z} rows, SANN count."""
+
+    def __init__(self, lst, rpos, nneigh, natoms):
+        self.list, self.rpos, self.nneigh, self.natoms = lst, rpos, list(nneigh), natoms
+        self.loff, self.roff = [0], [0]
+        for n in self.nneigh:
+            self.loff.append(self.loff[-1] + (n + 1) * natoms)
+            self.roff.append(self.roff[-1] + n * natoms * 4)
+
+    def size(self, a, k):
+        return int(self.list[self.loff[k] + a * (self.nneigh[k] + 1)])
+
+    def idx(self, a, k):
+        b = self.loff[k] + a * (self.nneigh[k] + 1)
+        return self.list[b + 1:b + 1 + self.size(a, k)].copy()
+
+    def r(self, a, k):
+        b = self.roff[k] + a * self.nneigh[k] * 4
+        return self.rpos[b:b + 4 * self.size(a, k)].reshape(-1, 4).copy()
+
+    def sann_n(self, a, k):
+        """Neighbours::get_sann_n (lib/src/neighbour.cpp:82-97) on the sorted list."""
+        r = self.r(a, k)[:, 0]
+        n = len(r)
+        if n < 3:
+            return 0
+        m, s = 3, 0.0
+        for i in range(3):
+            s += r[i]
+        while m < n:
+            if s <= r[m] * (m - 2):
+                break
+            s += r[m]
+            m += 1
+        return m
 
 
 class GofrError(RuntimeError):
@@ -52,6 +92,11 @@ class MsdParams(ctypes.Structure):
     _fields_ = [("skip", ctypes.c_uint), ("tmax", ctypes.c_uint), ("ntimesteps", ctypes.c_uint),
                 ("primo", ctypes.c_ulonglong), ("center_of_mass", ctypes.c_int),
                 ("in_center_of_mass_frame", ctypes.c_int)]
+
+
+class NeighSpec(ctypes.Structure):
+    _fields_ = [("nneigh", ctypes.c_ulonglong), ("cut2", ctypes.c_double),
+                ("skin2", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -115,6 +160,10 @@ def load_library(path=None):
     L.gofr_msd_output_size.argtypes = [vp, ctypes.POINTER(MsdParams),
                                        ctypes.POINTER(ctypes.c_size_t)]
     L.gofr_msd_run.argtypes = [vp, ctypes.POINTER(MsdParams), dp]
+    L.gofr_neigh_layout.argtypes = [vp, ctypes.POINTER(NeighSpec), ctypes.c_uint,
+                                    ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]
+    L.gofr_neigh_run.argtypes = [vp, ctypes.POINTER(NeighSpec), ctypes.c_uint, ctypes.c_size_t,
+                                 ctypes.c_int, up, dp]
     L.gofr_run_f64_noalloc.argtypes = [vp, vp, ctypes.c_int, vp, ctypes.c_uint, ctypes.c_size_t,
                                        ctypes.c_size_t, ctypes.POINTER(Params), vp, vp,
                                        ctypes.c_char_p, ctypes.c_size_t]
@@ -246,6 +295,20 @@ class Engine:
         self._check(self.L.gofr_msd_run(self._ctx, ctypes.byref(p), _dp(out)))
         leff = ntimesteps if (ntimesteps < tmax or tmax == 0) else tmax
         return out[:n.value].reshape(leff, 2 if center_of_mass else 1, self.ntypes)
+
+    def neighbours(self, timestep, spec, sort=True):
+        """Neighbours(t, spec).update_neigh(timestep, sort) on the resident
+        frames; spec = [(nneigh, cut2, skin2)] per type.  Returns NeighLists."""
+        arr = (NeighSpec * len(spec))(*[NeighSpec(int(a), float(b), float(c)) for a, b, c in spec])
+        nl, nr = ctypes.c_size_t(), ctypes.c_size_t()
+        self._check(self.L.gofr_neigh_layout(self._ctx, arr, len(spec), ctypes.byref(nl),
+                                             ctypes.byref(nr)))
+        lst = np.zeros(max(nl.value, 1), dtype=np.uint64)
+        rpos = np.zeros(max(nr.value, 1))
+        self._check(self.L.gofr_neigh_run(
+            self._ctx, arr, len(spec), int(timestep), int(bool(sort)),
+            lst.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)), _dp(rpos)))
+        return NeighLists(lst[:nl.value], rpos[:nr.value], [int(s[0]) for s in spec], self.natoms)
 
     def output_size(self, params):
         n = ctypes.c_size_t()

@@ -1,7 +1,7 @@
 // Python module `pyanalisi` of analisi_gb300: the reference's Gofrt path API
 // (pyanalisi/src/pyanalisi.cpp:67-82 for Gofrt, :124-152 for
-// MeanSquareDisplacement, :487-532 for Trajectory and BoxFormat) with the
-// GB300 engine behind it.
+// MeanSquareDisplacement, :196-236 for Neighbours, :487-532 for Trajectory and
+// BoxFormat) with the GB300 engine behind it.
 //
 //   import pyanalisi        # analisi_gb300/_build on sys.path
 //   t = pyanalisi.Trajectory(pos, vel, types, box, pyanalisi.BoxFormat.CellVectors, False, False)
@@ -19,6 +19,7 @@
 #include "gofrt.h"
 #include "lammps_file.h"
 #include "msd.h"
+#include "neighbour.h"
 #include "trajectory.h"
 
 namespace py = pybind11;
@@ -26,6 +27,7 @@ using analisi_gb300::BoxFormat;
 using analisi_gb300::Trajectory;
 using GofrtT = analisi_gb300::Gofrt<double, Trajectory>;
 using MsdT = analisi_gb300::MeanSquareDisplacement<Trajectory>;
+using NeighT = analisi_gb300::Neighbours<Trajectory, double>;
 
 namespace {
 
@@ -240,6 +242,33 @@ debug flag)doc")
         })
         .def("__enter__", [](MsdT &m) -> MsdT & { return m; }, py::return_value_policy::reference)
         .def("__exit__", [](MsdT &, py::object, py::object, py::object) {});
+
+    py::class_<NeighT>(m, "Neighbours")
+        .def(py::init<Trajectory *, typename NeighT::ListSpec>(), py::arg("trajectory"),
+             py::arg("nneigh_cut2_skin2"), py::keep_alive<1, 2>(),
+             "neighbour lists: [(max neighbours, cutoff^2, skin^2)] for each atomic type")
+        .def("calculate_neigh", [](NeighT &n, size_t timestep, bool sort) {
+            py::gil_scoped_release release;
+            n.update_neigh(timestep, sort);
+        })
+        .def("get_sann", [](NeighT &n, size_t iatom, size_t jtype) {
+            auto it = n.get_sann_r(iatom, jtype);
+            return py::array_t<double>({(ssize_t)it.size(), (ssize_t)4},
+                                       reinterpret_cast<const double *>(it.begin()));
+        })
+        .def("get_sann_idx", [](NeighT &n, size_t iatom, size_t jtype) {
+            auto it = n.get_sann(iatom, jtype);
+            return py::array_t<size_t>({(ssize_t)it.size()}, it.begin());
+        })
+        .def("get_neigh", [](NeighT &n, size_t iatom, size_t jtype) {
+            auto it = n.get_neigh_r(iatom, jtype);
+            return py::array_t<double>({(ssize_t)it.size(), (ssize_t)4},
+                                       reinterpret_cast<const double *>(it.begin()));
+        })
+        .def("get_neigh_idx", [](NeighT &n, size_t iatom, size_t jtype) {
+            auto it = n.get_neigh(iatom, jtype);
+            return py::array_t<size_t>({(ssize_t)it.size()}, it.begin());
+        });
 
     m.def("read_lammps_binary", [](const std::string &path) {
         analisi_gb300::LammpsFrames f = analisi_gb300::read_lammps_binary(path);

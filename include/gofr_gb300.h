@@ -46,7 +46,9 @@ enum gofr_status {
     GOFR_ERR_NOMEM = -4,    /* device or host allocation failed */
     GOFR_ERR_STATE = -5,    /* no frames uploaded yet */
     GOFR_ERR_DEVICE = -6,   /* a kernel reported an error word (bounded wait ran out, wrap loop cap) */
-    GOFR_ERR_UNSUPPORTED = -7
+    GOFR_ERR_UNSUPPORTED = -7,
+    GOFR_ERR_NEIGH_FULL = -8  /* a neighbour list overflowed (reference: "Too many neighbours in
+                                 shell!", lib/src/neighbour.cpp:44-47) */
 };
 
 enum gofr_box_kind {
@@ -276,6 +278,41 @@ int gofr_msd_output_size(const gofr_ctx *ctx, const gofr_msd_params *p, size_t *
  * the two agree to rounding (relative ~1e-13 for 1e7 terms).  Errors as
  * lib/src/msd.cpp:57-68 (GOFR_ERR_RANGE: trajectory too short). */
 int gofr_msd_run(gofr_ctx *ctx, const gofr_msd_params *p, double *out_host);
+
+/* ------------------------------------------------------------------------
+ * Neighbour lists of one resident frame (the reference's Neighbours<T,double>,
+ * lib/include/neighbour.h:9-104, lib/src/neighbour.cpp:9-97).
+ * ------------------------------------------------------------------------ */
+
+/* One entry of the reference's ListSpec: (max neighbours, cutoff^2, skin^2)
+ * for neighbours of one type (the skin is not used by the list build). */
+typedef struct gofr_neigh_spec {
+    unsigned long long nneigh;
+    double cut2;
+    double skin2;
+} gofr_neigh_spec;
+
+/* Lengths of the reference's two arrays for these specs (one per type):
+ * list  natoms * (sum nneigh + ntypes) u64: per type k from
+ *       list_off[k] = sum_{k'<k} (nneigh[k'] + 1) natoms, per atom i at
+ *       list_off[k] + i (nneigh[k] + 1): the list size, then the indices;
+ * rpos  natoms * 4 * sum nneigh doubles: from rpos_off[k] = sum_{k'<k}
+ *       nneigh[k'] natoms 4, per atom at rpos_off[k] + i nneigh[k] 4:
+ *       {r, x, y, z} per neighbour, x = x_i - x_neighbour (minimum image). */
+int gofr_neigh_layout(const gofr_ctx *ctx, const gofr_neigh_spec *spec, unsigned nspec,
+                      size_t *list_len, size_t *rpos_len);
+
+/* Neighbours::update_neigh(timestep, sort) on the resident frame `timestep`:
+ * for every atom and neighbour type, the atoms of that type within its cutoff
+ * (d2 <= cut2 of the neighbour's type, FP64 minimum image as the reference),
+ * in ascending index order, or sorted by distance when sort != 0 (stable);
+ * list_host / rpos_host receive the arrays above (entries past a list's size
+ * are 0).  A pair within either type's cutoff that finds one of the two lists
+ * full is the reference's error: GOFR_ERR_NEIGH_FULL, with the reference's
+ * message (iatom, jatom, ni, nj, itype, jtype of the first such pair in its
+ * loop order) in gofr_last_error.  At most 32 types. */
+int gofr_neigh_run(gofr_ctx *ctx, const gofr_neigh_spec *spec, unsigned nspec, size_t timestep,
+                   int sort, unsigned long long *list_host, double *rpos_host);
 
 #ifdef __cplusplus
 }

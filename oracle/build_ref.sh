@@ -1,12 +1,13 @@
 #!/bin/sh
-# Builds the reference's own Gofrt path (and MSD) into oracle/_ref/ (TEST
-# INFRASTRUCTURE).
+# Builds the reference's own Gofrt path (and MSD and neighbour lists) into
+# oracle/_ref/ (TEST INFRASTRUCTURE).
 #
 # Compiles the unmodified reference sources lib/src/gofrt.cpp, lib/src/msd.cpp,
-# lib/src/basetrajectory.cpp and lib/src/trajectory_numpy.cpp where they lie in
-# the reference tree, plus oracle/ref_shim.cpp, into one Python extension
-# pyanalisi_ref.  The reference's CMake build is not used (its pybind11
-# submodule is empty); this recipe replaces it for these four files only.
+# lib/src/neighbour.cpp, lib/src/basetrajectory.cpp and
+# lib/src/trajectory_numpy.cpp where they lie in the reference tree, plus
+# oracle/ref_shim.cpp, into one Python extension pyanalisi_ref.  The
+# reference's CMake build is not used (its pybind11 submodule is empty); this
+# recipe replaces it for these five files only.
 #
 # -ffp-contract=off pins the arithmetic to separate IEEE mul/add, which is what
 # an x86-64 build of the reference does by default; without it GCC on aarch64
@@ -44,7 +45,8 @@ static const char *_info_msg = "analisi reference Gofrt path built as a test ora
 EOF
 ${CXX:-g++} -std=c++17 -O3 -ffp-contract=off -fPIC -shared -w \
     -I"$OUT/cfg" -I"$REF/lib/include" -I"$REF/eigen3" -I"$PYBIND_INC" -I"$PYINC" \
-    "$REF/lib/src/gofrt.cpp" "$REF/lib/src/msd.cpp" "$REF/lib/src/basetrajectory.cpp" \
+    "$REF/lib/src/gofrt.cpp" "$REF/lib/src/msd.cpp" "$REF/lib/src/neighbour.cpp" \
+    "$REF/lib/src/basetrajectory.cpp" \
     "$REF/lib/src/trajectory_numpy.cpp" "$HERE/ref_shim.cpp" \
     -o "$OUT/pyanalisi_ref$SUFFIX" -lpthread
 echo "built $OUT/pyanalisi_ref$SUFFIX"

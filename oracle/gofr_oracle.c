@@ -26,6 +26,7 @@
  *   lib/include/calculatemultithread.h:50-78,80-104,106-162  split + loops
  *   lib/src/msd.cpp:37-118            MSD reset / calc_init / calc_single_th
  *   lib/src/trajectory_numpy.cpp:201-222  calc_cm_pos_vel  (centres of mass)
+ *   lib/src/neighbour.cpp:9-97        Neighbours update_neigh / get_sann_n
  */
 #include <math.h>
 #include <stdint.h>
@@ -332,4 +333,116 @@ int oracle_msd(const double *pos, const double *cm, const int *type_ids, unsigne
     }
     free(cont);
     return 0;
+}
+
+/*
+ * Neighbours<T,double>::update_neigh (lib/src/neighbour.cpp:9-79), literally:
+ * for i < j (i outer), d2 and x = x_i - x_j by the minimum image of frame
+ * `timestep`; a pair within either type's cutoff goes into i's list of j's
+ * type and j's list of i's type (written at the current size, counted only
+ * within the cutoff of the neighbour's type); a full list when such a pair
+ * arrives is the reference's "Too many neighbours in shell!" (returns -1 and
+ * err_info = {iatom, jatom, ni, nj, itype, jtype}).  Optional sort of every
+ * list by distance: a stable insertion sort (what std::sort does for up to 16
+ * elements; with ties in longer lists the reference's order is unspecified).
+ * Layout (neighbour.h:68-96): list[list_off[k] + i (nneigh[k]+1)] = size, then
+ * the indices; rpos[rpos_off[k] + i nneigh[k] 4 + 4 n] = {r, x, y, z}.
+ */
+int oracle_neigh(const double *pos, const double *boxes, size_t box_stride, int tric,
+                 const int *type_ids, unsigned ntypes, size_t natoms, size_t timestep,
+                 const uint64_t *nneigh, const double *cut2, int sort, uint64_t *list,
+                 double *rpos, uint64_t *err_info)
+{
+    size_t *loff = (size_t *)calloc(ntypes + 1, sizeof(size_t));
+    size_t *roff = (size_t *)calloc(ntypes + 1, sizeof(size_t));
+    size_t total = 0, max_n = 0;
+    for (unsigned k = 0; k < ntypes; ++k) {
+        loff[k + 1] = loff[k] + (nneigh[k] + 1) * natoms;
+        roff[k + 1] = roff[k] + nneigh[k] * natoms * 4;
+        total += nneigh[k];
+        if (nneigh[k] > max_n) max_n = nneigh[k];
+    }
+    for (size_t i = 0; i < natoms * (total + ntypes); ++i) list[i] = 0;
+    const double *box = boxes + timestep * box_stride;
+    static const double zero3[3] = {0.0, 0.0, 0.0};
+    int rc = 0;
+    for (size_t i = 0; i < natoms && rc == 0; ++i) {
+        const unsigned it = (unsigned)type_ids[i];
+        for (size_t j = i + 1; j < natoms; ++j) {
+            const unsigned jt = (unsigned)type_ids[j];
+            const double *xi = pos + (timestep * natoms + i) * 3;
+            const double *xj = pos + (timestep * natoms + j) * 3;
+            double x[3], d2 = 0.0;
+            for (int c = 0; c < 3; ++c) x[c] = xi[c] - xj[c];
+            oracle_min_image(x, box + 3, tric ? box + 6 : zero3, tric);
+            for (int c = 0; c < 3; ++c) d2 += x[c] * x[c];
+            if (d2 <= cut2[jt] || d2 <= cut2[it]) {
+                uint64_t *il = list + loff[jt] + i * (nneigh[jt] + 1);
+                uint64_t *jl = list + loff[it] + j * (nneigh[it] + 1);
+                const uint64_t ni = il[0], nj = jl[0];
+                if (ni < nneigh[jt] && nj < nneigh[it]) {
+                    const double r = sqrt(d2);
+                    il[1 + ni] = j;
+                    jl[1 + nj] = i;
+                    double *ip = rpos + roff[jt] + i * nneigh[jt] * 4 + ni * 4;
+                    double *jp = rpos + roff[it] + j * nneigh[it] * 4 + nj * 4;
+                    ip[0] = r;
+                    jp[0] = r;
+                    for (int c = 0; c < 3; ++c) {
+                        ip[1 + c] = x[c];
+                        jp[1 + c] = -x[c];
+                    }
+                    if (d2 <= cut2[jt]) il[0]++;
+                    if (d2 <= cut2[it]) jl[0]++;
+                } else {
+                    err_info[0] = i; err_info[1] = j; err_info[2] = ni; err_info[3] = nj;
+                    err_info[4] = it; err_info[5] = jt;
+                    rc = -1;
+                    break;
+                }
+            }
+        }
+    }
+    if (rc == 0 && sort) {
+        for (unsigned k = 0; k < ntypes; ++k) {
+            for (size_t a = 0; a < natoms; ++a) {
+                uint64_t *l = list + loff[k] + a * (nneigh[k] + 1);
+                double *rp = rpos + roff[k] + a * nneigh[k] * 4;
+                const size_t n = l[0];
+                for (size_t s = 1; s < n; ++s) {
+                    double e[4];
+                    memcpy(e, rp + 4 * s, sizeof e);
+                    const uint64_t id = l[1 + s];
+                    size_t q = s;
+                    while (q > 0 && e[0] < rp[4 * (q - 1)]) {
+                        memcpy(rp + 4 * q, rp + 4 * (q - 1), sizeof e);
+                        l[1 + q] = l[q];
+                        --q;
+                    }
+                    memcpy(rp + 4 * q, e, sizeof e);
+                    l[1 + q] = id;
+                }
+            }
+        }
+    }
+    (void)max_n;
+    free(loff);
+    free(roff);
+    return rc;
+}
+
+/* Neighbours::get_sann_n (lib/src/neighbour.cpp:82-97) on one list's
+ * distances r[0..n) (sorted). */
+uint64_t oracle_sann_n(const double *rpos4, uint64_t n)
+{
+    if (n < 3) return 0;
+    uint64_t m = 3;
+    double s = 0.0;
+    for (uint64_t i = 0; i < m; ++i) s += rpos4[4 * i];
+    while (m < n) {
+        if (s <= rpos4[4 * m] * (m - 2)) break;
+        s += rpos4[4 * m];
+        m++;
+    }
+    return m;
 }

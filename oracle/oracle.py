@@ -70,6 +70,13 @@ def lib():
                                  ctypes.c_uint, ctypes.c_uint, ctypes.c_uint, ctypes.c_size_t,
                                  ctypes.c_int, ctypes.c_int, dp]
         L.oracle_msd.restype = ctypes.c_int
+        u64p = ctypes.POINTER(ctypes.c_uint64)
+        L.oracle_neigh.argtypes = [dp, dp, ctypes.c_size_t, ctypes.c_int, ip, ctypes.c_uint,
+                                   ctypes.c_size_t, ctypes.c_size_t, u64p, dp, ctypes.c_int, u64p,
+                                   dp, u64p]
+        L.oracle_neigh.restype = ctypes.c_int
+        L.oracle_sann_n.argtypes = [dp, ctypes.c_uint64]
+        L.oracle_sann_n.restype = ctypes.c_uint64
         _lib = L
     return _lib
 
@@ -169,6 +176,62 @@ def msd(pos, type_ids, ntypes, skip, tmax, ntimesteps, primo, cm_msd=False, cm_s
                            "different starting timestep or lower the size of the average or "
                            "the lenght of the time lag")
     return out
+
+
+class NeighLists:
+    """The reference's neighbour-list arrays (neighbour.h:68-96) and accessors."""
+
+    def __init__(self, lst, rpos, nneigh, natoms):
+        self.list, self.rpos, self.nneigh, self.natoms = lst, rpos, list(nneigh), natoms
+        self.loff, self.roff = [0], [0]
+        for n in self.nneigh:
+            self.loff.append(self.loff[-1] + (n + 1) * natoms)
+            self.roff.append(self.roff[-1] + n * natoms * 4)
+
+    def size(self, a, k):
+        return int(self.list[self.loff[k] + a * (self.nneigh[k] + 1)])
+
+    def idx(self, a, k):
+        b = self.loff[k] + a * (self.nneigh[k] + 1)
+        return self.list[b + 1:b + 1 + self.size(a, k)].copy()
+
+    def r(self, a, k):
+        b = self.roff[k] + a * self.nneigh[k] * 4
+        return self.rpos[b:b + 4 * self.size(a, k)].reshape(-1, 4).copy()
+
+    def sann_n(self, a, k):
+        r = np.ascontiguousarray(self.r(a, k))
+        return int(lib().oracle_sann_n(_dp(r), r.shape[0])) if r.size else 0
+
+
+class TooManyNeighbours(RuntimeError):
+    pass
+
+
+def neighbours(pos, boxes, type_ids, ntypes, timestep, spec, sort):
+    """Neighbours(t, spec).update_neigh(timestep, sort) of the reference;
+    spec = [(nneigh, cut2, skin2)] per type.  Raises TooManyNeighbours with the
+    reference's message."""
+    pos = np.ascontiguousarray(pos, dtype=np.float64)
+    boxes = np.ascontiguousarray(boxes, dtype=np.float64)
+    type_ids = np.ascontiguousarray(type_ids, dtype=np.int32)
+    T, N = pos.shape[0], pos.shape[1]
+    nn = np.array([int(s[0]) for s in spec], dtype=np.uint64)
+    c2 = np.array([float(s[1]) for s in spec], dtype=np.float64)
+    tot = int(nn.sum())
+    lst = np.zeros(N * (tot + ntypes), dtype=np.uint64)
+    rpos = np.zeros(N * 4 * tot, dtype=np.float64)
+    err = np.zeros(6, dtype=np.uint64)
+    u64 = ctypes.POINTER(ctypes.c_uint64)
+    rc = lib().oracle_neigh(_dp(pos), _dp(boxes), boxes.shape[1], int(boxes.shape[1] == 9),
+                            type_ids.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), int(ntypes), N,
+                            int(timestep), nn.ctypes.data_as(u64), _dp(c2), int(bool(sort)),
+                            lst.ctypes.data_as(u64), _dp(rpos), err.ctypes.data_as(u64))
+    if rc == -1:
+        i, j, ni, nj, it, jt = (int(v) for v in err)
+        raise TooManyNeighbours(f"Too many neighbours in shell! (iatom={i} jatom={j} ni={ni} "
+                                f"nj={nj} itype={it} jtype={jt})")
+    return NeighLists(lst, rpos, nn, N)
 
 
 def incr(ntimesteps, skip):

@@ -1,19 +1,24 @@
-// Reduced Python binding of the reference's own Gofrt path (and its MSD).
+// Reduced Python binding of the reference's own Gofrt path (and its MSD and
+// neighbour lists).
 //
 // TEST INFRASTRUCTURE ONLY.  This file is compiled together with the
 // reference's unmodified sources lib/src/gofrt.cpp, lib/src/msd.cpp,
-// lib/src/basetrajectory.cpp and lib/src/trajectory_numpy.cpp (see
+// lib/src/neighbour.cpp, lib/src/basetrajectory.cpp and
+// lib/src/trajectory_numpy.cpp (see
 // oracle/build_ref.sh) into oracle/_ref/pyanalisi_ref*.so.  It exposes the
 // classes these paths need, with the constructor and method signatures of the
 // full reference binding (pyanalisi/src/pyanalisi.cpp:67-82 for Gofrt,
-// :124-152 for MeanSquareDisplacement, :487-527 for Trajectory, :528-532 for
+// :124-152 for MeanSquareDisplacement, :196-236 for Neighbours, :487-527 for
+// Trajectory, :528-532 for
 // BoxFormat), so that fixtures can be generated by the reference itself and
 // the C restatement in oracle/gofr_oracle.c can be pinned against it.
 #include <pybind11/pybind11.h>
 #include <pybind11/numpy.h>
+#include <pybind11/stl.h>
 #include "trajectory_numpy.h"
 #include "gofrt.h"
 #include "msd.h"
+#include "neighbour.h"
 
 namespace py = pybind11;
 
@@ -75,5 +80,25 @@ PYBIND11_MODULE(pyanalisi_ref, m) {
             return py::buffer_info(g.access_vdata(), sizeof(double),
                                    py::format_descriptor<double>::format(),
                                    g.get_shape().size(), g.get_shape(), g.get_stride());
+        });
+    using NEIGH = Neighbours<Trajectory_numpy, double>;
+    py::class_<NEIGH>(m, "Neighbours")
+        .def(py::init<Trajectory_numpy *, typename NEIGH::ListSpec>(), py::keep_alive<1, 2>())
+        .def("calculate_neigh", &NEIGH::update_neigh)
+        .def("get_sann", [](NEIGH &n, size_t iatom, size_t jtype) {
+            auto it = n.get_sann_r(iatom, jtype);
+            return py::array_t<double>({(ssize_t)it.size(), (ssize_t)4}, (const double *)it.begin());
+        })
+        .def("get_sann_idx", [](NEIGH &n, size_t iatom, size_t jtype) {
+            auto it = n.get_sann(iatom, jtype);
+            return py::array_t<size_t>({(ssize_t)it.size()}, it.begin());
+        })
+        .def("get_neigh", [](NEIGH &n, size_t iatom, size_t jtype) {
+            auto it = n.get_neigh_r(iatom, jtype);
+            return py::array_t<double>({(ssize_t)it.size(), (ssize_t)4}, (const double *)it.begin());
+        })
+        .def("get_neigh_idx", [](NEIGH &n, size_t iatom, size_t jtype) {
+            auto it = n.get_neigh(iatom, jtype);
+            return py::array_t<size_t>({(ssize_t)it.size()}, it.begin());
         });
 }
