@@ -1996,6 +1996,26 @@ int gofr_neigh_run(gofr_ctx *ctx, const gofr_neigh_spec *spec, unsigned nspec, s
     L.ntypes = (int)nt;
     L.timestep = (long long)timestep;
     L.tric = t.tric;
+    // FP32 prefilter with the all-pairs kernel's certified bound, where the
+    // minimum image of the near pairs is certain
+    {
+        double cmax = -INFINITY;
+        for (unsigned k = 0; k < nt; ++k) cmax = std::max(cmax, cut2[k]);
+        if (std::isfinite(cmax) && cmax >= 0.0) {
+            const Bound b = error_bound(t);
+            const float hi = f_up(cmax + Efun(b, cmax));
+            const double emax = std::max(b.e[0], std::max(b.e[1], b.e[2]));
+            const double reach = std::sqrt((double)hi) * (1.0 + std::ldexp(1.0, -20)) +
+                                 2.0 * emax + 1e-9;
+            if (std::isfinite(hi) && t.bs.lh_min > reach) {
+                L.prefilter = 1;
+                L.hi_f = hi;
+                L.pos32 = t.pos32;
+                L.box32 = t.box32;
+                L.NP = (long long)padded_natoms(t.N);
+            }
+        }
+    }
     std::memset(&ctx->stats, 0, sizeof ctx->stats);
     CK(cudaEventRecord(ctx->ev[1], ctx->stream));
     ++ctx->launches;

@@ -111,6 +111,13 @@ struct NeighLaunch {
     int N, ntypes;
     long long timestep;
     int tric;
+    // FP32 prefilter (the all-pairs kernel's certified arithmetic): a pair
+    // with d2_f32 > hi_f has reference d2 > the largest cutoff
+    int prefilter;
+    const float *pos32;                   // [T][3][NP]
+    const Box32 *box32;                   // [T]
+    long long NP;
+    float hi_f;
 };
 int launch_neigh_build(const NeighLaunch &L, int num_sms, cudaStream_t s);
 int launch_neigh_check(const NeighLaunch &L, int num_sms, cudaStream_t s);

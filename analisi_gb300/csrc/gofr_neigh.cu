@@ -8,7 +8,9 @@
 // minimum-image vector for the ordered pair (lower index first, negated for
 // the higher-index atom, as the reference stores -x), and the counted entries
 // of each neighbour type are placed by a ballot prefix, which keeps the
-// ascending order.  Overflow follows the reference's rule exactly: a pair
+// ascending order.  Where the all-pairs kernel's FP32 bound certifies it, an
+// FP32 minimum-image d2 first discards the pairs beyond every cutoff, so the
+// FP64 arithmetic runs only for the few near pairs.  Overflow follows the reference's rule exactly: a pair
 // (i < j) within either cutoff is an error when, at that point of the
 // reference's loop, i's list of j's type or j's list of i's type is full;
 // with full[a][k] = the neighbour index that filled a's list of type k, that
@@ -43,6 +45,43 @@ __device__ __forceinline__ double pair_vec(const NeighLaunch &L, const double *f
     return s;
 }
 
+// FP32 minimum-image d2 of one pair with exactly the all-pairs kernel's
+// operations (gofr_kernels.cu pair2<TRI, false>, one lane), so that kernel's
+// certified bound applies: d2_f32 > hi_f implies the reference's d2 exceeds
+// every cutoff.
+template <bool TRI>
+__device__ __forceinline__ float pair_f32(const NeighLaunch &L, int a, int b)
+{
+    const float MAG = 12582912.0f;
+    const float *f = L.pos32 + L.timestep * 3 * L.NP;
+    const Box32 bx = L.box32[L.timestep];
+    float dx = __fsub_rn(f[a], f[b]);
+    float dy = __fsub_rn(f[L.NP + a], f[L.NP + b]);
+    float dz = __fsub_rn(f[2 * L.NP + a], f[2 * L.NP + b]);
+    if (TRI) {
+        const float kz = __fsub_rn(__fmaf_rn(dz, bx.invL[2], MAG), MAG);
+        dz = __fmaf_rn(kz, -bx.L[2], dz);
+        dy = __fmaf_rn(kz, -bx.tilt[2], dy);
+        dx = __fmaf_rn(kz, -bx.tilt[1], dx);
+        const float ky = __fsub_rn(__fmaf_rn(dy, bx.invL[1], MAG), MAG);
+        dy = __fmaf_rn(ky, -bx.L[1], dy);
+        dx = __fmaf_rn(ky, -bx.tilt[0], dx);
+        const float kx = __fsub_rn(__fmaf_rn(dx, bx.invL[0], MAG), MAG);
+        dx = __fmaf_rn(kx, -bx.L[0], dx);
+    } else {
+        const float kx = __fsub_rn(__fmaf_rn(dx, bx.invL[0], MAG), MAG);
+        const float ky = __fsub_rn(__fmaf_rn(dy, bx.invL[1], MAG), MAG);
+        const float kz = __fsub_rn(__fmaf_rn(dz, bx.invL[2], MAG), MAG);
+        dx = __fmaf_rn(kx, -bx.L[0], dx);
+        dy = __fmaf_rn(ky, -bx.L[1], dy);
+        dz = __fmaf_rn(kz, -bx.L[2], dz);
+    }
+    float d2 = __fmul_rn(dx, dx);
+    d2 = __fmaf_rn(dy, dy, d2);
+    d2 = __fmaf_rn(dz, dz, d2);
+    return d2;
+}
+
 template <bool TRI>
 __global__ void __launch_bounds__(NT) k_neigh_build(const NeighLaunch L)
 {
@@ -67,7 +106,9 @@ __global__ void __launch_bounds__(NT) k_neigh_build(const NeighLaunch L)
             int tb = 0;
             double x[3] = {0.0, 0.0, 0.0}, d2 = 0.0;
             bool counted = false;
-            if (valid) {
+            if (valid && L.prefilter && !(pair_f32<TRI>(L, a, b) <= L.hi_f)) {
+                // certainly beyond every cutoff: neither counted nor a candidate
+            } else if (valid) {
                 tb = L.types[b];
                 const int i = a < b ? a : b, j = a < b ? b : a;
                 d2 = pair_vec<TRI>(L, frame, box, i, j, x);
@@ -117,6 +158,7 @@ __global__ void __launch_bounds__(NT) k_neigh_check(const NeighLaunch L)
         if (i >= L.N) continue;
         const int ti = L.types[i];
         for (int j = i + 1 + lane; j < L.N; j += 32) {
+            if (L.prefilter && !(pair_f32<TRI>(L, i, j) <= L.hi_f)) continue;
             const int tj = L.types[j];
             double x[3];
             const double d2 = pair_vec<TRI>(L, frame, box, i, j, x);

@@ -369,6 +369,37 @@ def bench_msd(eng, w, p, reps=3):
                                    "sample": "20 lags x 10 origins", "seconds": round(dt, 3)}}
 
 
+def bench_neigh(eng, w, frames=3):
+    """Neighbours::update_neigh on frames of the resident 16k-atom trajectory:
+    3 types, cutoff 3.5 (about 18 neighbours per type and atom), sorted lists; the
+    oracle (one thread, the reference's i < j loop) timed on one frame of the
+    first 2048 atoms, compared per pair."""
+    import numpy as np
+    from oracle import oracle
+    spec = [(64, 3.5 ** 2, 4.0 ** 2)] * w["ntypes"]
+    eng.neighbours(0, spec, True)
+    ms = []
+    for f in range(1, 1 + frames):
+        eng.neighbours(f, spec, True)
+        ms.append(eng.stats()["kernel_ms"])
+    N = w["positions"].shape[1]
+    n_sub = 2048
+    t0 = time.perf_counter()
+    oracle.neighbours(w["positions"][:2, :n_sub], w["boxes"][:2], w["type_ids"][:n_sub],
+                      w["ntypes"], 1, spec, True)
+    dt = time.perf_counter() - t0
+    cpu_pairs_per_s = n_sub * (n_sub - 1) / 2 / dt
+    gpu_frame_ms = sum(ms) / len(ms)
+    return {"workload": "c2 frames (N=16384, 3 types), cutoff 3.5 for every type, sorted",
+            "ms_per_frame": round(gpu_frame_ms, 3),
+            "value": round(N * (N - 1) / 2 / (gpu_frame_ms * 1e-3) / 1e9, 3),
+            "unit": "G atom pairs (i<j)/s",
+            "cpu_oracle_1thread": {"value": round(cpu_pairs_per_s / 1e9, 4),
+                                   "unit": "G atom pairs (i<j)/s",
+                                   "sample": f"one frame of the first {n_sub} atoms",
+                                   "seconds": round(dt, 3)}}
+
+
 def bench_cells(engine, workloads, device):
     """131072 atoms, 4 types, 250 bins on [0,10]: the cell-list kernel on a sample
     (10 origins x 50 lags), its counts checked against the all-pairs FP32 kernel on
@@ -544,6 +575,7 @@ def run_gpu(args):
     extra = {}
     if not args.no_extra:
         extra["msd"] = bench_msd(eng, w, p)
+        extra["neighbours"] = bench_neigh(eng, w)
         del w
         if kernel_used != 1:
             extra["allpairs_f32"] = bench_allpairs(eng, prm, args, flush)

@@ -112,3 +112,17 @@ def test_neighbour_argument_errors(gpu_engine):
         gpu_engine.neighbours(0, [(10, 4.0, 5.0)], True)
     with pytest.raises(engine.GofrError, match="outside"):
         gpu_engine.neighbours(5, [(10, 4.0, 5.0), (10, 4.0, 5.0)], True)
+
+
+def test_engine_neighbours_small_box_fp64_path(gpu_engine, oracle_mod):
+    """A cutoff just under half the box: the minimum image of near pairs is not
+    certain in FP32, so every pair takes the FP64 path; lists as the oracle's."""
+    w = workloads.small_case(83, 300, 2, 6.0, 0.1, [200, 100])
+    spec = [(300, 2.99 ** 2, 3.0 ** 2), (300, 2.9 ** 2, 3.0 ** 2)]
+    o = oracle_mod.neighbours(w["positions"], w["boxes"], w["type_ids"], 2, 1, spec, True)
+    gpu_engine.set_frames(w["positions"], w["boxes"], w["type_ids"], 2)
+    nl = gpu_engine.neighbours(1, spec, True)
+    for a in range(300):
+        for k in range(2):
+            np.testing.assert_array_equal(nl.idx(a, k), o.idx(a, k))
+            np.testing.assert_array_equal(nl.r(a, k), o.r(a, k))
