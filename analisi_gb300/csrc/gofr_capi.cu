@@ -92,6 +92,7 @@ struct gofr_ctx {
     unsigned long long *d_nl_list = nullptr, *d_nl_meta = nullptr;
     double *d_nl_rpos = nullptr, *d_nl_cut2 = nullptr;
     int *d_nl_full = nullptr;
+
     size_t cap_nl_list = 0, cap_nl_meta = 0, cap_nl_rpos = 0, cap_nl_cut2 = 0, cap_nl_full = 0;
     double *d_minmax = nullptr;
     unsigned *d_nonfinite = nullptr;
@@ -115,6 +116,14 @@ struct gofr_ctx {
         unsigned long long pairs = 0;
         int grid[2] = {0, 0};
         cudaGraphExec_t graph = nullptr;
+        // members run through the cell-list kernel (one launch for all of them)
+        std::vector<int> cell_trajs;
+        std::vector<CellLaunch> cells;
+        CellLaunch *d_cells = nullptr;
+        long long *d_cell_end = nullptr;
+        long long cell_items = 0;
+        unsigned long long allpairs_pairs = 0;  // pairs of the members not run with cells
+        int cell_r = 3, cell_max_nbin = 1, cell_max_nch = 1, cell_max_ntypes = 1, cell_grid = 0;
     } batch;
 };
 
@@ -823,6 +832,40 @@ int check_device_error(gofr_ctx *ctx)
     return GOFR_OK;
 }
 
+// Builds (once per grid and frames) the cell-sorted copy of t's frames.
+int ensure_cells(gofr_ctx *ctx, const TrajDev &t, const Plan &pl)
+{
+    TrajDev &tm = const_cast<TrajDev &>(t);
+    if (tm.cell_nc[0] == pl.nc[0] && tm.cell_nc[1] == pl.nc[1] && tm.cell_nc[2] == pl.nc[2])
+        return GOFR_OK;
+    cudaFree(tm.d_cstart); cudaFree(tm.d_sidt); cudaFree(tm.d_spos);
+    tm.d_cstart = nullptr; tm.d_sidt = nullptr; tm.d_spos = nullptr;
+    tm.cell_nc[0] = tm.cell_nc[1] = tm.cell_nc[2] = 0;
+    const size_t ncell = (size_t)pl.nc[0] * pl.nc[1] * pl.nc[2];
+    const size_t NP = padded_natoms(t.N);
+    int *cell_of = nullptr, *rank_of = nullptr, *count = nullptr;
+    CK(cudaMalloc(&tm.d_cstart, t.T * (ncell + 1) * sizeof(int)));
+    CK(cudaMalloc(&tm.d_sidt, t.T * NP * sizeof(unsigned)));
+    CK(cudaMalloc(&tm.d_spos, t.T * 3 * NP * sizeof(float)));
+    CK(cudaMalloc(&cell_of, t.T * t.N * sizeof(int)));
+    CK(cudaMalloc(&rank_of, t.T * t.N * sizeof(int)));
+    CK(cudaMalloc(&count, t.T * (ncell + 1) * sizeof(int)));
+    ctx->launches += 3;
+    double centre[3];
+    for (int k = 0; k < 3; ++k) centre[k] = t.h_box[k] + t.h_box[3 + k];  // xlo + L/2
+    const int brc = launch_cell_build(t.pos64, t.types8, t.T, t.N, &t.h_box[0], centre, pl.nc,
+                                      cell_of, rank_of, count, tm.d_cstart, tm.d_spos,
+                                      tm.d_sidt, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(cell_of);
+    cudaFree(rank_of);
+    cudaFree(count);
+    if (brc) return fail(ctx, GOFR_ERR_CUDA, "cell-list build failed: %s",
+                         cudaGetErrorString(cudaGetLastError()));
+    for (int k = 0; k < 3; ++k) tm.cell_nc[k] = pl.nc[k];
+    return GOFR_OK;
+}
+
 // Queue every launch of one trajectory's calculate on the stream; counts is
 // a device pointer to data_length*(nparts>1?nparts:1) zeroed counts.
 int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const RunShape &rs,
@@ -883,34 +926,8 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
         L.wlim = (float)(0.5 - pl.b.eta);
     }
     if (pl.cells && !ghist) {
-        TrajDev &tm = const_cast<TrajDev &>(t);
-        if (tm.cell_nc[0] != pl.nc[0] || tm.cell_nc[1] != pl.nc[1] || tm.cell_nc[2] != pl.nc[2]) {
-            cudaFree(tm.d_cstart); cudaFree(tm.d_sidt); cudaFree(tm.d_spos);
-            tm.d_cstart = nullptr; tm.d_sidt = nullptr; tm.d_spos = nullptr;
-            tm.cell_nc[0] = tm.cell_nc[1] = tm.cell_nc[2] = 0;
-            const size_t ncell = (size_t)pl.nc[0] * pl.nc[1] * pl.nc[2];
-            const size_t NP = padded_natoms(t.N);
-            int *cell_of = nullptr, *rank_of = nullptr, *count = nullptr;
-            CK(cudaMalloc(&tm.d_cstart, t.T * (ncell + 1) * sizeof(int)));
-            CK(cudaMalloc(&tm.d_sidt, t.T * NP * sizeof(unsigned)));
-            CK(cudaMalloc(&tm.d_spos, t.T * 3 * NP * sizeof(float)));
-            CK(cudaMalloc(&cell_of, t.T * t.N * sizeof(int)));
-            CK(cudaMalloc(&rank_of, t.T * t.N * sizeof(int)));
-            CK(cudaMalloc(&count, t.T * (ncell + 1) * sizeof(int)));
-            ctx->launches += 3;
-            double centre[3];
-            for (int k = 0; k < 3; ++k) centre[k] = t.h_box[k] + t.h_box[3 + k];  // xlo + L/2
-            const int brc = launch_cell_build(t.pos64, t.types8, t.T, t.N, &t.h_box[0], centre,
-                                              pl.nc, cell_of, rank_of, count, tm.d_cstart,
-                                              tm.d_spos, tm.d_sidt, ctx->stream);
-            cudaStreamSynchronize(ctx->stream);
-            cudaFree(cell_of);
-            cudaFree(rank_of);
-            cudaFree(count);
-            if (brc) return fail(ctx, GOFR_ERR_CUDA, "cell-list build failed: %s",
-                                 cudaGetErrorString(cudaGetLastError()));
-            for (int k = 0; k < 3; ++k) tm.cell_nc[k] = pl.nc[k];
-        }
+        int brc = ensure_cells(ctx, t, pl);
+        if (brc) return brc;
         CellLaunch C{};
         C.pair = L;
         C.pair.a0 = 0;
@@ -1191,6 +1208,8 @@ void free_batch(gofr_ctx *ctx)
     cudaFree(B.d_win);
     cudaFree(B.d_chtab);
     cudaFree(B.d_counts);
+    cudaFree(B.d_cells);
+    cudaFree(B.d_cell_end);
     if (B.h_stage) cudaFreeHost(B.h_stage);
     B = gofr_ctx::Batch{};
 }
@@ -1209,6 +1228,8 @@ int build_batch(gofr_ctx *ctx)
     unsigned long long total = 0;
     std::vector<Plan> plans(ctx->trajs.size());
     std::vector<RunShape> shapes(ctx->trajs.size());
+    std::vector<std::vector<CellCand>> cands(ctx->trajs.size());
+    std::vector<double> work(ctx->trajs.size(), 0.0);
     for (size_t k = 0; k < ctx->trajs.size(); ++k) {
         TrajDev &t = ctx->trajs[k];
         gofr_params p = t.params;
@@ -1216,11 +1237,52 @@ int build_batch(gofr_ctx *ctx)
         p.nparts = 1;
         int rc = shape_of(ctx, t, p, shapes[k]);
         if (rc) return rc;
-        rc = make_plan(ctx, t, p, plans[k], false);  // the batch kernel is all-pairs
+        rc = make_plan(ctx, t, p, plans[k], false);  // all-pairs plan; cells decided below
         if (rc) return rc;
-        total += (unsigned long long)shapes[k].n_lags * shapes[k].n_orig * t.N * t.N;
+        const unsigned long long pk = (unsigned long long)shapes[k].n_lags * shapes[k].n_orig * t.N * t.N;
+        total += pk;
+        work[k] = (double)pk;
+        if (plans[k].kind == 0 && !plans[k].wrapcheck && !plans[k].empty)
+            cands[k] = cell_candidates(t, p);
     }
     B.pairs = total;
+    // One cell-list launch serves every member that gains from cell lists; it
+    // has one first-atoms-per-thread count R, the one with the least modelled
+    // time over the batch.
+    auto best_of = [&](size_t k, int r) -> const CellCand * {
+        for (const CellCand &c : cands[k])
+            if (c.r == r) return c.time < kCellAutoTime ? &c : nullptr;
+        return nullptr;
+    };
+    {
+        double best_total = 1e300;
+        for (int r = 2; r <= 4; ++r) {
+            double tot = 0.0;
+            for (size_t k = 0; k < ctx->trajs.size(); ++k) {
+                const CellCand *c = best_of(k, r);
+                tot += work[k] * (c ? c->time : 1.0);
+            }
+            if (tot < best_total) { best_total = tot; B.cell_r = r; }
+        }
+    }
+    std::vector<char> is_cell(ctx->trajs.size(), 0);
+    for (size_t k = 0; k < ctx->trajs.size(); ++k) {
+        const CellCand *c = best_of(k, B.cell_r);
+        if (!c) {
+            B.allpairs_pairs += (unsigned long long)work[k];
+            continue;
+        }
+        Plan q = plans[k];
+        gofr_params p = ctx->trajs[k].params;
+        p.nparts = 1;
+        if (make_cell_plan(ctx->trajs[k], p, q, *c) &&
+            cell_smem_bytes((int)shapes[k].nch, (int)p.nbin, (int)ctx->trajs[k].ntypes) <= 160 * 1024) {
+            plans[k] = q;
+            is_cell[k] = 1;
+        } else {
+            B.allpairs_pairs += (unsigned long long)work[k];
+        }
+    }
     const unsigned long long target =
         std::max<unsigned long long>(total / ((unsigned long long)ctx->num_sms * 2 * 24), 1ull << 24);
     struct Cost { unsigned long long c; WorkDesc w; bool tri; };
@@ -1237,6 +1299,13 @@ int build_batch(gofr_ctx *ctx)
         std::vector<unsigned short> tab = channel_table(t.ntypes);
         tab_off[k] = tabs.size();
         tabs.insert(tabs.end(), tab.begin(), tab.end());
+        if (is_cell[k]) {
+            B.cell_trajs.push_back((int)k);
+            B.cell_max_nbin = std::max(B.cell_max_nbin, (int)t.params.nbin);
+            B.cell_max_nch = std::max(B.cell_max_nch, (int)rs.nch);
+            B.cell_max_ntypes = std::max(B.cell_max_ntypes, (int)t.ntypes);
+            continue;
+        }
         B.max_nbin = std::max(B.max_nbin, (int)t.params.nbin);
         B.max_nch = std::max(B.max_nch, (int)rs.nch);
         B.max_ntypes = std::max(B.max_ntypes, (int)t.ntypes);
@@ -1304,6 +1373,35 @@ int build_batch(gofr_ctx *ctx)
         L.tric = t.tric;
         L.wchk = pl.wrapcheck ? 1 : 0;
     }
+    // cell-list members: sorted frames, one record each, their items back to back
+    std::vector<long long> cell_end;
+    for (int k : B.cell_trajs) {
+        TrajDev &t = ctx->trajs[k];
+        const Plan &pl = plans[k];
+        int rc = ensure_cells(ctx, t, pl);
+        if (rc) return rc;
+        CellLaunch C{};
+        C.pair = B.launches[k];
+        C.pair.n_items = (long long)C.pair.n_lags * pl.nb[0] * pl.nb[1] * pl.nb[2] * C.pair.n_orig;
+        C.start = t.d_cstart;
+        C.spos = t.d_spos;
+        C.sidt = t.d_sidt;
+        for (int a = 0; a < 3; ++a) { C.nc[a] = pl.nc[a]; C.b[a] = pl.blk[a]; C.nb[a] = pl.nb[a]; }
+        C.reach = pl.reach;
+        C.r = pl.cell_r;
+        B.cells.push_back(C);
+        B.cell_items += C.pair.n_items;
+        cell_end.push_back(B.cell_items);
+        B.launches[k] = PairLaunch{};  // not in the all-pairs queue
+    }
+    if (!B.cells.empty()) {
+        CK(cudaMalloc(&B.d_cells, B.cells.size() * sizeof(CellLaunch)));
+        CK(cudaMalloc(&B.d_cell_end, cell_end.size() * sizeof(long long)));
+        CK(cudaMemcpy(B.d_cells, B.cells.data(), B.cells.size() * sizeof(CellLaunch),
+                      cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(B.d_cell_end, cell_end.data(), cell_end.size() * sizeof(long long),
+                      cudaMemcpyHostToDevice));
+    }
     CK(cudaMalloc(&B.d_launches, std::max<size_t>(B.launches.size(), 1) * sizeof(PairLaunch)));
     CK(cudaMemcpy(B.d_launches, B.launches.data(), B.launches.size() * sizeof(PairLaunch),
                   cudaMemcpyHostToDevice));
@@ -1326,6 +1424,15 @@ int build_batch(gofr_ctx *ctx)
                           (int)B.work[v].size(), &B.grid[v]))
             return fail(ctx, GOFR_ERR_CUDA, "batched kernel setup failed");
     }
+    if (!B.cells.empty()) {
+        const int csmem = cell_smem_bytes(B.cell_max_nch, B.cell_max_nbin, B.cell_max_ntypes);
+        if (csmem > max_smem)
+            return fail(ctx, GOFR_ERR_UNSUPPORTED, "batch cell-list histograms need %d B", csmem);
+        if (prepare_cell_pairs_multi(B.cell_r, B.cell_max_nbin, B.cell_max_nch,
+                                     B.cell_max_ntypes, ctx->num_sms, B.cell_items,
+                                     &B.cell_grid))
+            return fail(ctx, GOFR_ERR_CUDA, "batched cell-list kernel setup failed");
+    }
     return GOFR_OK;
 }
 
@@ -1344,6 +1451,14 @@ int enqueue_batch(gofr_ctx *ctx)
                               B.max_nbin, B.max_nch, B.max_ntypes, v == 1, ctx->d_err,
                               ctx->d_stats, B.grid[v], ctx->stream))
             return fail(ctx, GOFR_ERR_CUDA, "batched kernel launch failed: %s",
+                        cudaGetErrorString(cudaGetLastError()));
+    }
+    if (!B.cells.empty()) {
+        ++ctx->launches;
+        if (launch_cell_pairs_multi(B.d_cells, B.d_cell_end, (int)B.cells.size(), B.cell_r,
+                                    B.cell_max_nbin, B.cell_max_nch, B.cell_max_ntypes,
+                                    B.cell_grid, ctx->stream))
+            return fail(ctx, GOFR_ERR_CUDA, "batched cell-list kernel launch failed: %s",
                         cudaGetErrorString(cudaGetLastError()));
     }
     for (int k : B.f64_trajs) {
@@ -1430,6 +1545,7 @@ void gofr_ctx_destroy(gofr_ctx *ctx)
         cudaFree(ctx->d_nl_rpos);
         cudaFree(ctx->d_nl_cut2);
         cudaFree(ctx->d_nl_full);
+
         for (auto &e : ctx->ev)
             if (e) cudaEventDestroy(e);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -1805,7 +1921,7 @@ int gofr_batch_run(gofr_ctx *ctx, int use_graph, unsigned long long *counts_host
     if (use_graph) {
         CK(cudaGraphLaunch(B.graph, ctx->stream));
         ctx->launches += (B.work[0].empty() ? 0 : 1) + (B.work[1].empty() ? 0 : 1) +
-                         B.f64_trajs.size();
+                         (B.cells.empty() ? 0 : 1) + B.f64_trajs.size();
     } else {
         int rc = enqueue_batch(ctx);
         if (rc) return rc;
@@ -1815,9 +1931,11 @@ int gofr_batch_run(gofr_ctx *ctx, int use_graph, unsigned long long *counts_host
     std::memset(&ctx->stats, 0, sizeof ctx->stats);
     ctx->stats.pairs = B.pairs;
     ctx->stats.evaluated = B.pairs;
-    ctx->stats.kernel_used = GOFR_KERNEL_AUTO;
+    ctx->stats.kernel_used = B.cells.empty() ? GOFR_KERNEL_AUTO : GOFR_KERNEL_CELL;
     int rc = gofr_sync(ctx);
     if (rc) return rc;
+    // evaluated: every pair of the all-pairs members, the cell members' own count
+    if (!B.cells.empty()) ctx->stats.evaluated += B.allpairs_pairs;
     std::memcpy(counts_host, B.h_stage, ctx->batch_total * sizeof(unsigned long long));
     return GOFR_OK;
 }

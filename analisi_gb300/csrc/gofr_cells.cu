@@ -248,44 +248,108 @@ __device__ __forceinline__ void cp_async_wait()
 // stay in L2.  Each item streams its neighbourhood atoms through two
 // shared-memory tiles, the next one copied asynchronously while the current
 // one is evaluated.
-template <int R>
-__global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
+//
+// MULTI: the items of several trajectories in one launch (Cs, item_end in
+// device memory, the current trajectory's record copied to shared memory);
+// otherwise one trajectory whose record Cp stays in the kernel parameters,
+// which instructions read directly (no registers held for them).
+template <int R, bool MULTI>
+__global__ void __launch_bounds__(NT, 2)
+    k_pairs_cell(const CellLaunch Cp, const CellLaunch *__restrict__ Cs,
+                 const long long *__restrict__ item_end, int nmem, int win_cap, int hist_cap)
 {
     constexpr int TI = NT * R;
     extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ CellLaunch sC;  // the trajectory of the current items (MULTI)
+    const CellLaunch &C = MULTI ? sC : Cp;
     const PairLaunch &P = C.pair;
     unsigned *jbuf = reinterpret_cast<unsigned *>(smem);          // [2][x|y|z|id-type][TJ]
     uint2 *slots = reinterpret_cast<uint2 *>(jbuf + 2 * 4 * TJ);  // [SLOTS][NT]
     uint4 *rq = reinterpret_cast<uint4 *>(slots + SLOTS * NT);    // [QCAP]
-    float2 *win = reinterpret_cast<float2 *>(rq + QCAP);          // [nbin]
-    unsigned *hist = reinterpret_cast<unsigned *>(win + P.nbin);  // [nch][nbin]
-    unsigned short *chtab = reinterpret_cast<unsigned short *>(hist + P.nch * P.nbin);
+    float2 *win = reinterpret_cast<float2 *>(rq + QCAP);          // [win_cap]
+    unsigned *hist = reinterpret_cast<unsigned *>(win + win_cap); // [hist_cap]
+    unsigned short *chtab = reinterpret_cast<unsigned short *>(hist + hist_cap);
     __shared__ Range irg[MAXR], jrg[MAXR];
     __shared__ int ipre[MAXR + 1], jpre[MAXR + 1];
     __shared__ int nir, njr, rqn;
 
-    const int tid = threadIdx.x;
-    const int hlen = P.nch * P.nbin;
-    const int half = P.nch / 2;
-    for (int i = tid; i < P.nbin; i += NT) win[i] = P.win[i];
-    for (int i = tid; i < hlen; i += NT) hist[i] = 0u;
-    for (int i = tid; i < P.ntypes * P.ntypes; i += NT) chtab[i] = P.chtab[i];
-    if (tid == 0) rqn = 0;
-    __syncthreads();
+    // the current trajectory's item range (kept in shared memory: the pair
+    // loop needs every register)
+    __shared__ long long s_begin, s_end;
+    __shared__ int s_m;
 
-    const int nbx = C.nb[0], nby = C.nb[1], nbz = C.nb[2];
-    const long long nblocks = (long long)nbx * nby * nbz;
-    const long long per_lag = nblocks * P.n_orig;
-    const long long NP = P.NP;
-    const int ncell = C.nc[0] * C.nc[1] * C.nc[2];
-    const float hi_f = P.hi_f;
+    const int tid = threadIdx.x;
     float L32[3];
     int cur_lag = -1;
     long long pairs_since = 0;
     unsigned long long n_cand = 0, n_rech = 0, n_eval = 0;
     uint2 *const my_slots = slots + tid;
+    const long long total = MULTI ? (nmem > 0 ? item_end[nmem - 1] : 0) : Cp.pair.n_items;
+    if (tid == 0) {
+        s_m = -1;
+        s_begin = 0;
+        s_end = MULTI ? 0 : total;
+    }
+    if (!MULTI) {
+        for (int i = tid; i < P.nbin; i += NT) win[i] = P.win[i];
+        for (int i = tid; i < P.nch * P.nbin; i += NT) hist[i] = 0u;
+        for (int i = tid; i < P.ntypes * P.ntypes; i += NT) chtab[i] = P.chtab[i];
+        if (tid == 0) rqn = 0;
+    }
+    __syncthreads();
 
-    for (long long item = blockIdx.x; item < P.n_items; item += gridDim.x) {
+    // adds the shared histogram of the current (trajectory, lag) to its counts
+    auto flush_hist = [&]() {
+        const int hlen = P.nch * P.nbin;
+        for (int i = tid; i < hlen; i += NT) {
+            const unsigned v = hist[i];
+            if (v) {
+                atomicAdd(P.counts + (long long)cur_lag * P.every * hlen + i, (unsigned long long)v);
+                hist[i] = 0u;
+            }
+        }
+    };
+
+    for (long long g = blockIdx.x; g < total; g += gridDim.x) {
+        if (MULTI && g >= s_end) {  // next trajectory (the same decision in every thread)
+            __syncthreads();
+            if (cur_lag >= 0) flush_hist();
+            __syncthreads();
+            if (tid == 0) {
+                int m = s_m;
+                long long b = s_begin, e = s_end;
+                while (g >= e) {
+                    ++m;
+                    b = e;
+                    e = item_end[m];
+                }
+                s_m = m;
+                s_begin = b;
+                s_end = e;
+            }
+            __syncthreads();
+            {
+                const int *src = reinterpret_cast<const int *>(Cs + s_m);
+                int *dst = reinterpret_cast<int *>(&sC);
+                for (int i = tid; i < (int)(sizeof(CellLaunch) / sizeof(int)); i += NT) dst[i] = src[i];
+            }
+            __syncthreads();
+            for (int i = tid; i < P.nbin; i += NT) win[i] = P.win[i];
+            for (int i = tid; i < P.nch * P.nbin; i += NT) hist[i] = 0u;
+            for (int i = tid; i < P.ntypes * P.ntypes; i += NT) chtab[i] = P.chtab[i];
+            if (tid == 0) rqn = 0;
+            cur_lag = -1;
+            pairs_since = 0;
+            __syncthreads();
+        }
+        const long long item = MULTI ? g - s_begin : g;
+        const int nbx = C.nb[0], nby = C.nb[1], nbz = C.nb[2];
+        const long long nblocks = (long long)nbx * nby * nbz;
+        const long long per_lag = nblocks * P.n_orig;
+        const long long NP = P.NP;
+        const int ncell = C.nc[0] * C.nc[1] * C.nc[2];
+        const float hi_f = P.hi_f;
+        const int half = P.nch / 2;
         const int lag_idx = (int)(item / per_lag);
         const long long rem = item - (long long)lag_idx * per_lag;
         const int k = (int)(rem / nblocks);
@@ -322,14 +386,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
             const long long pairs_item = (long long)ipre[nir] * jpre[njr];
             if (lag_idx != cur_lag || pairs_since + pairs_item >= (1ll << 31)) {
                 if (cur_lag >= 0) {
-                    for (int i = tid; i < hlen; i += NT) {
-                        const unsigned v = hist[i];
-                        if (v) {
-                            atomicAdd(P.counts + (long long)cur_lag * P.every * hlen + i,
-                                      (unsigned long long)v);
-                            hist[i] = 0u;
-                        }
-                    }
+                    flush_hist();
                     __syncthreads();
                 }
                 cur_lag = lag_idx;
@@ -538,10 +595,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cell(const CellLaunch C)
     }
     if (cur_lag >= 0) {
         __syncthreads();
-        for (int i = tid; i < hlen; i += NT) {
-            const unsigned v = hist[i];
-            if (v) atomicAdd(P.counts + (long long)cur_lag * P.every * hlen + i, (unsigned long long)v);
-        }
+        flush_hist();
     }
     for (int o = 16; o > 0; o >>= 1) {
         n_cand += __shfl_xor_sync(0xffffffffu, n_cand, o);
@@ -594,34 +648,86 @@ int launch_cell_build(const double *pos64, const unsigned char *types8, size_t T
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-template <int R>
-static int launch_cell_r(const CellLaunch &C, int num_sms, cudaStream_t s)
+template <int R, bool MULTI>
+static int launch_cell_r(const CellLaunch &C, const CellLaunch *d_cells, const long long *d_end,
+                         int nmem, long long total, int max_nbin, int max_nch, int max_ntypes,
+                         int num_sms, cudaStream_t s)
 {
     using namespace cells;
-    const int smem = cell_smem_bytes(C.pair.nch, C.pair.nbin, C.pair.ntypes);
-    if (cudaFuncSetAttribute(k_pairs_cell<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
-        cudaSuccess)
+    const int smem = cell_smem_bytes(max_nch, max_nbin, max_ntypes);
+    if (cudaFuncSetAttribute(k_pairs_cell<R, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess)
         return -1;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairs_cell<R>, NT, smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairs_cell<R, MULTI>, NT, smem) !=
         cudaSuccess)
         return -1;
     if (per_sm < 1) return -2;
     long long grid = (long long)num_sms * per_sm;
-    if (grid > C.pair.n_items) grid = C.pair.n_items;
-    k_pairs_cell<R><<<(unsigned)grid, NT, smem, s>>>(C);
+    if (grid > total) grid = total;
+    k_pairs_cell<R, MULTI><<<(unsigned)grid, NT, smem, s>>>(C, d_cells, d_end, nmem, max_nbin,
+                                                             max_nch * max_nbin);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 int launch_cell_pairs(const CellLaunch &C, int num_sms, cudaStream_t s)
 {
-    if (C.pair.n_items <= 0) return 0;
+    const long long total = C.pair.n_items;
+    if (total <= 0) return 0;
+    const int nb = C.pair.nbin, nc = C.pair.nch, nt = C.pair.ntypes;
     switch (C.r) {
-    case 2: return launch_cell_r<2>(C, num_sms, s);
-    case 3: return launch_cell_r<3>(C, num_sms, s);
-    case 4: return launch_cell_r<4>(C, num_sms, s);
+    case 2: return launch_cell_r<2, false>(C, nullptr, nullptr, 1, total, nb, nc, nt, num_sms, s);
+    case 3: return launch_cell_r<3, false>(C, nullptr, nullptr, 1, total, nb, nc, nt, num_sms, s);
+    case 4: return launch_cell_r<4, false>(C, nullptr, nullptr, 1, total, nb, nc, nt, num_sms, s);
     default: return -3;
     }
+}
+
+template <int R>
+static int prepare_multi_r(int smem, int num_sms, long long total, int *grid)
+{
+    using namespace cells;
+    if (cudaFuncSetAttribute(k_pairs_cell<R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess)
+        return -1;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairs_cell<R, true>, NT, smem) !=
+        cudaSuccess)
+        return -1;
+    if (per_sm < 1) return -2;
+    long long g = (long long)num_sms * per_sm;
+    if (g > total) g = total;
+    *grid = (int)g;
+    return 0;
+}
+
+int prepare_cell_pairs_multi(int r, int max_nbin, int max_nch, int max_ntypes, int num_sms,
+                             long long total, int *grid)
+{
+    const int smem = cell_smem_bytes(max_nch, max_nbin, max_ntypes);
+    switch (r) {
+    case 2: return prepare_multi_r<2>(smem, num_sms, total, grid);
+    case 3: return prepare_multi_r<3>(smem, num_sms, total, grid);
+    case 4: return prepare_multi_r<4>(smem, num_sms, total, grid);
+    default: return -3;
+    }
+}
+
+int launch_cell_pairs_multi(const CellLaunch *d_cells, const long long *d_end, int nmem,
+                            int r, int max_nbin, int max_nch, int max_ntypes, int grid,
+                            cudaStream_t s)
+{
+    using namespace cells;
+    if (grid <= 0 || nmem <= 0) return 0;
+    const int smem = cell_smem_bytes(max_nch, max_nbin, max_ntypes);
+    const CellLaunch none{};
+    switch (r) {
+    case 2: k_pairs_cell<2, true><<<grid, NT, smem, s>>>(none, d_cells, d_end, nmem, max_nbin, max_nch * max_nbin); break;
+    case 3: k_pairs_cell<3, true><<<grid, NT, smem, s>>>(none, d_cells, d_end, nmem, max_nbin, max_nch * max_nbin); break;
+    case 4: k_pairs_cell<4, true><<<grid, NT, smem, s>>>(none, d_cells, d_end, nmem, max_nbin, max_nch * max_nbin); break;
+    default: return -3;
+    }
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace gofr

@@ -127,7 +127,17 @@ int launch_cell_build(const double *pos64, const unsigned char *types8, size_t T
                       const double *box_internal, const double *centre, const int *nc,
                       int *cell_of, int *rank_of, int *count, int *start, float *spos,
                       unsigned *sidt, cudaStream_t s);
+// One trajectory's cell-list items in one launch.
 int launch_cell_pairs(const CellLaunch &C, int num_sms, cudaStream_t s);
+// One launch over the items of nmem trajectories: Cs[m] (device) holds
+// trajectory m's parameters, item_end[m] (device) the end of its items in the
+// global item order; shared memory is sized for the largest histogram.
+// prepare_* sets the kernel attributes and the grid (outside graph capture).
+int prepare_cell_pairs_multi(int r, int max_nbin, int max_nch, int max_ntypes, int num_sms,
+                             long long total, int *grid);
+int launch_cell_pairs_multi(const CellLaunch *d_cells, const long long *d_end, int nmem,
+                            int r, int max_nbin, int max_nch, int max_ntypes, int grid,
+                            cudaStream_t s);
 
 // Launch configuration helpers implemented in gofr_kernels.cu.
 int launch_minmax(const double *pos64, size_t n3, double *d_out6, unsigned *d_nonfinite,
