@@ -4,11 +4,10 @@
 // The reference loops lag -> origin -> atom and keeps, per (lag, type), a
 // running mean of |x_i(o) - x_i(o+t)|^2 (optionally minus the type's
 // centre-of-mass displacement), and of the centres' own squared displacement.
-// Here every (origin, lag) item is one CTA: it forms each atom's squared
-// displacement with the reference's FP64 operations (pow(d, 2) = d*d, summed
-// x, y, z in that order), sums the atoms of each type (atoms visited in
-// type-sorted order, one block reduction per type) and writes one partial
-// sum per (lag, origin, type).  A second kernel adds the origins of each
+// Here every (origin, lag) item is one CTA: it forms each atom's displacement
+// with the reference's FP64 operations, adds its squared components into the
+// type's sum with FMAs (atoms visited in type-sorted order, one block
+// reduction per type) and writes one partial sum per (lag, origin, type).  A second kernel adds the origins of each
 // (lag, type) in a fixed order and divides by the count.  Items are ordered
 // origin-major so that consecutive CTAs share the origin frame and slide the
 // lagged frame, which keeps the frames they read in L2.
@@ -74,7 +73,10 @@ __global__ void __launch_bounds__(NT) k_msd_partial(const MsdLaunch M)
                     dy = __dsub_rn(dy, cy);
                     dz = __dsub_rn(dz, cz);
                 }
-                acc = __dadd_rn(acc, sq3(dx, dy, dz));
+                // the squares go straight into the sum (three FMAs instead of
+                // three products, two additions and one accumulation: the
+                // kernel is bound by the FP64 pipe)
+                acc = __fma_rn(dz, dz, __fma_rn(dy, dy, __fma_rn(dx, dx, acc)));
             }
             const double s = block_sum(acc, red);
             if (threadIdx.x == 0) out[k] = s;

@@ -9,8 +9,10 @@
 // the higher-index atom, as the reference stores -x), and the counted entries
 // of each neighbour type are placed by a ballot prefix, which keeps the
 // ascending order.  Where the all-pairs kernel's FP32 bound certifies it, an
-// FP32 minimum-image d2 first discards the pairs beyond every cutoff, so the
-// FP64 arithmetic runs only for the few near pairs.  Overflow follows the reference's rule exactly: a pair
+// FP32 minimum-image d2 first discards the pairs beyond every cutoff; the
+// remaining candidates are queued in shared memory (ascending) and their FP64
+// arithmetic runs 32 at a time, one per lane, so the slow FP64 pipe works only
+// on full warps of near pairs.  Overflow follows the reference's rule exactly: a pair
 // (i < j) within either cutoff is an error when, at that point of the
 // reference's loop, i's list of j's type or j's list of i's type is full;
 // with full[a][k] = the neighbour index that filled a's list of type k, that
@@ -86,6 +88,7 @@ template <bool TRI>
 __global__ void __launch_bounds__(NT) k_neigh_build(const NeighLaunch L)
 {
     __shared__ unsigned long long cnt[WARPS][NEIGH_MAXT];
+    __shared__ int cq[WARPS][64];  // candidates of this warp's atom, ascending
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const double *frame = L.pos64 + (size_t)L.timestep * L.N * 3;
     const double *box = L.box64 + (size_t)L.timestep * 9;
@@ -93,22 +96,21 @@ __global__ void __launch_bounds__(NT) k_neigh_build(const NeighLaunch L)
     for (long long a0 = (long long)blockIdx.x * WARPS; a0 < L.N; a0 += (long long)gridDim.x * WARPS) {
         const int a = (int)(a0 + w);
         if (a >= L.N) continue;  // warp-uniform
-        const int ta = L.types[a];
         for (int k = lane; k < L.ntypes; k += 32) {
             cnt[w][k] = 0ull;
             // a list of capacity 0 is full before its first neighbour
             L.full[(size_t)a * L.ntypes + k] = L.nneigh[k] == 0 ? -1 : L.N;
         }
         __syncwarp();
-        for (int b0 = 0; b0 < L.N; b0 += 32) {
-            const int b = b0 + lane;
-            const bool valid = b < L.N && b != a;
+        // FP64 arithmetic and placement of the first n queued candidates, one
+        // per lane, in ascending order
+        auto place = [&](int n) {
+            const bool have = lane < n;
+            const int b = have ? cq[w][lane] : 0;
             int tb = 0;
             double x[3] = {0.0, 0.0, 0.0}, d2 = 0.0;
             bool counted = false;
-            if (valid && L.prefilter && !(pair_f32<TRI>(L, a, b) <= L.hi_f)) {
-                // certainly beyond every cutoff: neither counted nor a candidate
-            } else if (valid) {
+            if (have) {
                 tb = L.types[b];
                 const int i = a < b ? a : b, j = a < b ? b : a;
                 d2 = pair_vec<TRI>(L, frame, box, i, j, x);
@@ -136,7 +138,28 @@ __global__ void __launch_bounds__(NT) k_neigh_build(const NeighLaunch L)
                 if (lane == 0) cnt[w][k] = base + __popc(m);
                 __syncwarp();
             }
+        };
+        int qn = 0;  // queued candidates (warp-uniform)
+        for (int b0 = 0; b0 < L.N; b0 += 32) {
+            const int b = b0 + lane;
+            bool cand = b < L.N && b != a;
+            if (cand && L.prefilter) cand = pair_f32<TRI>(L, a, b) <= L.hi_f;
+            const unsigned m = __ballot_sync(0xffffffffu, cand);
+            if (!m) continue;
+            if (cand) cq[w][qn + __popc(m & lt)] = b;
+            qn += __popc(m);
+            __syncwarp();
+            if (qn >= 32) {
+                place(32);
+                const int rest = qn - 32;
+                const int v = lane < rest ? cq[w][32 + lane] : 0;
+                __syncwarp();
+                if (lane < rest) cq[w][lane] = v;
+                __syncwarp();
+                qn = rest;
+            }
         }
+        if (qn > 0) place(qn);
         for (int k = lane; k < L.ntypes; k += 32) {
             const unsigned long long c = cnt[w][k], nk = L.nneigh[k];
             L.list[L.loff[k] + (size_t)a * (nk + 1)] = c < nk ? c : nk;

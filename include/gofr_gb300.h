@@ -272,10 +272,11 @@ int gofr_msd_output_size(const gofr_ctx *ctx, const gofr_msd_params *p, size_t *
  * result [leff][f_cm][ntypes] to out_host (double).  Element (t, 0, k) is the
  * mean over origins and atoms of type k of |x(o) - x(o+t)|^2 (optionally
  * minus the type's centre-of-mass displacement); (t, 1, k) the mean over
- * origins of the centre-of-mass |cm_k(o) - cm_k(o+t)|^2.  Each squared
- * displacement is the reference's FP64 value; the means are FP64 sums in a
- * fixed order divided by the count, where the reference keeps a running mean:
- * the two agree to rounding (relative ~1e-13 for 1e7 terms).  Errors as
+ * origins of the centre-of-mass |cm_k(o) - cm_k(o+t)|^2.  Each displacement is
+ * the reference's FP64 value; its squared components are added into FP64 sums
+ * (fused multiply-adds, a fixed order) divided by the count, where the
+ * reference keeps a running mean: the two agree to rounding (relative ~1e-13
+ * for 1e7 terms).  Errors as
  * lib/src/msd.cpp:57-68 (GOFR_ERR_RANGE: trajectory too short). */
 int gofr_msd_run(gofr_ctx *ctx, const gofr_msd_params *p, double *out_host);
 
