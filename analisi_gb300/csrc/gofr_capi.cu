@@ -153,6 +153,21 @@ int fail(gofr_ctx *ctx, int code, const char *fmt, ...)
                         "%s failed: %s", #call, cudaGetErrorString(e_));                     \
     } while (0)
 
+// Every device allocation of this file goes through here.  Fault-injection
+// hook for tests: with ANALISI_GB300_FAIL_ALLOC=1 in the environment every
+// allocation fails as if the device were out of memory (the error path must
+// leave the context usable).
+template <class T>
+cudaError_t dev_malloc(T **p, size_t bytes)
+{
+    const char *e = std::getenv("ANALISI_GB300_FAIL_ALLOC");
+    if (e && e[0] == '1') {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(reinterpret_cast<void **>(p), bytes);
+}
+
 struct DevGuard {
     int prev = -1;
     explicit DevGuard(int d)
@@ -174,7 +189,7 @@ int ensure(gofr_ctx *ctx, T *&p, size_t &cap, size_t n)
     p = nullptr;
     cap = 0;
     size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
-    CK(cudaMalloc(reinterpret_cast<void **>(&p), bytes));
+    CK(dev_malloc(&p, bytes));
     cap = n;
     return GOFR_OK;
 }
@@ -522,13 +537,13 @@ int upload_traj(gofr_ctx *ctx, TrajDev &t, const double *positions, const double
         t.box_constant = std::memcmp(&t.h_box[f * 9], &t.h_box[0], 9 * sizeof(double)) == 0;
     free_traj(t);
     const size_t n3 = nframes * natoms * 3;
-    CK(cudaMalloc(&t.pos64, n3 * sizeof(double)));
+    CK(dev_malloc(&t.pos64, n3 * sizeof(double)));
     const size_t NP = padded_natoms(natoms);
-    CK(cudaMalloc(&t.pos32, nframes * 3 * NP * sizeof(float)));
-    CK(cudaMalloc(&t.types8, NP));
-    CK(cudaMalloc(&t.box64, nframes * 9 * sizeof(double)));
-    CK(cudaMalloc(&t.box32, nframes * sizeof(Box32)));
-    CK(cudaMalloc(&t.types, natoms * sizeof(int)));
+    CK(dev_malloc(&t.pos32, nframes * 3 * NP * sizeof(float)));
+    CK(dev_malloc(&t.types8, NP));
+    CK(dev_malloc(&t.box64, nframes * 9 * sizeof(double)));
+    CK(dev_malloc(&t.box32, nframes * sizeof(Box32)));
+    CK(dev_malloc(&t.types, natoms * sizeof(int)));
     CK(cudaMemcpyAsync(t.pos64, positions, n3 * sizeof(double), cudaMemcpyHostToDevice,
                        ctx->stream));
     CK(cudaMemcpyAsync(t.box64, t.h_box.data(), nframes * 9 * sizeof(double),
@@ -547,8 +562,8 @@ int upload_traj(gofr_ctx *ctx, TrajDev &t, const double *positions, const double
         std::vector<int> fill(t.h_tbegin.begin(), t.h_tbegin.end() - 1);
         for (size_t a = 0; a < natoms; ++a) t.h_perm[fill[type_ids[a]]++] = (int)a;
     }
-    CK(cudaMalloc(&t.d_perm, natoms * sizeof(int)));
-    CK(cudaMalloc(&t.d_tbegin, (ntypes + 1) * sizeof(int)));
+    CK(dev_malloc(&t.d_perm, natoms * sizeof(int)));
+    CK(dev_malloc(&t.d_tbegin, (ntypes + 1) * sizeof(int)));
     CK(cudaMemcpyAsync(t.d_perm, t.h_perm.data(), natoms * sizeof(int), cudaMemcpyHostToDevice,
                        ctx->stream));
     CK(cudaMemcpyAsync(t.d_tbegin, t.h_tbegin.data(), (ntypes + 1) * sizeof(int),
@@ -844,12 +859,12 @@ int ensure_cells(gofr_ctx *ctx, const TrajDev &t, const Plan &pl)
     const size_t ncell = (size_t)pl.nc[0] * pl.nc[1] * pl.nc[2];
     const size_t NP = padded_natoms(t.N);
     int *cell_of = nullptr, *rank_of = nullptr, *count = nullptr;
-    CK(cudaMalloc(&tm.d_cstart, t.T * (ncell + 1) * sizeof(int)));
-    CK(cudaMalloc(&tm.d_sidt, t.T * NP * sizeof(unsigned)));
-    CK(cudaMalloc(&tm.d_spos, t.T * 3 * NP * sizeof(float)));
-    CK(cudaMalloc(&cell_of, t.T * t.N * sizeof(int)));
-    CK(cudaMalloc(&rank_of, t.T * t.N * sizeof(int)));
-    CK(cudaMalloc(&count, t.T * (ncell + 1) * sizeof(int)));
+    CK(dev_malloc(&tm.d_cstart, t.T * (ncell + 1) * sizeof(int)));
+    CK(dev_malloc(&tm.d_sidt, t.T * NP * sizeof(unsigned)));
+    CK(dev_malloc(&tm.d_spos, t.T * 3 * NP * sizeof(float)));
+    CK(dev_malloc(&cell_of, t.T * t.N * sizeof(int)));
+    CK(dev_malloc(&rank_of, t.T * t.N * sizeof(int)));
+    CK(dev_malloc(&count, t.T * (ncell + 1) * sizeof(int)));
     ctx->launches += 3;
     double centre[3];
     for (int k = 0; k < 3; ++k) centre[k] = t.h_box[k] + t.h_box[3 + k];  // xlo + L/2
@@ -1326,8 +1341,8 @@ int build_batch(gofr_ctx *ctx)
     }
     std::stable_sort(all.begin(), all.end(), [](const Cost &a, const Cost &b) { return a.c > b.c; });
     for (auto &c : all) B.work[c.tri ? 1 : 0].push_back(c.w);
-    CK(cudaMalloc(&B.d_win, std::max<size_t>(wins.size(), 1) * sizeof(float2)));
-    CK(cudaMalloc(&B.d_chtab, std::max<size_t>(tabs.size(), 1) * sizeof(unsigned short)));
+    CK(dev_malloc(&B.d_win, std::max<size_t>(wins.size(), 1) * sizeof(float2)));
+    CK(dev_malloc(&B.d_chtab, std::max<size_t>(tabs.size(), 1) * sizeof(unsigned short)));
     if (!wins.empty())
         CK(cudaMemcpy(B.d_win, wins.data(), wins.size() * sizeof(float2), cudaMemcpyHostToDevice));
     if (!tabs.empty())
@@ -1395,23 +1410,23 @@ int build_batch(gofr_ctx *ctx)
         B.launches[k] = PairLaunch{};  // not in the all-pairs queue
     }
     if (!B.cells.empty()) {
-        CK(cudaMalloc(&B.d_cells, B.cells.size() * sizeof(CellLaunch)));
-        CK(cudaMalloc(&B.d_cell_end, cell_end.size() * sizeof(long long)));
+        CK(dev_malloc(&B.d_cells, B.cells.size() * sizeof(CellLaunch)));
+        CK(dev_malloc(&B.d_cell_end, cell_end.size() * sizeof(long long)));
         CK(cudaMemcpy(B.d_cells, B.cells.data(), B.cells.size() * sizeof(CellLaunch),
                       cudaMemcpyHostToDevice));
         CK(cudaMemcpy(B.d_cell_end, cell_end.data(), cell_end.size() * sizeof(long long),
                       cudaMemcpyHostToDevice));
     }
-    CK(cudaMalloc(&B.d_launches, std::max<size_t>(B.launches.size(), 1) * sizeof(PairLaunch)));
+    CK(dev_malloc(&B.d_launches, std::max<size_t>(B.launches.size(), 1) * sizeof(PairLaunch)));
     CK(cudaMemcpy(B.d_launches, B.launches.data(), B.launches.size() * sizeof(PairLaunch),
                   cudaMemcpyHostToDevice));
     for (int v = 0; v < 2; ++v) {
         if (B.work[v].empty()) continue;
-        CK(cudaMalloc(&B.d_work[v], B.work[v].size() * sizeof(WorkDesc)));
+        CK(dev_malloc(&B.d_work[v], B.work[v].size() * sizeof(WorkDesc)));
         CK(cudaMemcpy(B.d_work[v], B.work[v].data(), B.work[v].size() * sizeof(WorkDesc),
                       cudaMemcpyHostToDevice));
     }
-    CK(cudaMalloc(&B.d_head, 2 * sizeof(unsigned)));
+    CK(dev_malloc(&B.d_head, 2 * sizeof(unsigned)));
     CK(cudaMallocHost(&B.h_stage, std::max<size_t>(ctx->batch_total, 1) * sizeof(unsigned long long)));
     const int smem = batch_smem_bytes(B.max_nbin, B.max_nch, B.max_ntypes);
     int max_smem = 0;
@@ -1509,10 +1524,10 @@ int gofr_ctx_create(gofr_ctx **out, int device)
         }
         bool ok = true;
         for (auto &e : ctx->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
-        ok = ok && cudaMalloc(&ctx->d_err, sizeof(unsigned)) == cudaSuccess;
-        ok = ok && cudaMalloc(&ctx->d_stats, ST_COUNT * sizeof(unsigned long long)) == cudaSuccess;
-        ok = ok && cudaMalloc(&ctx->d_minmax, 256 * 6 * sizeof(double)) == cudaSuccess;
-        ok = ok && cudaMalloc(&ctx->d_nonfinite, sizeof(unsigned)) == cudaSuccess;
+        ok = ok && dev_malloc(&ctx->d_err, sizeof(unsigned)) == cudaSuccess;
+        ok = ok && dev_malloc(&ctx->d_stats, ST_COUNT * sizeof(unsigned long long)) == cudaSuccess;
+        ok = ok && dev_malloc(&ctx->d_minmax, 256 * 6 * sizeof(double)) == cudaSuccess;
+        ok = ok && dev_malloc(&ctx->d_nonfinite, sizeof(unsigned)) == cudaSuccess;
         if (!ok) rc = GOFR_ERR_CUDA;
     } while (0);
     if (rc) {
@@ -1714,9 +1729,9 @@ int gofr_run_windows(gofr_ctx *ctx, const gofr_params *p, unsigned nwin,
         if (prepare_batch((int)p->nbin, (int)rs.nch, (int)t.ntypes, t.tric != 0, ctx->num_sms,
                           (int)work.size(), &grid))
             return fail(ctx, GOFR_ERR_CUDA, "batched kernel setup failed");
-        CK(cudaMalloc(&d_l, ls.size() * sizeof(PairLaunch)));
-        CK(cudaMalloc(&d_w, std::max<size_t>(work.size(), 1) * sizeof(WorkDesc)));
-        CK(cudaMalloc(&d_head, sizeof(unsigned)));
+        CK(dev_malloc(&d_l, ls.size() * sizeof(PairLaunch)));
+        CK(dev_malloc(&d_w, std::max<size_t>(work.size(), 1) * sizeof(WorkDesc)));
+        CK(dev_malloc(&d_head, sizeof(unsigned)));
         CK(cudaMemcpyAsync(d_l, ls.data(), ls.size() * sizeof(PairLaunch), cudaMemcpyHostToDevice,
                            ctx->stream));
         CK(cudaMemcpyAsync(d_w, work.data(), work.size() * sizeof(WorkDesc),
@@ -1866,7 +1881,7 @@ int gofr_batch_set(gofr_ctx *ctx, const gofr_traj_desc *trajs, unsigned ntraj)
     }
     ctx->batch_total = off;
     int rc = GOFR_OK;
-    if (cudaMalloc(&ctx->batch.d_counts, std::max<size_t>(off, 1) * 8) != cudaSuccess)
+    if (dev_malloc(&ctx->batch.d_counts, std::max<size_t>(off, 1) * 8) != cudaSuccess)
         rc = fail(ctx, GOFR_ERR_NOMEM, "cannot allocate the batch counts");
     if (rc == GOFR_OK) rc = build_batch(ctx);
     if (rc) {
@@ -1953,7 +1968,7 @@ int gofr_set_centres(gofr_ctx *ctx, const double *centres, size_t nframes, unsig
     cudaFree(t.d_cm);
     t.d_cm = nullptr;
     const size_t n = nframes * ntypes * 3;
-    CK(cudaMalloc(&t.d_cm, n * sizeof(double)));
+    CK(dev_malloc(&t.d_cm, n * sizeof(double)));
     CK(cudaMemcpyAsync(t.d_cm, centres, n * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return GOFR_OK;

@@ -1,0 +1,73 @@
+"""Failure paths of the C ABI, injected on the host (no GPU fault): device
+allocations made to fail through the ANALISI_GB300_FAIL_ALLOC hook return
+GOFR_ERR_NOMEM with a message, leak nothing the context keeps, and leave the
+context usable: the next call without the hook gives the oracle's counts."""
+import numpy as np
+import pytest
+
+from analisi_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _case():
+    return workloads.small_case(91, 600, 8, 16.0, 0.2, [400, 200], rmin=0.0, rmax=5.0, nbin=50,
+                                tmax=3, skip=2, every=1, ntimesteps=4, primo=0)
+
+
+def test_context_creation_failure_is_clean(built_engine, monkeypatch):
+    from analisi_gb300 import engine
+    monkeypatch.setenv("ANALISI_GB300_FAIL_ALLOC", "1")
+    with pytest.raises(engine.GofrError):
+        engine.Engine(0)
+    monkeypatch.delenv("ANALISI_GB300_FAIL_ALLOC")
+    with engine.Engine(0):
+        pass
+
+
+def test_upload_and_run_failures_leave_context_usable(built_engine, oracle_mod, monkeypatch):
+    from analisi_gb300 import engine
+    w = _case()
+    p = w["params"]
+    ref = oracle_mod.gofrt_counts(w["positions"], w["boxes"], w["type_ids"], w["ntypes"],
+                                  p["rmin"], p["rmax"], p["nbin"], p["tmax"], 1, p["skip"],
+                                  p["every"], p["ntimesteps"], p["primo"])
+    with engine.Engine(0) as e:
+        monkeypatch.setenv("ANALISI_GB300_FAIL_ALLOC", "1")
+        with pytest.raises(engine.GofrError) as err:
+            e.set_frames(w["positions"], w["boxes"], w["type_ids"], w["ntypes"])
+        assert err.value.code == -4 and "memory" in str(err.value)
+        with pytest.raises(engine.GofrError):  # nothing uploaded: a state error
+            e.run(p["rmin"], p["rmax"], p["nbin"], p["tmax"], p["skip"], 1, p["ntimesteps"], 0)
+        monkeypatch.delenv("ANALISI_GB300_FAIL_ALLOC")
+        e.set_frames(w["positions"], w["boxes"], w["type_ids"], w["ntypes"])
+        # the counts buffer is allocated at the first run: make that one fail
+        monkeypatch.setenv("ANALISI_GB300_FAIL_ALLOC", "1")
+        with pytest.raises(engine.GofrError) as err:
+            e.run(p["rmin"], p["rmax"], p["nbin"], p["tmax"], p["skip"], 1, p["ntimesteps"], 0)
+        assert err.value.code == -4
+        monkeypatch.delenv("ANALISI_GB300_FAIL_ALLOC")
+        got = e.run(p["rmin"], p["rmax"], p["nbin"], p["tmax"], p["skip"], 1, p["ntimesteps"], 0)
+        np.testing.assert_array_equal(got, ref)
+
+
+def test_msd_and_neighbour_allocation_failures(built_engine, oracle_mod, monkeypatch):
+    from analisi_gb300 import engine
+    w = _case()
+    with engine.Engine(0) as e:
+        e.set_frames(w["positions"], w["boxes"], w["type_ids"], w["ntypes"])
+        monkeypatch.setenv("ANALISI_GB300_FAIL_ALLOC", "1")
+        with pytest.raises(engine.GofrError) as err:
+            e.msd(1, 3, 4, 0)
+        assert err.value.code == -4
+        with pytest.raises(engine.GofrError) as err:
+            e.neighbours(0, [(40, 9.0, 10.0), (40, 9.0, 10.0)], True)
+        assert err.value.code == -4
+        monkeypatch.delenv("ANALISI_GB300_FAIL_ALLOC")
+        ref = oracle_mod.msd(w["positions"], w["type_ids"], w["ntypes"], 1, 3, 4, 0)
+        np.testing.assert_allclose(e.msd(1, 3, 4, 0), ref, rtol=1e-12, atol=0)
+        o = oracle_mod.neighbours(w["positions"], w["boxes"], w["type_ids"], w["ntypes"], 0,
+                                  [(40, 9.0, 10.0), (40, 9.0, 10.0)], True)
+        nl = e.neighbours(0, [(40, 9.0, 10.0), (40, 9.0, 10.0)], True)
+        for a in range(0, 600, 13):
+            np.testing.assert_array_equal(nl.idx(a, 1), o.idx(a, 1))
