@@ -78,3 +78,46 @@ def test_cli_matches_reference_block_average(built_engine, oracle_mod, tmp_path,
     want = expected_output(oracle_mod, pos_int, boxes_int, tids, nt, rmin, rmax, nbin, tmax, nth,
                            skip, every, B, tric)
     assert body[:len(want)] == want
+
+
+@pytest.mark.parametrize("flag", ["-q", "-Q", "--mean-square-displacement-self"])
+def test_cli_msd_matches_reference_block_average(built_engine, oracle_mod, tmp_path, flag):
+    """`analisi -q/-Q/--mean-square-displacement-self`: block averages of MSD as
+    analisi/main.cpp:520-551 prints them (mean and variance per type, and per
+    type's centre of mass with -Q), against the oracle's running means fed to
+    the same MediaVar recurrence; printed with 6 significant digits."""
+    from analisi_gb300 import build, workloads
+    build.build_host()
+    rng = np.random.default_rng(91)
+    T, N, L = 50, 120, 10.0
+    pos = np.cumsum(np.concatenate([rng.uniform(0, L, (1, N, 3)),
+                                    rng.normal(0, 0.3, (T - 1, N, 3))]), axis=0)
+    types = rng.choice([2, 6, 4], N).astype(np.int32)
+    boxes = np.tile([0, L, 0, L, 0, L], (T, 1)).astype(float)
+    path = str(tmp_path / "traj.bin")
+    lammps_writer.write(path, pos, types, boxes, triclinic=False, nchunk=3)
+    tmax, skip, nth, B = 6, 2, 2, 5
+    out = subprocess.run([CLI, "-i", path, flag, "-S", str(tmax), "-s", str(skip), "-N", str(nth),
+                          "-B", str(B)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    got = np.array([[float(v) for v in l.split()] for l in out.stdout.strip().split("\n")])
+    cm_msd, cm_self = flag == "-Q", flag == "--mean-square-displacement-self"
+    tids, nt = workloads.dense_type_ids(types)
+    cm = oracle_mod.centres(pos, tids, nt)
+    n_extra = T // (B + 1) + 1
+    if not (n_extra < tmax or tmax == 0):
+        n_extra = tmax
+    s = (T - n_extra) // B
+    mean = var = None
+    for ib in range(B):
+        calc = oracle_mod.msd(pos, tids, nt, skip, tmax, s, ib * s, cm_msd, cm_self, cm=cm)
+        if mean is None:
+            mean, var = np.zeros_like(calc), np.zeros_like(calc)
+        delta = calc - mean
+        mean = mean + delta / (ib + 1)
+        var = var + (calc - mean) * delta
+    var = var / ((B - 1) * B)
+    want = np.stack([mean.reshape(mean.shape[0], -1), var.reshape(var.shape[0], -1)],
+                    axis=-1).reshape(mean.shape[0], -1)
+    assert got.shape == want.shape
+    np.testing.assert_allclose(got, want, rtol=2e-5, atol=1e-12)
