@@ -8,6 +8,8 @@ Produces, under analisi_gb300/_build/:
   pyanalisi*.so      the pybind11 module with the reference's Gofrt /
                      Trajectory / BoxFormat API, linked against libgofr_gb300
   analisi            the command-line front end (-g/-F options)
+and, on request (build_engine(debug_bounds=True)), analisi_gb300/_build_debug/
+libgofr_gb300.so with the GOFR_DEBUG_BOUNDS device-side index checks.
 
 Translation units are compiled in parallel; nothing here needs cmake.
 Host code is compiled with -ffp-contract=off so that the host-side bin
@@ -25,6 +27,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 HOST = os.path.join(HERE, "host")
 OUT = os.path.join(HERE, "_build")
+OUT_DEBUG = os.path.join(HERE, "_build_debug")
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -65,22 +68,26 @@ def _deps_cuda():
     return files + [os.path.join(INCLUDE, "gofr_gb300.h")]
 
 
-def build_engine(force=False, jobs=None):
-    """Compile the CUDA engine into analisi_gb300/_build/libgofr_gb300.so."""
-    os.makedirs(OUT, exist_ok=True)
-    lib = os.path.join(OUT, LIB_NAME)
+def build_engine(force=False, jobs=None, debug_bounds=False):
+    """Compile the CUDA engine into analisi_gb300/_build/libgofr_gb300.so, or
+    with debug_bounds the GOFR_DEBUG_BOUNDS variant (device-side index checks
+    that set an error word) into analisi_gb300/_build_debug/."""
+    out = OUT_DEBUG if debug_bounds else OUT
+    os.makedirs(out, exist_ok=True)
+    lib = os.path.join(out, LIB_NAME)
     deps = _deps_cuda()
     if not force and not _stale(lib, deps):
         return lib
     nv = nvcc()
+    extra = ["-DGOFR_DEBUG_BOUNDS"] if debug_bounds else []
     objs = []
     cmds = []
     for src in CU_SOURCES:
-        obj = os.path.join(OUT, src.replace(".cu", ".o"))
+        obj = os.path.join(out, src.replace(".cu", ".o"))
         objs.append(obj)
-        cmds.append(([nv] + ARCH + NVCC_FLAGS + ["-I", INCLUDE, "-I", CSRC, "-c",
+        cmds.append(([nv] + ARCH + NVCC_FLAGS + extra + ["-I", INCLUDE, "-I", CSRC, "-c",
                       os.path.join(CSRC, src), "-o", obj],
-                     os.path.join(OUT, src.replace(".cu", ".ptxas.log"))))
+                     os.path.join(out, src.replace(".cu", ".ptxas.log"))))
     with cf.ThreadPoolExecutor(max_workers=jobs or len(cmds)) as ex:
         list(ex.map(lambda c: _run(*c), cmds))
     _run([nv] + ARCH + ["-shared", "-o", lib + ".tmp"] + objs)

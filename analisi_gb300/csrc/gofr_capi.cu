@@ -840,10 +840,11 @@ int check_device_error(gofr_ctx *ctx)
     CK(cudaMemcpyAsync(&e, ctx->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     if (e)
-        return fail(ctx, GOFR_ERR_DEVICE, "kernel reported error word 0x%x (%s%s%s)", e,
+        return fail(ctx, GOFR_ERR_DEVICE, "kernel reported error word 0x%x (%s%s%s%s)", e,
                     (e & ERRW_WAIT_TIMEOUT) ? "bounded wait ran out " : "",
                     (e & ERRW_WRAP_LOOP) ? "minimum-image iteration cap " : "",
-                    (e & ERRW_QUEUE) ? "work queue overflow" : "");
+                    (e & ERRW_QUEUE) ? "work queue overflow " : "",
+                    (e & ERRW_BOUNDS) ? "debug bounds check failed" : "");
     return GOFR_OK;
 }
 

@@ -374,6 +374,7 @@ __global__ void __launch_bounds__(NT, 2)
             const int m = C.reach;
             njr = build_ranges(st_l, C.nc[0], C.nc[1], C.nc[2], cx0 - m, cnx + 2 * m, cy0 - m,
                                cny + 2 * m, cz0 - m, cnz + 2 * m, jrg);
+            if (!GOFR_CHECK(nir <= MAXR && njr <= MAXR, P.err)) nir = njr = 0;
             ipre[0] = 0;
             for (int r = 0; r < nir; ++r) ipre[r + 1] = ipre[r] + (irg[r].end - irg[r].begin);
             jpre[0] = 0;
@@ -528,7 +529,10 @@ __global__ void __launch_bounds__(NT, 2)
                         }
 #pragma unroll
                         for (int u = 0; u < FLUSH_ILP; ++u) {
-                            if (ok[u]) atomicAdd(hist + ch[u] * P.nbin + bi[u], 1u);
+                            if (ok[u] && GOFR_CHECK(ch[u] >= 0 && ch[u] < P.nch && bi[u] >= 0 &&
+                                                        bi[u] < P.nbin,
+                                                    P.err))
+                                atomicAdd(hist + ch[u] * P.nbin + bi[u], 1u);
                             if (need[u]) {
                                 ++n_rech;
                                 const int slot = atomicAdd(&rqn, 1);
@@ -571,6 +575,7 @@ __global__ void __launch_bounds__(NT, 2)
                         if (d1 <= hi_f) { my_slots[cnt * NT] = make_uint2(__float_as_uint(d1), m0 + 4u); ++cnt; }
                         if (d2v <= hi_f) { my_slots[cnt * NT] = make_uint2(__float_as_uint(d2v), m0 + 8u); ++cnt; }
                         if (d3 <= hi_f) { my_slots[cnt * NT] = make_uint2(__float_as_uint(d3), m0 + 12u); ++cnt; }
+                        if (!GOFR_CHECK(cnt <= SLOTS, P.err)) cnt = SLOTS;
                         if (__any_sync(0xffffffffu, cnt > SLOTS - 4)) warp_flush();
                     }
                 }

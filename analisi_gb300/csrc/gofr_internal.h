@@ -11,8 +11,18 @@ namespace gofr {
 enum : unsigned {
     ERRW_WAIT_TIMEOUT = 1u,   // a bounded mbarrier wait ran out
     ERRW_WRAP_LOOP = 2u,      // the FP64 iterative minimum image exceeded its iteration cap
-    ERRW_QUEUE = 4u           // a work queue overflowed its capacity
+    ERRW_QUEUE = 4u,          // a work queue overflowed its capacity
+    ERRW_BOUNDS = 8u          // a debug bounds check failed (GOFR_DEBUG_BOUNDS builds only)
 };
+
+// Debug builds (-DGOFR_DEBUG_BOUNDS): GOFR_CHECK(cond, err) records a failed
+// index check in the error word (no trap) and is false, so the access it
+// guards is skipped; in normal builds it is `true` and costs nothing.
+#ifdef GOFR_DEBUG_BOUNDS
+#define GOFR_CHECK(cond, err) ((cond) ? true : (atomicOr((err), (unsigned)ERRW_BOUNDS), false))
+#else
+#define GOFR_CHECK(cond, err) true
+#endif
 
 // Stats slots (unsigned long long) on the device.
 enum : int { ST_CANDIDATES = 0, ST_RECHECKS = 1, ST_EVALUATED = 2, ST_COUNT = 4 };

@@ -107,7 +107,7 @@ __device__ __forceinline__ void recheck_pair(const double *__restrict__ pos64,
     const double *box = box64 + fo * 9;
     double d2 = ref_d2<TRI>(xi[0], xi[1], xi[2], xj[0], xj[1], xj[2], box, err);
     int b = ref_bin(d2, rmin, dr, rmin2, rmax2, nbin);
-    if (b >= 0) hist_add(hist, gcounts, ch, nbin, b);
+    if (b >= 0 && GOFR_CHECK(b < nbin && ch >= 0, err)) hist_add(hist, gcounts, ch, nbin, b);
 }
 
 // ---------------------------------------------------------------------------
@@ -423,7 +423,12 @@ __device__ __forceinline__ bool f32_item(const PairLaunch &P, const F32Views &V,
                         int bi = __float2int_rd(__fmul_rn(__fsub_rn(rr_, P.rmin_f), P.inv_dr_f));
                         bi = min(max(bi, 0), P.nbin - 1);
                         const float2 w = V.win[bi];
-                        if (d2 >= w.x && d2 <= w.y) hist_add(V.hist, gc, ch, P.nbin, bi);
+                        if (d2 >= w.x && d2 <= w.y) {
+                            if (GOFR_CHECK(ch >= 0 && ch < P.nch && bi >= 0 && bi < P.nbin &&
+                                               jj < tj && ia < P.a1,
+                                           P.err))
+                                hist_add(V.hist, gc, ch, P.nbin, bi);
+                        }
                         else need = true;
                     }
                     if (need) {
@@ -474,6 +479,7 @@ __device__ __forceinline__ bool f32_item(const PairLaunch &P, const F32Views &V,
                     my_slots[cnt * NT] = make_uint2(__float_as_uint(d3), (m0 + 12u) | (WCHK && (wb & 2u) ? 0x80000000u : 0u));
                     ++cnt;
                 }
+                if (!GOFR_CHECK(cnt <= SLOTS, P.err)) cnt = SLOTS;
                 if (__any_sync(0xffffffffu, cnt > SLOTS - 4)) warp_flush();
             }
         }
@@ -680,7 +686,8 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f64(const PairLaunch P)
                     int b = ref_bin(d2, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
                     if (b >= 0) {
                         int ch = chtab[ti[r] * P.ntypes + tj_] + (ia[r] == jbase + jj ? half : 0);
-                        hist_add(hist, gc, ch, P.nbin, b);
+                        if (GOFR_CHECK(ch >= 0 && ch < P.nch && b < P.nbin, P.err))
+                            hist_add(hist, gc, ch, P.nbin, b);
                     }
                 }
             }

@@ -229,8 +229,10 @@ def counts_to_buffer(counts, ntimesteps, skip, nparts=0):
 class Engine:
     """One gofr_ctx: resident frames on one GPU and runs on them."""
 
-    def __init__(self, device=0):
-        self.L = load_library()
+    def __init__(self, device=0, library=None):
+        """library: a ctypes handle from load_library(path) to use another build
+        of the engine (e.g. the GOFR_DEBUG_BOUNDS variant); default the in-tree one."""
+        self.L = library if library is not None else load_library()
         self._ctx = ctypes.c_void_p()
         rc = self.L.gofr_ctx_create(ctypes.byref(self._ctx), int(device))
         if rc != GOFR_OK:
