@@ -84,6 +84,16 @@ def dist_info():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
+def max_over_ranks(v, world):
+    """The largest of every rank's v (the job's time is its slowest rank's)."""
+    if world <= 1:
+        return v
+    import torch
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t[0])
+
+
 def step_window(s, rank=0):
     """primo of step s: 9 windows of 200 origin-frames cover reset(1800)."""
     return 200 * ((s + rank * 4) % STEP_WINDOWS)
@@ -481,11 +491,7 @@ def run_gpu(args):
             kernels_used.add(int(st["kernel_used"]))
     barrier()
     launches = eng.stats()["launches"] - launches0
-    dev_s = sum(total_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([dev_s], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_s = float(t[0])
+    dev_s = max_over_ranks(sum(total_ms) / 1e3, world)
     value = pairs * world / dev_s / 1e9
     kernel_avg_s = sum(kernel_ms) / len(kernel_ms) / 1e3
     pairs_per_launch = pairs / args.steps
@@ -516,11 +522,7 @@ def run_gpu(args):
                 times.append(dt)
         e2_launch = e2.stats()["launches"]
         e2.close()
-        e2e_s = sum(times)
-        if world > 1:
-            t = torch.tensor([e2e_s], dtype=torch.float64)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            e2e_s = float(t[0])
+        e2e_s = max_over_ranks(sum(times), world)
         e2e = {"value": round(pairs * world / e2e_s / 1e9, 3), "unit": UNIT,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(nout * 8),
                "timing": "host wall clock around gofr_set_frames + gofr_run (synchronous)",
