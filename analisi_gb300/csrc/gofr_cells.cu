@@ -272,6 +272,9 @@ __global__ void __launch_bounds__(NT, 2)
     __shared__ Range irg[MAXR], jrg[MAXR];
     __shared__ int ipre[MAXR + 1], jpre[MAXR + 1];
     __shared__ int nir, njr, rqn;
+    // type << 24 | atom id of this pass's first atoms, read by the flush
+    // (a shared load in place of an R-way register select)
+    __shared__ unsigned s_iv[R][NT];
 
     // the current trajectory's item range (kept in shared memory: the pair
     // loop needs every register)
@@ -452,7 +455,6 @@ __global__ void __launch_bounds__(NT, 2)
 
         for (int ibase = 0; ibase < n_i; ibase += TI) {
             f2 xi[R], yi[R], zi[R];
-            int ti[R], iid[R];
 #pragma unroll
             for (int r = 0; r < R; ++r) {
                 const int q = ibase + r * NT + tid;
@@ -461,13 +463,10 @@ __global__ void __launch_bounds__(NT, 2)
                     const int rr = range_of(ipre, nir, q);
                     const int s = irg[rr].begin + (q - ipre[rr]);  // block cells: image (0,0,0)
                     x = fo32[s]; y = fo32[NP + s]; z = fo32[2 * NP + s];
-                    const unsigned v = fo_idt[s];
-                    ti[r] = (int)(v >> 24);
-                    iid[r] = (int)(v & 0xffffffu);
+                    s_iv[r][tid] = fo_idt[s];
                 } else {
                     x = y = z = __int_as_float(0x7fc00000);
-                    ti[r] = 0;
-                    iid[r] = -1;
+                    s_iv[r][tid] = 0x00ffffffu;  // type 0, no atom id
                 }
                 xi[r] = f2pk(x, x); yi[r] = f2pk(y, y); zi[r] = f2pk(z, z);
             }
@@ -507,14 +506,10 @@ __global__ void __launch_bounds__(NT, 2)
                             const float d2 = __uint_as_float(e[u].x);
                             const int r = e[u].y & 3;  // R <= 4
                             const int jj = (e[u].y >> 2) & 0x1fff;
-                            int t_i = ti[0], a_ = iid[0];
-#pragma unroll
-                            for (int rr = 1; rr < R; ++rr) {
-                                t_i = (r == rr) ? ti[rr] : t_i;
-                                a_ = (r == rr) ? iid[rr] : a_;
-                            }
+                            const unsigned iv = s_iv[r][tid];  // written by this thread
+                            const int t_i = (int)(iv >> 24);
                             const unsigned jv = jidt[jj];
-                            ia[u] = a_;
+                            ia[u] = (int)(iv & 0xffffffu);
                             ja[u] = (int)(jv & 0xffffffu);
                             ch[u] = chtab[t_i * P.ntypes + (int)(jv >> 24)] +
                                     (ia[u] == ja[u] ? half : 0);
@@ -528,12 +523,20 @@ __global__ void __launch_bounds__(NT, 2)
                             need[u] = test && !inw;
                         }
 #pragma unroll
-                        for (int u = 0; u < FLUSH_ILP; ++u) {
-                            if (ok[u] && GOFR_CHECK(ch[u] >= 0 && ch[u] < P.nch && bi[u] >= 0 &&
-                                                        bi[u] < P.nbin,
-                                                    P.err))
-                                atomicAdd(hist + ch[u] * P.nbin + bi[u], 1u);
-                            if (need[u]) {
+                        for (int u = 0; u < FLUSH_ILP; ++u)
+                            red_shared_add1_if(smem_u32(hist + ch[u] * P.nbin + bi[u]),
+                                               ok[u] && GOFR_CHECK(ch[u] >= 0 && ch[u] < P.nch &&
+                                                                       bi[u] >= 0 && bi[u] < P.nbin,
+                                                                   P.err));
+                        // FP64 rechecks are rare: one warp-uniform branch
+                        // around them
+                        bool any_need = false;
+#pragma unroll
+                        for (int u = 0; u < FLUSH_ILP; ++u) any_need |= need[u];
+                        if (__any_sync(0xffffffffu, any_need)) {
+#pragma unroll
+                            for (int u = 0; u < FLUSH_ILP; ++u) {
+                                if (!need[u]) continue;
                                 ++n_rech;
                                 const int slot = atomicAdd(&rqn, 1);
                                 if (slot < QCAP) {

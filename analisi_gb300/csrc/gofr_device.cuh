@@ -82,6 +82,16 @@ __device__ __forceinline__ float sqrt_guess(float x)
     return r;
 }
 
+// Adds 1 to the shared-memory word at addr when p holds, as one predicated
+// reduction: the histogram updates of a warp flush issue without a branch
+// (and its convergence bookkeeping) around each of them.
+__device__ __forceinline__ void red_shared_add1_if(unsigned addr, bool p)
+{
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %1, 0;\n\t@q red.shared.add.u32 [%0], 1;\n\t}"
+                 ::"r"(addr), "r"((unsigned)p)
+                 : "memory");
+}
+
 // ---------------------------------------------------------------------------
 // FP64 restatement of the reference pair arithmetic.
 // Every operation is an explicitly rounded IEEE intrinsic, so nvcc cannot

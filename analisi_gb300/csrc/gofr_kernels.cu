@@ -402,43 +402,67 @@ __device__ __forceinline__ bool f32_item(const PairLaunch &P, const F32Views &V,
         const unsigned char *btp = V.jt + b * TJ32;
 
         // Bins every slot of this warp's lanes (all lanes take part; each
-        // processes its own slots), then empties them.
+        // processes its own slots, two per round so that their shared-memory
+        // load chains overlap), then empties them.  Shared-histogram updates
+        // are predicated reductions; the rare FP64 rechecks sit behind one
+        // warp-uniform branch.
         auto warp_flush = [&]() {
             const int maxc = __reduce_max_sync(0xffffffffu, (unsigned)cnt);
-            for (int q = 0; q < maxc; ++q) {
-                if (q < cnt) {
-                    const uint2 e = my_slots[q * NT];
-                    const float d2 = __uint_as_float(e.x);
-                    const int r = e.y & 3;
-                    const int jj = (e.y >> 2) & 0x1fff;
-                    const int ia = ia0 + r * NT;
-                    const int ja = jbase + jj;
+            for (int q0 = 0; q0 < maxc; q0 += 2) {
+                uint2 e[2];
+                bool v[2], ok[2], need[2];
+                int ch[2], bi[2], ia[2], ja[2];
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    v[u] = q0 + u < cnt;
+                    e[u] = v[u] ? my_slots[(q0 + u) * NT] : make_uint2(0x7f800000u, 0u);
+                }
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    const float d2 = __uint_as_float(e[u].x);
+                    const int r = e[u].y & 3;
+                    const int jj = (e[u].y >> 2) & 0x1fff;
+                    ia[u] = ia0 + r * NT;
+                    ja[u] = jbase + jj;
                     int t_i = ti[0];
 #pragma unroll
                     for (int rr = 1; rr < R32; ++rr) t_i = (r == rr) ? ti[rr] : t_i;
-                    const int ch = V.chtab[t_i * P.ntypes + btp[jj]] + (ia == ja ? half : 0);
-                    bool need = WCHK && (e.y >> 31);
-                    if (!need && d2 >= P.lo_f) {
-                        const float rr_ = sqrt_guess(d2);
-                        int bi = __float2int_rd(__fmul_rn(__fsub_rn(rr_, P.rmin_f), P.inv_dr_f));
-                        bi = min(max(bi, 0), P.nbin - 1);
-                        const float2 w = V.win[bi];
-                        if (d2 >= w.x && d2 <= w.y) {
-                            if (GOFR_CHECK(ch >= 0 && ch < P.nch && bi >= 0 && bi < P.nbin &&
-                                               jj < tj && ia < P.a1,
-                                           P.err))
-                                hist_add(V.hist, gc, ch, P.nbin, bi);
-                        }
-                        else need = true;
-                    }
-                    if (need) {
+                    ch[u] = V.chtab[t_i * P.ntypes + btp[jj]] + (ia[u] == ja[u] ? half : 0);
+                    const bool wrap = WCHK && (e[u].y >> 31);  // minimum image not certain
+                    const int b_ = __float2int_rd(
+                        __fmul_rn(__fsub_rn(sqrt_guess(d2), P.rmin_f), P.inv_dr_f));
+                    bi[u] = min(max(b_, 0), P.nbin - 1);
+                    const float2 w = V.win[bi[u]];
+                    const bool test = v[u] && !wrap && d2 >= P.lo_f;
+                    const bool inw = d2 >= w.x && d2 <= w.y;
+                    ok[u] = test && inw &&
+                            GOFR_CHECK(ch[u] >= 0 && ch[u] < P.nch && bi[u] >= 0 &&
+                                           bi[u] < P.nbin && jj < tj && ia[u] < P.a1,
+                                       P.err);
+                    need[u] = (v[u] && wrap) || (test && !inw);
+                }
+                if (gc) {
+#pragma unroll
+                    for (int u = 0; u < 2; ++u)
+                        if (ok[u]) atomicAdd(gc + ch[u] * P.nbin + bi[u], 1ull);
+                } else {
+#pragma unroll
+                    for (int u = 0; u < 2; ++u)
+                        red_shared_add1_if(smem_u32(V.hist + ch[u] * P.nbin + bi[u]), ok[u]);
+                }
+                if (__any_sync(0xffffffffu, need[0] || need[1])) {
+#pragma unroll
+                    for (int u = 0; u < 2; ++u) {
+                        if (!need[u]) continue;
                         ++th.n_rech;
                         const int slot = atomicAdd(V.rqn, 1);
                         if (slot < QCAP) {
-                            V.rq[slot] = make_uint4((unsigned)ia, (unsigned)ja, (unsigned)ch, 0u);
+                            V.rq[slot] =
+                                make_uint4((unsigned)ia[u], (unsigned)ja[u], (unsigned)ch[u], 0u);
                         } else {
-                            recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, ia, ja, V.hist, ch,
-                                              P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err, gc);
+                            recheck_pair<TRI>(P.pos64, P.box64, N, fo, fl, ia[u], ja[u], V.hist,
+                                              ch[u], P.nbin, P.rmin, P.dr, P.rmin2, P.rmax2, P.err,
+                                              gc);
                         }
                     }
                 }
