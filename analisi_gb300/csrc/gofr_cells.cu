@@ -42,6 +42,7 @@ constexpr int SLOTS = 16;
 constexpr int QCAP = 1024;
 constexpr int MAXR = 128;     // max contiguous ranges of a neighbourhood (checked on host)
 constexpr int FLUSH_ILP = 2;  // slots binned per round of a warp flush
+static_assert(SLOTS % FLUSH_ILP == 0, "a flush round reads rows q0 .. q0 + FLUSH_ILP - 1 < SLOTS");
 
 typedef unsigned long long f2;
 __device__ __forceinline__ f2 f2pk(float a, float b)
@@ -497,7 +498,9 @@ __global__ void __launch_bounds__(NT, 2)
 #pragma unroll
                         for (int u = 0; u < FLUSH_ILP; ++u) {
                             v[u] = q0 + u < cnt;
-                            e[u] = v[u] ? my_slots[(q0 + u) * NT] : make_uint2(0x7f800000u, 0u);
+                            // rows < SLOTS (q0 even, SLOTS even): load, then select
+                            const uint2 g = my_slots[(q0 + u) * NT];
+                            e[u] = make_uint2(v[u] ? g.x : 0x7f800000u, v[u] ? g.y : 0u);
                         }
                         int ch[FLUSH_ILP], bi[FLUSH_ILP], ia[FLUSH_ILP], ja[FLUSH_ILP];
                         bool ok[FLUSH_ILP], need[FLUSH_ILP];
@@ -584,6 +587,24 @@ __global__ void __launch_bounds__(NT, 2)
                 }
                 if (__any_sync(0xffffffffu, cnt > 0)) warp_flush();
                 __syncthreads();  // every thread done with buffer t & 1
+                // FP64 recheck queue more than half full: drain it now, all
+                // threads together (the same decision in every thread), so that
+                // it rarely fills and a flush rarely recomputes a pair itself
+                if (rqn > QCAP / 2) {
+                    const int nq = min(rqn, QCAP);
+                    for (int q = tid; q < nq; q += NT) {
+                        const uint4 e = rq[q];
+                        const double *xi64 = P.pos64 + (fo * P.N + (int)e.x) * 3;
+                        const double *xj64 = P.pos64 + (fl * P.N + (int)e.y) * 3;
+                        const double d2d = ref_d2<false>(xi64[0], xi64[1], xi64[2], xj64[0],
+                                                         xj64[1], xj64[2], P.box64 + fo * 9, P.err);
+                        const int bb = ref_bin(d2d, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
+                        if (bb >= 0) atomicAdd(hist + (int)e.z * P.nbin + bb, 1u);
+                    }
+                    __syncthreads();
+                    if (tid == 0) rqn = 0;
+                    __syncthreads();
+                }
             }
         }
         // end of item: FP64 recheck queue of this item's frames, all threads together
