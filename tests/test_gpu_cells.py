@@ -114,3 +114,43 @@ def test_tuned_kernel_choice_is_exact_and_cached(gpu_engine, oracle_mod, tmp_pat
     b, st2 = _run(gpu_engine, w, "tuned")
     np.testing.assert_array_equal(b, ref)
     assert st2["kernel_used"] == st["kernel_used"]
+
+
+def copies_on_thresholds(copies=12, distinct=600):
+    """A 2-type random walk whose atoms each have `copies` copies spaced by 0.5
+    along x (the same trajectory shifted), with rmin = dr = 0.5: at lag 0 every
+    pair of copies lies on a bin threshold, where the reference's bin depends on
+    the last bit of its FP64 arithmetic and FP32 cannot certify anything."""
+    w = workloads.small_case(66, distinct, 6, 30.0, 0.3, [distinct // 2, distinct - distinct // 2],
+                             rmin=0.5, rmax=6.0, nbin=11, tmax=3, skip=1, every=1,
+                             ntimesteps=4, primo=0)
+    pos = np.repeat(w["positions"], copies, axis=1)
+    pos[..., 0] += np.tile(0.5 * np.arange(copies), distinct)
+    w["positions"] = np.ascontiguousarray(pos)
+    w["type_ids"] = np.ascontiguousarray(np.repeat(w["type_ids"], copies))
+    return w
+
+
+@pytest.mark.parametrize("kernel,plan", [("cell", "2,3,3,3,3"), ("cell", "1,4,1,1,1"),
+                                         ("f32", None)],
+                         ids=["cell-2,3,3,3,3", "cell-1,4,1,1,1", "all-pairs"])
+def test_many_rechecks_drain_the_queue(gpu_engine, oracle_mod, kernel, plan, monkeypatch):
+    """Thousands of FP64 rechecks per lag-0 work item, more than a CTA's recheck
+    queue holds within one tile: the queue is drained between tiles and the
+    flush recomputes what does not fit; the counts must still be the oracle's."""
+    if plan is None:
+        monkeypatch.delenv("ANALISI_GB300_CELL_PLAN", raising=False)
+    else:
+        monkeypatch.setenv("ANALISI_GB300_CELL_PLAN", plan)
+    copies = 12
+    w = copies_on_thresholds(copies)
+    N = w["positions"].shape[1]
+    p = w["params"]
+    ref = oracle_mod.gofrt_counts(w["positions"], w["boxes"], w["type_ids"], w["ntypes"],
+                                  p["rmin"], p["rmax"], p["nbin"], p["tmax"], 8, p["skip"],
+                                  p["every"], p["ntimesteps"], p["primo"])
+    got, st = _run(gpu_engine, w, kernel)
+    assert st["kernel_used"] == (3 if kernel == "cell" else 1)
+    # at lag 0 every ordered pair of copies sits on a threshold and is rechecked
+    assert st["rechecks"] >= N * (copies - 1)
+    np.testing.assert_array_equal(got, ref)

@@ -59,3 +59,20 @@ def test_debug_build_batch(debug_lib, oracle_mod):
         outs = e.batch_run(use_graph=True)
     for w, got in zip(mem, outs):
         np.testing.assert_array_equal(got, _ref(oracle_mod, w, w["params"]))
+
+
+@pytest.mark.parametrize("kernel", ["cell", "f32"])
+def test_debug_build_recheck_queue_overflow(debug_lib, oracle_mod, kernel, monkeypatch):
+    """Copies of every atom on bin thresholds: the recheck queue is drained
+    between tiles and overflows into the flush's own FP64 path, with every index
+    check passing."""
+    from analisi_gb300 import engine
+    from test_gpu_cells import copies_on_thresholds
+    monkeypatch.setenv("ANALISI_GB300_CELL_PLAN", "2,3,3,3,3")
+    w = copies_on_thresholds()
+    p = w["params"]
+    with engine.Engine(0, library=debug_lib) as e:
+        e.set_frames(w["positions"], w["boxes"], w["type_ids"], w["ntypes"])
+        got = e.run(p["rmin"], p["rmax"], p["nbin"], p["tmax"], p["skip"], p["every"],
+                    p["ntimesteps"], p["primo"], kernel=kernel)
+    np.testing.assert_array_equal(got, _ref(oracle_mod, w, p))
