@@ -601,7 +601,9 @@ def run_gpu(args):
                                       "recheck_frac": rech / pairs}),
            "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
            "clocks": clocks, "fp64_kernel": f64, **extra,
-           "kernel_ms_per_step": round(1e3 * kernel_avg_s, 3)}
+           "kernel_ms_per_step": round(1e3 * kernel_avg_s, 3),
+           # (origin, lag) items of all ranks per second (frames compared per second)
+           "items_per_s": round(world * ORIGINS_PER_STEP * lags * args.steps / dev_s, 1)}
     print(json.dumps(res))
     if world > 1:
         torch.distributed.barrier()
