@@ -604,7 +604,13 @@ def run_gpu(args):
             "kernel": KERNEL_NAMES.get(kernel_used, str(kernel_used)),
             "evaluated_pairs_per_launch": int(evaluated_per_launch),
             "smem_atomic_peak_per_s": satom_peak,
-            "atomics_needed_per_s": round(cands / (sum(kernel_ms) / 1e3), 1)}
+            "atomics_needed_per_s": round(cands / (sum(kernel_ms) / 1e3), 1),
+            # the all-pairs bound: every N^2 pair at 16 FP32 operations and the
+            # measured peak; the cell-list kernel's all-pairs-equivalent rate
+            # against it says how much of that bound the algorithm recovers
+            "allpairs_bound_gpairs_per_s": round(fp32_peak / OPS_PER_PAIR / 1e9, 1),
+            "kernel_rate_vs_allpairs_bound": round(
+                pairs_per_launch / kernel_avg_s / (fp32_peak / OPS_PER_PAIR), 4)}
     cpu = None
     if not args.no_cpu_baseline:
         v, thr, desc, dt = cpu_sample(w, seconds=15.0)
