@@ -2132,9 +2132,9 @@ int gofr_neigh_run(gofr_ctx *ctx, const gofr_neigh_spec *spec, unsigned nspec, s
     L.tric = t.tric;
     // FP32 prefilter with the all-pairs kernel's certified bound, where the
     // minimum image of the near pairs is certain
+    double cmax = -INFINITY;
+    for (unsigned k = 0; k < nt; ++k) cmax = std::max(cmax, cut2[k]);
     {
-        double cmax = -INFINITY;
-        for (unsigned k = 0; k < nt; ++k) cmax = std::max(cmax, cut2[k]);
         if (std::isfinite(cmax) && cmax >= 0.0) {
             const Bound b = error_bound(t);
             const float hi = f_up(cmax + Efun(b, cmax));
@@ -2150,6 +2150,28 @@ int gofr_neigh_run(gofr_ctx *ctx, const gofr_neigh_spec *spec, unsigned nspec, s
             }
         }
     }
+    // Cell-list form: orthorhombic boxes constant over the trajectory, cells
+    // of edge >= the largest cutoff (x (1 + 1e-6)), at least 3 per axis.
+    // ANALISI_GB300_NEIGH_KERNEL=allpairs keeps the all-pairs form.
+    {
+        const char *env = std::getenv("ANALISI_GB300_NEIGH_KERNEL");
+        const bool allpairs = env && std::strcmp(env, "allpairs") == 0;
+        gofr_params q{};
+        q.rmax = cmax > 0.0 ? std::sqrt(cmax) : 0.0;
+        int nc[3];
+        if (!allpairs && L.prefilter && !t.tric && t.box_constant && t.N < (1u << 24) &&
+            q.rmax > 0.0 && cell_grid(t, q, 1, nc)) {
+            Plan pl;
+            for (int k = 0; k < 3; ++k) pl.nc[k] = nc[k];
+            rc = ensure_cells(ctx, t, pl);
+            if (rc) return rc;
+            const size_t ncell = (size_t)nc[0] * nc[1] * nc[2];
+            L.cells = 1;
+            for (int k = 0; k < 3; ++k) L.nc[k] = nc[k];
+            L.cstart = t.d_cstart + timestep * (ncell + 1);
+            L.csidt = t.d_sidt + timestep * padded_natoms(t.N);
+        }
+    }
     std::memset(&ctx->stats, 0, sizeof ctx->stats);
     CK(cudaEventRecord(ctx->ev[1], ctx->stream));
     ++ctx->launches;
@@ -2159,6 +2181,22 @@ int gofr_neigh_run(gofr_ctx *ctx, const gofr_neigh_spec *spec, unsigned nspec, s
     unsigned long long tail[2] = {0ull, 0ull};
     CK(cudaMemcpyAsync(tail, ctx->d_nl_meta + 3 * nt, 16, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    if (tail[0] & 2ull) {
+        // a cell neighbourhood held more survivors than a warp's buffer: the
+        // all-pairs form over again
+        L.cells = 0;
+        CK(cudaMemcpyAsync(ctx->d_nl_meta + 3 * nt, meta.data() + 3 * nt, 16,
+                           cudaMemcpyHostToDevice, ctx->stream));
+        if (list_len) CK(cudaMemsetAsync(ctx->d_nl_list, 0, list_len * 8, ctx->stream));
+        if (rpos_len) CK(cudaMemsetAsync(ctx->d_nl_rpos, 0, rpos_len * 8, ctx->stream));
+        ++ctx->launches;
+        if (launch_neigh_build(L, ctx->num_sms, ctx->stream))
+            return fail(ctx, GOFR_ERR_CUDA, "neighbour-list kernel launch failed: %s",
+                        cudaGetErrorString(cudaGetLastError()));
+        CK(cudaMemcpyAsync(tail, ctx->d_nl_meta + 3 * nt, 16, cudaMemcpyDeviceToHost,
+                           ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+    }
     if (tail[0] & 1ull) {  // some list is full: look for the reference's overflow
         ++ctx->launches;
         if (launch_neigh_check(L, ctx->num_sms, ctx->stream))
@@ -2185,7 +2223,7 @@ int gofr_neigh_run(gofr_ctx *ctx, const gofr_neigh_spec *spec, unsigned nspec, s
     CK(cudaEventRecord(ctx->ev[3], ctx->stream));
     ctx->stats.pairs = (unsigned long long)t.N * t.N;
     ctx->stats.evaluated = ctx->stats.pairs;
-    ctx->stats.kernel_used = -1;
+    ctx->stats.kernel_used = L.cells ? -2 : -1;  // neighbour lists: -2 cell-list form
     rc = gofr_sync(ctx);
     if (rc) return rc;
     if (overflow) {

@@ -115,7 +115,8 @@ struct NeighLaunch {
     unsigned long long *list;             // the reference's list array
     double *rpos;                         // the reference's rpos array
     int *full;                            // [N][ntypes] neighbour that filled a list (N: not full)
-    unsigned *flags;                      // bit 0: some list is full
+    unsigned *flags;                      // bit 0: some list is full; bit 1: a cell
+                                          // neighbourhood held too many candidates
     unsigned long long *first_err;        // min i*N + j over overflowing pairs
     unsigned *err;                        // error word (minimum-image iteration cap)
     int N, ntypes;
@@ -128,6 +129,12 @@ struct NeighLaunch {
     const Box32 *box32;                   // [T]
     long long NP;
     float hi_f;
+    // cell-list form (orthorhombic boxes, prefilter on): the frame's cells of
+    // edge >= the largest cutoff, at least 3 per axis
+    int cells;
+    int nc[3];
+    const int *cstart;                    // [ncell + 1] first sorted slot of each cell
+    const unsigned *csidt;                // [N] type << 24 | atom id in cell order
 };
 int launch_neigh_build(const NeighLaunch &L, int num_sms, cudaStream_t s);
 int launch_neigh_check(const NeighLaunch &L, int num_sms, cudaStream_t s);

@@ -84,6 +84,51 @@ __device__ __forceinline__ float pair_f32(const NeighLaunch &L, int a, int b)
     return d2;
 }
 
+// FP64 arithmetic and placement of the n (<= 32) candidates src[0..n) of
+// atom a, one per lane, in ascending order: the counted entries of each
+// neighbour type go to the list at the running count cnt[k] (ballot prefix),
+// and full[a][k] records the neighbour that fills a list.
+template <bool TRI>
+__device__ __forceinline__ void place(const NeighLaunch &L, const double *frame, const double *box,
+                                      int a, const int *src, int n, unsigned long long *cnt)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
+    const bool have = lane < n;
+    const int b = have ? src[lane] : 0;
+    int tb = 0;
+    double x[3] = {0.0, 0.0, 0.0}, d2 = 0.0;
+    bool counted = false;
+    if (have) {
+        tb = L.types[b];
+        const int i = a < b ? a : b, j = a < b ? b : a;
+        d2 = pair_vec<TRI>(L, frame, box, i, j, x);
+        if (a > b) { x[0] = -x[0]; x[1] = -x[1]; x[2] = -x[2]; }
+        counted = d2 <= L.cut2[tb];
+    }
+    for (int k = 0; k < L.ntypes; ++k) {
+        const unsigned m = __ballot_sync(0xffffffffu, counted && tb == k);
+        if (!m) continue;
+        const unsigned long long base = cnt[k];
+        const unsigned long long nk = L.nneigh[k];
+        if (counted && tb == k) {
+            const unsigned long long pos = base + __popc(m & lt);
+            if (pos < nk) {
+                L.list[L.loff[k] + (size_t)a * (nk + 1) + 1 + pos] = (unsigned long long)b;
+                double *r = L.rpos + L.roff[k] + ((size_t)a * nk + pos) * 4;
+                r[0] = __dsqrt_rn(d2);
+                r[1] = x[0];
+                r[2] = x[1];
+                r[3] = x[2];
+            }
+            if (pos + 1 == nk) L.full[(size_t)a * L.ntypes + k] = b;
+        }
+        __syncwarp();
+        if (lane == 0) cnt[k] = base + __popc(m);
+        __syncwarp();
+    }
+}
+
 template <bool TRI>
 __global__ void __launch_bounds__(NT) k_neigh_build(const NeighLaunch L)
 {
@@ -102,43 +147,6 @@ __global__ void __launch_bounds__(NT) k_neigh_build(const NeighLaunch L)
             L.full[(size_t)a * L.ntypes + k] = L.nneigh[k] == 0 ? -1 : L.N;
         }
         __syncwarp();
-        // FP64 arithmetic and placement of the first n queued candidates, one
-        // per lane, in ascending order
-        auto place = [&](int n) {
-            const bool have = lane < n;
-            const int b = have ? cq[w][lane] : 0;
-            int tb = 0;
-            double x[3] = {0.0, 0.0, 0.0}, d2 = 0.0;
-            bool counted = false;
-            if (have) {
-                tb = L.types[b];
-                const int i = a < b ? a : b, j = a < b ? b : a;
-                d2 = pair_vec<TRI>(L, frame, box, i, j, x);
-                if (a > b) { x[0] = -x[0]; x[1] = -x[1]; x[2] = -x[2]; }
-                counted = d2 <= L.cut2[tb];
-            }
-            for (int k = 0; k < L.ntypes; ++k) {
-                const unsigned m = __ballot_sync(0xffffffffu, counted && tb == k);
-                if (!m) continue;
-                const unsigned long long base = cnt[w][k];
-                const unsigned long long nk = L.nneigh[k];
-                if (counted && tb == k) {
-                    const unsigned long long pos = base + __popc(m & lt);
-                    if (pos < nk) {
-                        L.list[L.loff[k] + (size_t)a * (nk + 1) + 1 + pos] = (unsigned long long)b;
-                        double *r = L.rpos + L.roff[k] + ((size_t)a * nk + pos) * 4;
-                        r[0] = __dsqrt_rn(d2);
-                        r[1] = x[0];
-                        r[2] = x[1];
-                        r[3] = x[2];
-                    }
-                    if (pos + 1 == nk) L.full[(size_t)a * L.ntypes + k] = b;
-                }
-                __syncwarp();
-                if (lane == 0) cnt[w][k] = base + __popc(m);
-                __syncwarp();
-            }
-        };
         int qn = 0;  // queued candidates (warp-uniform)
         for (int b0 = 0; b0 < L.N; b0 += 32) {
             const int b = b0 + lane;
@@ -150,7 +158,7 @@ __global__ void __launch_bounds__(NT) k_neigh_build(const NeighLaunch L)
             qn += __popc(m);
             __syncwarp();
             if (qn >= 32) {
-                place(32);
+                place<TRI>(L, frame, box, a, cq[w], 32, cnt[w]);
                 const int rest = qn - 32;
                 const int v = lane < rest ? cq[w][32 + lane] : 0;
                 __syncwarp();
@@ -159,7 +167,112 @@ __global__ void __launch_bounds__(NT) k_neigh_build(const NeighLaunch L)
                 qn = rest;
             }
         }
-        if (qn > 0) place(qn);
+        if (qn > 0) place<TRI>(L, frame, box, a, cq[w], qn, cnt[w]);
+        for (int k = lane; k < L.ntypes; k += 32) {
+            const unsigned long long c = cnt[w][k], nk = L.nneigh[k];
+            L.list[L.loff[k] + (size_t)a * (nk + 1)] = c < nk ? c : nk;
+            if (c >= nk) atomicOr(L.flags, 1u);  // some list is full: run the check
+        }
+        __syncwarp();
+    }
+}
+
+// Cell-list form (orthorhombic boxes): the frame's atoms sorted by cells of
+// edge >= the largest cutoff, at least 3 per axis, so every pair within a
+// cutoff lies in neighbouring cells.  A warp takes the atom of one sorted
+// slot, gathers the atoms of the 27 cells around its cell through the FP32
+// prefilter, sorts the survivors by index (the reference's list order) and
+// places them as the all-pairs form does.  A neighbourhood with more than
+// CQCAP survivors sets flags bit 1 and the host runs the all-pairs form.
+constexpr int CQCAP = 256;
+
+__global__ void __launch_bounds__(NT) k_neigh_build_cells(const NeighLaunch L)
+{
+    __shared__ unsigned long long cnt[WARPS][NEIGH_MAXT];
+    __shared__ int cq[WARPS][CQCAP];  // survivors in cell order
+    __shared__ int cs[WARPS][CQCAP];  // the same, ascending
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const double *frame = L.pos64 + (size_t)L.timestep * L.N * 3;
+    const double *box = L.box64 + (size_t)L.timestep * 9;
+    const unsigned lt = (1u << lane) - 1u;
+    const int nx = L.nc[0], ny = L.nc[1], nz = L.nc[2];
+    const int ncell = nx * ny * nz;
+    for (long long s0 = (long long)blockIdx.x * WARPS; s0 < L.N; s0 += (long long)gridDim.x * WARPS) {
+        const int s = (int)(s0 + w);
+        if (s >= L.N) continue;  // warp-uniform
+        const int a = (int)(L.csidt[s] & 0xffffffu);
+        // the cell of slot s: the last cell whose first slot is <= s
+        int lo = 0, hi = ncell - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (L.cstart[mid] <= s) lo = mid;
+            else hi = mid - 1;
+        }
+        const int cx = lo % nx, cy = (lo / nx) % ny, cz = lo / (nx * ny);
+        for (int k = lane; k < L.ntypes; k += 32) {
+            cnt[w][k] = 0ull;
+            L.full[(size_t)a * L.ntypes + k] = L.nneigh[k] == 0 ? -1 : L.N;
+        }
+        // lane k < 27 takes neighbour cell k: its first slot and atom count
+        int beg = 0, num = 0;
+        if (lane < 27) {
+            const int ux = (cx + lane % 3 - 1 + nx) % nx;
+            const int uy = (cy + (lane / 3) % 3 - 1 + ny) % ny;
+            const int uz = (cz + lane / 9 - 1 + nz) % nz;
+            const int cc = (uz * ny + uy) * nx + ux;
+            beg = L.cstart[cc];
+            num = L.cstart[cc + 1] - beg;
+        }
+        int incl = num;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int excl = incl - num;
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        int qn = 0;  // survivors (warp-uniform)
+        bool over = false;
+        for (int f0 = 0; f0 < total; f0 += 32) {
+            const int f = f0 + lane;
+            // the neighbour cell holding flat index f: the last lane with excl <= f
+            int src = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                const int e = __shfl_sync(0xffffffffu, excl, src + step);
+                if (e <= f) src += step;
+            }
+            const int sb = __shfl_sync(0xffffffffu, beg, src) + f -
+                           __shfl_sync(0xffffffffu, excl, src);
+            bool cand = false;
+            int b = 0;
+            if (f < total) {
+                b = (int)(L.csidt[sb] & 0xffffffu);
+                cand = b != a && pair_f32<false>(L, a, b) <= L.hi_f;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, cand);
+            if (qn + __popc(m) > CQCAP) {
+                over = true;
+                break;
+            }
+            if (cand) cq[w][qn + __popc(m & lt)] = b;
+            qn += __popc(m);
+        }
+        if (over) {
+            if (lane == 0) atomicOr(L.flags, 2u);
+            continue;
+        }
+        __syncwarp();
+        // ascending order: the rank of each survivor among the (distinct) indices
+        for (int k = lane; k < qn; k += 32) {
+            const int v = cq[w][k];
+            int rank = 0;
+            for (int q = 0; q < qn; ++q) rank += cq[w][q] < v ? 1 : 0;
+            cs[w][rank] = v;
+        }
+        __syncwarp();
+        for (int p0 = 0; p0 < qn; p0 += 32)
+            place<false>(L, frame, box, a, cs[w] + p0, min(32, qn - p0), cnt[w]);
         for (int k = lane; k < L.ntypes; k += 32) {
             const unsigned long long c = cnt[w][k], nk = L.nneigh[k];
             L.list[L.loff[k] + (size_t)a * (nk + 1)] = c < nk ? c : nk;
@@ -232,7 +345,8 @@ int launch_neigh_build(const NeighLaunch &L, int num_sms, cudaStream_t s)
     long long grid = (L.N + WARPS - 1) / WARPS;
     if (grid > (long long)num_sms * 16) grid = (long long)num_sms * 16;
     if (grid < 1) return 0;
-    if (L.tric) k_neigh_build<true><<<(unsigned)grid, NT, 0, s>>>(L);
+    if (L.cells && !L.tric && L.prefilter) k_neigh_build_cells<<<(unsigned)grid, NT, 0, s>>>(L);
+    else if (L.tric) k_neigh_build<true><<<(unsigned)grid, NT, 0, s>>>(L);
     else k_neigh_build<false><<<(unsigned)grid, NT, 0, s>>>(L);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

@@ -126,3 +126,71 @@ def test_engine_neighbours_small_box_fp64_path(gpu_engine, oracle_mod):
         for k in range(2):
             np.testing.assert_array_equal(nl.idx(a, k), o.idx(a, k))
             np.testing.assert_array_equal(nl.r(a, k), o.r(a, k))
+
+
+def _full_compare(nl, o, sort):
+    np.testing.assert_array_equal(nl.list[_counted_mask(o)], o.list[_counted_mask(o)])
+    for a in range(o.natoms):
+        for k in range(len(o.nneigh)):
+            n = o.size(a, k)
+            assert nl.size(a, k) == n
+            np.testing.assert_array_equal(nl.r(a, k), o.r(a, k))
+            if sort:
+                assert nl.sann_n(a, k) == o.sann_n(a, k)
+
+
+@pytest.mark.parametrize("sort", [False, True])
+def test_cell_form_matches_oracle_and_all_pairs(gpu_engine, oracle_mod, sort, monkeypatch):
+    """Orthorhombic box of 11^3 cells of edge >= the largest cutoff, atoms far
+    outside the box (iterated minimum image), a box not at the origin, three
+    types: the cell-list form's lists, vectors and SANN counts equal the
+    oracle's and the all-pairs form's, bit for bit."""
+    L = 40.0
+    w = workloads.small_case(84, 4000, 3, L, 0.2, [2000, 1200, 800])
+    rng = np.random.default_rng(840)
+    shift = np.array([-11.5, 4.25, 7.0])
+    w["positions"] = w["positions"] + L * rng.integers(-3, 4, size=(1, 4000, 3)) + shift
+    w["boxes"] = w["boxes"].copy()
+    w["boxes"][:, 0:3] += shift
+    spec = [(50, 3.1 ** 2, 3.6 ** 2), (50, 2.7 ** 2, 3.6 ** 2), (50, 3.5 ** 2, 3.6 ** 2)]
+    o = oracle_mod.neighbours(w["positions"], w["boxes"], w["type_ids"], 3, 2, spec, sort)
+    gpu_engine.set_frames(w["positions"], w["boxes"], w["type_ids"], 3)
+    monkeypatch.delenv("ANALISI_GB300_NEIGH_KERNEL", raising=False)
+    nl = gpu_engine.neighbours(2, spec, sort)
+    assert gpu_engine.stats()["kernel_used"] == -2
+    _full_compare(nl, o, sort)
+    monkeypatch.setenv("ANALISI_GB300_NEIGH_KERNEL", "allpairs")
+    nl2 = gpu_engine.neighbours(2, spec, sort)
+    assert gpu_engine.stats()["kernel_used"] == -1
+    np.testing.assert_array_equal(nl2.list, nl.list)
+    np.testing.assert_array_equal(nl2.rpos, nl.rpos)
+
+
+def test_cell_form_overflow_error_is_the_references(gpu_engine, oracle_mod, monkeypatch):
+    """Lists too short for the shell: the cell-list form fills them in the
+    reference's order, so the first overflowing pair and the message are the
+    reference's."""
+    monkeypatch.delenv("ANALISI_GB300_NEIGH_KERNEL", raising=False)
+    from analisi_gb300 import engine
+    w = workloads.small_case(85, 3000, 2, 36.0, 0.2, [1800, 1200])
+    spec = [(5, 3.4 ** 2, 3.6 ** 2), (4, 3.0 ** 2, 3.6 ** 2)]
+    with pytest.raises(oracle_mod.TooManyNeighbours) as eo:
+        oracle_mod.neighbours(w["positions"], w["boxes"], w["type_ids"], 2, 1, spec, True)
+    gpu_engine.set_frames(w["positions"], w["boxes"], w["type_ids"], 2)
+    with pytest.raises(engine.GofrError) as eg:
+        gpu_engine.neighbours(1, spec, True)
+    assert gpu_engine.stats()["kernel_used"] == -2
+    assert str(eg.value).endswith(str(eo.value))
+
+
+def test_cell_form_dense_neighbourhood_falls_back(gpu_engine, oracle_mod, monkeypatch):
+    """A cutoff holding ~400 atoms (more than a warp's survivor buffer): the
+    build reruns in the all-pairs form, lists as the oracle's."""
+    monkeypatch.delenv("ANALISI_GB300_NEIGH_KERNEL", raising=False)
+    w = workloads.small_case(86, 3000, 2, 21.0, 0.1, [1500, 1500])
+    spec = [(300, 6.8 ** 2, 7.0 ** 2), (300, 6.5 ** 2, 7.0 ** 2)]
+    o = oracle_mod.neighbours(w["positions"], w["boxes"], w["type_ids"], 2, 1, spec, False)
+    gpu_engine.set_frames(w["positions"], w["boxes"], w["type_ids"], 2)
+    nl = gpu_engine.neighbours(1, spec, False)
+    assert gpu_engine.stats()["kernel_used"] == -1
+    _full_compare(nl, o, False)
