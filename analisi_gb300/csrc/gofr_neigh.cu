@@ -305,35 +305,93 @@ __global__ void __launch_bounds__(NT) k_neigh_check(const NeighLaunch L)
     }
 }
 
-// stable insertion sort of every list by distance
-__global__ void k_neigh_sort(const NeighLaunch L)
+// Every list sorted by distance, stably (equal distances keep their index
+// order), as the reference's sort.  One warp per list: lane q holds entries
+// q, q + 32, ... (up to SORTC per lane) in registers and their distances in
+// shared memory, ranks each one against the whole list (rank = entries with
+// a smaller distance, or an equal one earlier), then writes it at its rank.
+// A longer list is insertion-sorted by the warp's first lane.
+constexpr int SORTC = 4;
+
+__global__ void __launch_bounds__(NT) k_neigh_sort(const NeighLaunch L)
 {
-    const long long n = (long long)L.N * L.ntypes;
-    for (long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x; g < n;
-         g += (long long)gridDim.x * blockDim.x) {
+    __shared__ double sd[WARPS][32 * SORTC];
+    const int lane = threadIdx.x & 31;
+    double *const d = sd[threadIdx.x >> 5];
+    const long long n_lists = (long long)L.N * L.ntypes;
+    const long long nwarps = (long long)gridDim.x * WARPS;
+    for (long long g = (long long)blockIdx.x * WARPS + (threadIdx.x >> 5); g < n_lists;
+         g += nwarps) {
         const int k = (int)(g / L.N), a = (int)(g - (long long)k * L.N);
         const unsigned long long nk = L.nneigh[k];
         unsigned long long *l = L.list + L.loff[k] + (size_t)a * (nk + 1);
         double *r = L.rpos + L.roff[k] + (size_t)a * nk * 4;
-        const unsigned long long cntk = l[0];
-        for (unsigned long long s = 1; s < cntk; ++s) {
-            const double e0 = r[4 * s], e1 = r[4 * s + 1], e2 = r[4 * s + 2], e3 = r[4 * s + 3];
-            const unsigned long long id = l[1 + s];
-            unsigned long long q = s;
-            while (q > 0 && e0 < r[4 * (q - 1)]) {
-                r[4 * q] = r[4 * (q - 1)];
-                r[4 * q + 1] = r[4 * (q - 1) + 1];
-                r[4 * q + 2] = r[4 * (q - 1) + 2];
-                r[4 * q + 3] = r[4 * (q - 1) + 3];
-                l[1 + q] = l[q];
-                --q;
+        const int n = (int)l[0];
+        if (n <= 1) continue;  // warp-uniform
+        if (n > 32 * SORTC) {
+            if (lane == 0) {
+                for (int s = 1; s < n; ++s) {
+                    const double e0 = r[4 * s], e1 = r[4 * s + 1], e2 = r[4 * s + 2],
+                                 e3 = r[4 * s + 3];
+                    const unsigned long long id = l[1 + s];
+                    int q = s;
+                    while (q > 0 && e0 < r[4 * (q - 1)]) {
+                        r[4 * q] = r[4 * (q - 1)];
+                        r[4 * q + 1] = r[4 * (q - 1) + 1];
+                        r[4 * q + 2] = r[4 * (q - 1) + 2];
+                        r[4 * q + 3] = r[4 * (q - 1) + 3];
+                        l[1 + q] = l[q];
+                        --q;
+                    }
+                    r[4 * q] = e0;
+                    r[4 * q + 1] = e1;
+                    r[4 * q + 2] = e2;
+                    r[4 * q + 3] = e3;
+                    l[1 + q] = id;
+                }
             }
-            r[4 * q] = e0;
-            r[4 * q + 1] = e1;
-            r[4 * q + 2] = e2;
-            r[4 * q + 3] = e3;
-            l[1 + q] = id;
+            __syncwarp();
+            continue;
         }
+        double e0[SORTC], e1[SORTC], e2[SORTC], e3[SORTC];
+        unsigned long long id[SORTC];
+        int rank[SORTC];
+#pragma unroll
+        for (int c = 0; c < SORTC; ++c) {
+            const int q = lane + 32 * c;
+            rank[c] = -1;
+            if (q < n) {
+                e0[c] = r[4 * q];
+                e1[c] = r[4 * q + 1];
+                e2[c] = r[4 * q + 2];
+                e3[c] = r[4 * q + 3];
+                id[c] = l[1 + q];
+                rank[c] = 0;
+                d[q] = e0[c];
+            }
+        }
+        __syncwarp();
+        for (int m = 0; m < n; ++m) {
+            const double v = d[m];
+#pragma unroll
+            for (int c = 0; c < SORTC; ++c) {
+                const int q = lane + 32 * c;
+                if (q < n) rank[c] += (v < e0[c] || (v == e0[c] && m < q)) ? 1 : 0;
+            }
+        }
+        __syncwarp();  // every entry read before any is moved
+#pragma unroll
+        for (int c = 0; c < SORTC; ++c) {
+            if (rank[c] >= 0) {
+                const int q = rank[c];
+                r[4 * q] = e0[c];
+                r[4 * q + 1] = e1[c];
+                r[4 * q + 2] = e2[c];
+                r[4 * q + 3] = e3[c];
+                l[1 + q] = id[c];
+            }
+        }
+        __syncwarp();
     }
 }
 
@@ -365,9 +423,9 @@ int launch_neigh_check(const NeighLaunch &L, int num_sms, cudaStream_t s)
 int launch_neigh_sort(const NeighLaunch &L, int num_sms, cudaStream_t s)
 {
     using namespace neigh;
-    long long n = (long long)L.N * L.ntypes;
-    long long grid = (n + NT - 1) / NT;
-    if (grid > (long long)num_sms * 8) grid = (long long)num_sms * 8;
+    long long n = (long long)L.N * L.ntypes;  // lists, one warp each
+    long long grid = (n + WARPS - 1) / WARPS;
+    if (grid > (long long)num_sms * 16) grid = (long long)num_sms * 16;
     if (grid < 1) return 0;
     k_neigh_sort<<<(unsigned)grid, NT, 0, s>>>(L);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
