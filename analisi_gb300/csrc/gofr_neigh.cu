@@ -305,6 +305,48 @@ __global__ void __launch_bounds__(NT) k_neigh_check(const NeighLaunch L)
     }
 }
 
+// The check in the cell-list form: the same pairs (i < j within either
+// cutoff) come from the 27 cells around i's cell, one warp per first atom;
+// the minimum over them is order-independent.
+__global__ void __launch_bounds__(NT) k_neigh_check_cells(const NeighLaunch L)
+{
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const double *frame = L.pos64 + (size_t)L.timestep * L.N * 3;
+    const double *box = L.box64 + (size_t)L.timestep * 9;
+    const int nx = L.nc[0], ny = L.nc[1], nz = L.nc[2];
+    const int ncell = nx * ny * nz;
+    for (long long s0 = (long long)blockIdx.x * WARPS; s0 < L.N; s0 += (long long)gridDim.x * WARPS) {
+        const int s = (int)(s0 + w);
+        if (s >= L.N) continue;  // warp-uniform
+        const int i = (int)(L.csidt[s] & 0xffffffu);
+        const int ti = L.types[i];
+        int lo = 0, hi = ncell - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (L.cstart[mid] <= s) lo = mid;
+            else hi = mid - 1;
+        }
+        const int cx = lo % nx, cy = (lo / nx) % ny, cz = lo / (nx * ny);
+        for (int c = 0; c < 27; ++c) {
+            const int ux = (cx + c % 3 - 1 + nx) % nx;
+            const int uy = (cy + (c / 3) % 3 - 1 + ny) % ny;
+            const int uz = (cz + c / 9 - 1 + nz) % nz;
+            const int cc = (uz * ny + uy) * nx + ux;
+            const int beg = L.cstart[cc], end = L.cstart[cc + 1];
+            for (int q = beg + lane; q < end; q += 32) {
+                const int j = (int)(L.csidt[q] & 0xffffffu);
+                if (j <= i || !(pair_f32<false>(L, i, j) <= L.hi_f)) continue;
+                const int tj = L.types[j];
+                double x[3];
+                const double d2 = pair_vec<false>(L, frame, box, i, j, x);
+                if (!(d2 <= L.cut2[tj] || d2 <= L.cut2[ti])) continue;
+                if (L.full[(size_t)i * L.ntypes + tj] < j || L.full[(size_t)j * L.ntypes + ti] < i)
+                    atomicMin(L.first_err, (unsigned long long)i * (unsigned long long)L.N + j);
+            }
+        }
+    }
+}
+
 // Every list sorted by distance, stably (equal distances keep their index
 // order), as the reference's sort.  One warp per list: lane q holds entries
 // q, q + 32, ... (up to SORTC per lane) in registers and their distances in
@@ -415,7 +457,8 @@ int launch_neigh_check(const NeighLaunch &L, int num_sms, cudaStream_t s)
     long long grid = (L.N + WARPS - 1) / WARPS;
     if (grid > (long long)num_sms * 16) grid = (long long)num_sms * 16;
     if (grid < 1) return 0;
-    if (L.tric) k_neigh_check<true><<<(unsigned)grid, NT, 0, s>>>(L);
+    if (L.cells && !L.tric && L.prefilter) k_neigh_check_cells<<<(unsigned)grid, NT, 0, s>>>(L);
+    else if (L.tric) k_neigh_check<true><<<(unsigned)grid, NT, 0, s>>>(L);
     else k_neigh_check<false><<<(unsigned)grid, NT, 0, s>>>(L);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }

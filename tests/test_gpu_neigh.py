@@ -194,3 +194,19 @@ def test_cell_form_dense_neighbourhood_falls_back(gpu_engine, oracle_mod, monkey
     nl = gpu_engine.neighbours(1, spec, False)
     assert gpu_engine.stats()["kernel_used"] == -1
     _full_compare(nl, o, False)
+
+
+def test_cell_form_exactly_full_lists(gpu_engine, oracle_mod, monkeypatch):
+    """Capacities equal to the largest list of each type: every such list is
+    full, so the overflow check runs (in the cell-list form) and must find
+    nothing; the lists are the oracle's."""
+    monkeypatch.delenv("ANALISI_GB300_NEIGH_KERNEL", raising=False)
+    w = workloads.small_case(87, 3000, 2, 36.0, 0.2, [1800, 1200])
+    roomy = [(200, 3.4 ** 2, 3.6 ** 2), (200, 3.0 ** 2, 3.6 ** 2)]
+    big = oracle_mod.neighbours(w["positions"], w["boxes"], w["type_ids"], 2, 1, roomy, True)
+    spec = [(max(big.size(a, k) for a in range(3000)), roomy[k][1], roomy[k][2]) for k in range(2)]
+    o = oracle_mod.neighbours(w["positions"], w["boxes"], w["type_ids"], 2, 1, spec, True)
+    gpu_engine.set_frames(w["positions"], w["boxes"], w["type_ids"], 2)
+    nl = gpu_engine.neighbours(1, spec, True)
+    assert gpu_engine.stats()["kernel_used"] == -2
+    _full_compare(nl, o, True)
