@@ -507,8 +507,10 @@ def run_gpu(args):
     kernel_ms, total_ms, cands, rech, pairs, evaluated = [], [], 0, 0, 0, 0
     kernels_used = set()
     barrier()
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-    with Clocks(os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv")) as clk:
+    # raw clock samples of the timed region (the JSON line carries their summary)
+    out_dir = os.environ.get("ANALISI_GB300_BENCH_OUT", os.path.join(ROOT, "bench_out"))
+    os.makedirs(out_dir, exist_ok=True)
+    with Clocks(os.path.join(out_dir, f"clocks_rank{rank}.csv")) as clk:
         for s in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
