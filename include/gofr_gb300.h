@@ -109,7 +109,8 @@ typedef struct gofr_stats {
  * Gofrt object, lib/src/gofrt.cpp:22-31, whose work is per-call here). */
 int gofr_ctx_create(gofr_ctx **out, int device);
 
-/* Releases the context, its stream and all its device memory. */
+/* Releases the context, its stream and all its device memory (the end of a
+ * Gofrt object, Gofrt::~Gofrt, lib/src/gofrt.cpp:33). */
 void gofr_ctx_destroy(gofr_ctx *ctx);
 
 /* Message of the last error on ctx ("" if none); ctx may be NULL for
@@ -127,7 +128,8 @@ int gofr_set_frames(gofr_ctx *ctx, const double *positions, const double *boxes,
                     size_t natoms, size_t nframes);
 
 /* Number of unsigned 64-bit counts gofr_run writes for these parameters
- * (leff * ntypes*(ntypes+1) * nbin, times nparts when nparts > 1). */
+ * (leff * ntypes*(ntypes+1) * nbin, times nparts when nparts > 1): the
+ * product of Gofrt::get_shape, lib/src/gofrt.cpp:65-67. */
 int gofr_output_size(const gofr_ctx *ctx, const gofr_params *p, size_t *n_counts);
 
 /* One Gofrt::calculate(primo) on the resident frames (replaces
@@ -136,12 +138,15 @@ int gofr_output_size(const gofr_ctx *ctx, const gofr_params *p, size_t *n_counts
  * Writes exact counts into the caller's host buffer and returns when done. */
 int gofr_run(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_host);
 
-/* Same as gofr_run, asynchronous: counts go to a caller-owned device buffer
- * of gofr_output_size elements, work is queued on the context's stream.
- * Call gofr_sync before reading the counts. */
+/* Same as gofr_run (Gofrt::calculate, lib/src/gofrt.cpp:74-155), asynchronous:
+ * counts go to a caller-owned device buffer of gofr_output_size elements,
+ * work is queued on the context's stream.  Call gofr_sync before reading the
+ * counts. */
 int gofr_run_device(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_device);
 
-/* Waits for the context's stream and reports device-side errors. */
+/* Waits for the context's stream and reports device-side errors (the join
+ * that ends the reference's CalculateMultiThread::calculate,
+ * lib/include/calculatemultithread.h:106-162, which is synchronous). */
 int gofr_sync(gofr_ctx *ctx);
 
 /* Several Gofrt::calculate windows of the resident frames in one persistent
@@ -154,7 +159,8 @@ int gofr_sync(gofr_ctx *ctx);
 int gofr_run_windows(gofr_ctx *ctx, const gofr_params *p, unsigned nwin,
                      const unsigned long long *primos, unsigned long long *counts_host);
 
-/* Statistics of the last completed run. */
+/* Statistics of the last completed run.  No reference counterpart: the
+ * reference reports no per-run statistics. */
 int gofr_get_stats(const gofr_ctx *ctx, gofr_stats *out);
 
 /* Converts counts to the reference's double result buffer, with
@@ -225,14 +231,19 @@ typedef struct gofr_traj_desc {
     gofr_params params;      /* per-trajectory parameters (kernel and nparts ignored) */
 } gofr_traj_desc;
 
-/* Uploads a batch of trajectories to a context (replacing any frames). */
+/* Uploads a batch of trajectories to a context (replacing any frames).  The
+ * reference runs one Gofrt per trajectory (lib/src/gofrt.cpp:22-31 per object,
+ * the caller's loop, e.g. pyanalisi/common.py:196-203); a batch replaces that
+ * loop. */
 int gofr_batch_set(gofr_ctx *ctx, const gofr_traj_desc *trajs, unsigned ntraj);
 
-/* Number of counts of trajectory k of the current batch, and its offset in
- * the concatenated output of gofr_batch_run. */
+/* Number of counts of trajectory k of the current batch (Gofrt::get_shape,
+ * lib/src/gofrt.cpp:65-67, of that trajectory), and its offset in the
+ * concatenated output of gofr_batch_run. */
 int gofr_batch_output_layout(const gofr_ctx *ctx, unsigned k, size_t *offset, size_t *n_counts);
 
-/* Runs every trajectory of the batch in one persistent launch that pulls
+/* One Gofrt::calculate (lib/src/gofrt.cpp:74-155) per trajectory of the
+ * batch, all in one persistent launch that pulls
  * (trajectory, origin, lag, tile) items from a device work queue.  With
  * use_graph != 0 the launch sequence is captured once into a CUDA graph and
  * replayed.  counts_host receives the concatenation of every trajectory's
@@ -264,7 +275,8 @@ typedef struct gofr_msd_params {
  * options.  nframes and ntypes must match the uploaded frames. */
 int gofr_set_centres(gofr_ctx *ctx, const double *centres, size_t nframes, unsigned ntypes);
 
-/* Number of doubles of the MSD result: leff * (center_of_mass ? 2 : 1) * ntypes. */
+/* Number of doubles of the MSD result: leff * (center_of_mass ? 2 : 1) * ntypes,
+ * the product of MSD::get_shape, lib/include/msd.h:38. */
 int gofr_msd_output_size(const gofr_ctx *ctx, const gofr_msd_params *p, size_t *n);
 
 /* Runs MSD::calculate(primo) on the resident frames (positions as they are,
@@ -293,7 +305,8 @@ typedef struct gofr_neigh_spec {
     double skin2;
 } gofr_neigh_spec;
 
-/* Lengths of the reference's two arrays for these specs (one per type):
+/* Lengths of the reference's two arrays for these specs (one per type), as
+ * the Neighbours constructor sizes them (lib/include/neighbour.h:31-46):
  * list  natoms * (sum nneigh + ntypes) u64: per type k from
  *       list_off[k] = sum_{k'<k} (nneigh[k'] + 1) natoms, per atom i at
  *       list_off[k] + i (nneigh[k] + 1): the list size, then the indices;
@@ -303,7 +316,8 @@ typedef struct gofr_neigh_spec {
 int gofr_neigh_layout(const gofr_ctx *ctx, const gofr_neigh_spec *spec, unsigned nspec,
                       size_t *list_len, size_t *rpos_len);
 
-/* Neighbours::update_neigh(timestep, sort) on the resident frame `timestep`:
+/* Neighbours::update_neigh(timestep, sort), lib/src/neighbour.cpp:9-79, with
+ * the sort of lib/src/neighbour.cpp:49-78, on the resident frame `timestep`:
  * for every atom and neighbour type, the atoms of that type within its cutoff
  * (d2 <= cut2 of the neighbour's type, FP64 minimum image as the reference),
  * in ascending index order, or sorted by distance when sort != 0 (stable);
