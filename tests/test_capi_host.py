@@ -27,6 +27,22 @@ def test_library_exports_every_declared_symbol(built_engine):
     assert sorted(engine.EXPORTED) == decl
 
 
+def test_every_entry_point_cites_what_it_replaces():
+    """Each declaration's comment names the reference interface it replaces
+    (path:line in the analisi tree) or says that there is no counterpart."""
+    src = open(os.path.join(ROOT, "include", "gofr_gb300.h")).read()
+    decls = re.finditer(r"/\*((?:(?!\*/).)*)\*/\s*(?:const\s+)?[a-z_ ]+\*?\s*(gofr_[a-z0-9_]+)\s*\(",
+                        src, flags=re.S)
+    seen = set()
+    for m in decls:
+        comment, name = m.group(1), m.group(2)
+        seen.add(name)
+        if name == "gofr_last_error":
+            continue  # the message accessor of the C ABI's own error convention
+        assert re.search(r"\.(cpp|h|py):\d+", comment) or "counterpart" in comment, name
+    assert seen >= set(declared_symbols()) - {"gofr_last_error"}
+
+
 def test_no_device_is_a_clean_error(built_engine):
     from conftest import HAS_GPU
     if HAS_GPU:
