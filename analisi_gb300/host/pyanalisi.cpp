@@ -98,7 +98,7 @@ std::unique_ptr<Trajectory> make_trajectory(py::buffer pos, py::buffer vel, py::
 py::array_t<double> copy3(const double *p, size_t a, size_t b, size_t c)
 {
     py::array_t<double> out({a, b, c});
-    if (a * b * c) std::memcpy(out.mutable_data(), p, sizeof(double) * a * b * c);
+    if (a * b * c != 0) std::memcpy(out.mutable_data(), p, sizeof(double) * a * b * c);
     return out;
 }
 
