@@ -663,7 +663,9 @@ bool cell_grid(const TrajDev &t, const gofr_params &p, int reach, int nc[3])
         nc[k] = (int)n;
         ncell *= nc[k];
     }
-    return ncell <= (1ll << 22);
+    // at most 6 cells per atom (+64): the per-frame cell starts then take no
+    // more device memory than the frames' FP64 coordinates
+    return ncell <= (1ll << 22) && (double)ncell <= 6.0 * (double)t.N + 64.0;
 }
 
 // Every configuration, fastest (modelled) first.  The cost counts, over all
@@ -2163,13 +2165,18 @@ int gofr_neigh_run(gofr_ctx *ctx, const gofr_neigh_spec *spec, unsigned nspec, s
             q.rmax > 0.0 && cell_grid(t, q, 1, nc)) {
             Plan pl;
             for (int k = 0; k < 3; ++k) pl.nc[k] = nc[k];
-            rc = ensure_cells(ctx, t, pl);
-            if (rc) return rc;
-            const size_t ncell = (size_t)nc[0] * nc[1] * nc[2];
-            L.cells = 1;
-            for (int k = 0; k < 3; ++k) L.nc[k] = nc[k];
-            L.cstart = t.d_cstart + timestep * (ncell + 1);
-            L.csidt = t.d_sidt + timestep * padded_natoms(t.N);
+            if (ensure_cells(ctx, t, pl) == GOFR_OK) {
+                const size_t ncell = (size_t)nc[0] * nc[1] * nc[2];
+                L.cells = 1;
+                for (int k = 0; k < 3; ++k) L.nc[k] = nc[k];
+                L.cstart = t.d_cstart + timestep * (ncell + 1);
+                L.csidt = t.d_sidt + timestep * padded_natoms(t.N);
+            } else {
+                // no room for the cell lists: the all-pairs form (and the failed
+                // allocation's error is not a later launch's)
+                ctx->err.clear();
+                (void)cudaGetLastError();
+            }
         }
     }
     std::memset(&ctx->stats, 0, sizeof ctx->stats);
