@@ -39,10 +39,21 @@ LIB_NAME = "libgofr_gb300.so"
 
 
 def nvcc():
-    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
-    if not os.path.exists(cand):
-        raise RuntimeError("nvcc not found")
-    return cand
+    """nvcc from PATH, else from the CUDA toolkit that $CUDA_HOME / $CUDA_PATH
+    name, else from the toolkit PyTorch was told about (its own lookup)."""
+    cand = shutil.which("nvcc")
+    if cand:
+        return cand
+    homes = [os.environ.get("CUDA_HOME"), os.environ.get("CUDA_PATH")]
+    try:
+        from torch.utils import cpp_extension
+        homes.append(cpp_extension.CUDA_HOME)
+    except Exception:  # torch absent or without CUDA: only the first two
+        pass
+    for h in homes:
+        if h and os.path.exists(os.path.join(h, "bin", "nvcc")):
+            return os.path.join(h, "bin", "nvcc")
+    raise RuntimeError("nvcc not found: put it on PATH or set CUDA_HOME")
 
 
 def _run(cmd, log=None):

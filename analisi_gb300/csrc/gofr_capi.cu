@@ -155,13 +155,16 @@ int fail(gofr_ctx *ctx, int code, const char *fmt, ...)
 
 // Every device allocation of this file goes through here.  Fault-injection
 // hook for tests: with ANALISI_GB300_FAIL_ALLOC=1 in the environment every
-// allocation fails as if the device were out of memory (the error path must
-// leave the context usable).
+// allocation fails as if the device were out of memory, with
+// ANALISI_GB300_FAIL_ALLOC=<tag> only the allocations made with that tag
+// (e.g. "cells": the cell-sorted frames), so that the error paths and the
+// fallbacks can be run without a real shortage; they must leave the context
+// usable.
 template <class T>
-cudaError_t dev_malloc(T **p, size_t bytes)
+cudaError_t dev_malloc(T **p, size_t bytes, const char *tag = nullptr)
 {
     const char *e = std::getenv("ANALISI_GB300_FAIL_ALLOC");
-    if (e && e[0] == '1') {
+    if (e && (std::strcmp(e, "1") == 0 || (tag && std::strcmp(e, tag) == 0))) {
         *p = nullptr;
         return cudaErrorMemoryAllocation;
     }
@@ -850,36 +853,54 @@ int check_device_error(gofr_ctx *ctx)
     return GOFR_OK;
 }
 
-// Builds (once per grid and frames) the cell-sorted copy of t's frames.
+// Builds (once per grid and frames) the cell-sorted copy of t's frames.  On
+// any failure every buffer of the cell lists (kept and temporary) is freed
+// and the trajectory is left without cell lists (cell_nc 0), so a retry
+// starts clean and nothing leaks.
 int ensure_cells(gofr_ctx *ctx, const TrajDev &t, const Plan &pl)
 {
     TrajDev &tm = const_cast<TrajDev &>(t);
     if (tm.cell_nc[0] == pl.nc[0] && tm.cell_nc[1] == pl.nc[1] && tm.cell_nc[2] == pl.nc[2])
         return GOFR_OK;
-    cudaFree(tm.d_cstart); cudaFree(tm.d_sidt); cudaFree(tm.d_spos);
-    tm.d_cstart = nullptr; tm.d_sidt = nullptr; tm.d_spos = nullptr;
-    tm.cell_nc[0] = tm.cell_nc[1] = tm.cell_nc[2] = 0;
+    auto drop_kept = [&tm]() {
+        cudaFree(tm.d_cstart); cudaFree(tm.d_sidt); cudaFree(tm.d_spos);
+        tm.d_cstart = nullptr; tm.d_sidt = nullptr; tm.d_spos = nullptr;
+        tm.cell_nc[0] = tm.cell_nc[1] = tm.cell_nc[2] = 0;
+    };
+    drop_kept();
     const size_t ncell = (size_t)pl.nc[0] * pl.nc[1] * pl.nc[2];
     const size_t NP = padded_natoms(t.N);
     int *cell_of = nullptr, *rank_of = nullptr, *count = nullptr;
-    CK(dev_malloc(&tm.d_cstart, t.T * (ncell + 1) * sizeof(int)));
-    CK(dev_malloc(&tm.d_sidt, t.T * NP * sizeof(unsigned)));
-    CK(dev_malloc(&tm.d_spos, t.T * 3 * NP * sizeof(float)));
-    CK(dev_malloc(&cell_of, t.T * t.N * sizeof(int)));
-    CK(dev_malloc(&rank_of, t.T * t.N * sizeof(int)));
-    CK(dev_malloc(&count, t.T * (ncell + 1) * sizeof(int)));
+    auto drop_temp = [&]() {
+        cudaFree(cell_of); cudaFree(rank_of); cudaFree(count);
+        cell_of = rank_of = count = nullptr;
+    };
+    cudaError_t e = dev_malloc(&tm.d_cstart, t.T * (ncell + 1) * sizeof(int), "cells");
+    if (e == cudaSuccess) e = dev_malloc(&tm.d_sidt, t.T * NP * sizeof(unsigned), "cells");
+    if (e == cudaSuccess) e = dev_malloc(&tm.d_spos, t.T * 3 * NP * sizeof(float), "cells");
+    if (e == cudaSuccess) e = dev_malloc(&cell_of, t.T * t.N * sizeof(int), "cells");
+    if (e == cudaSuccess) e = dev_malloc(&rank_of, t.T * t.N * sizeof(int), "cells");
+    if (e == cudaSuccess) e = dev_malloc(&count, t.T * (ncell + 1) * sizeof(int), "cells");
+    if (e != cudaSuccess) {
+        drop_temp();
+        drop_kept();
+        (void)cudaGetLastError();
+        return fail(ctx, e == cudaErrorMemoryAllocation ? GOFR_ERR_NOMEM : GOFR_ERR_CUDA,
+                    "cell-list allocation failed: %s", cudaGetErrorString(e));
+    }
     ctx->launches += 3;
     double centre[3];
     for (int k = 0; k < 3; ++k) centre[k] = t.h_box[k] + t.h_box[3 + k];  // xlo + L/2
     const int brc = launch_cell_build(t.pos64, t.types8, t.T, t.N, &t.h_box[0], centre, pl.nc,
                                       cell_of, rank_of, count, tm.d_cstart, tm.d_spos,
                                       tm.d_sidt, ctx->stream);
-    cudaStreamSynchronize(ctx->stream);
-    cudaFree(cell_of);
-    cudaFree(rank_of);
-    cudaFree(count);
-    if (brc) return fail(ctx, GOFR_ERR_CUDA, "cell-list build failed: %s",
-                         cudaGetErrorString(cudaGetLastError()));
+    const cudaError_t se = cudaStreamSynchronize(ctx->stream);
+    drop_temp();
+    if (brc || se != cudaSuccess) {
+        drop_kept();
+        return fail(ctx, GOFR_ERR_CUDA, "cell-list build failed: %s",
+                    cudaGetErrorString(se != cudaSuccess ? se : cudaGetLastError()));
+    }
     for (int k = 0; k < 3; ++k) tm.cell_nc[k] = pl.nc[k];
     return GOFR_OK;
 }
@@ -934,6 +955,15 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
     L.primo = (long long)p.primo;
     L.tric = t.tric;
     L.ghist = ghist ? 1 : 0;
+#ifdef GOFR_DEBUG_BOUNDS
+    {
+        // test hook of the debug build: ANALISI_GB300_DEBUG_STALL=1 makes the
+        // all-pairs FP32 kernel's first bounded wait run out with no copy in
+        // flight; the run must end with GOFR_ERR_DEVICE and a usable context
+        const char *st = std::getenv("ANALISI_GB300_DEBUG_STALL");
+        L.dbg_stall = (st && std::strcmp(st, "1") == 0) ? 1 : 0;
+    }
+#endif
     BinMap bm(p.rmin, p.rmax, p.nbin);
     L.rmin = bm.rmin; L.rmax = bm.rmax; L.dr = bm.dr; L.rmin2 = bm.rmin2; L.rmax2 = bm.rmax2;
     if (pl.kind == 0) {
@@ -1182,6 +1212,23 @@ int run_common(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_d
     if (p->kernel == GOFR_KERNEL_TUNED && p->nparts <= 1) {
         rc = tune_plan(ctx, t, *p, pl);
         if (rc) return rc;
+    }
+    if (pl.cells && p->kernel != GOFR_KERNEL_CELL) {
+        // a plan the engine chose (AUTO / TUNED) whose cell lists do not fit
+        // the device: the all-pairs form gives the same counts
+        const int crc = ensure_cells(ctx, t, pl);
+        if (crc == GOFR_ERR_NOMEM) {
+            ctx->err.clear();
+            (void)cudaGetLastError();
+            gofr_params q = *p;
+            q.kernel = GOFR_KERNEL_AUTO;
+            Plan ap;
+            rc = make_plan(ctx, t, q, ap, false);
+            if (rc) return rc;
+            pl = ap;
+        } else if (crc) {
+            return crc;
+        }
     }
     const unsigned nparts = p->nparts > 1 ? p->nparts : 1;
     const size_t n_out = rs.data_length * nparts;
@@ -2165,17 +2212,20 @@ int gofr_neigh_run(gofr_ctx *ctx, const gofr_neigh_spec *spec, unsigned nspec, s
             q.rmax > 0.0 && cell_grid(t, q, 1, nc)) {
             Plan pl;
             for (int k = 0; k < 3; ++k) pl.nc[k] = nc[k];
-            if (ensure_cells(ctx, t, pl) == GOFR_OK) {
+            const int crc = ensure_cells(ctx, t, pl);
+            if (crc == GOFR_OK) {
                 const size_t ncell = (size_t)nc[0] * nc[1] * nc[2];
                 L.cells = 1;
                 for (int k = 0; k < 3; ++k) L.nc[k] = nc[k];
                 L.cstart = t.d_cstart + timestep * (ncell + 1);
                 L.csidt = t.d_sidt + timestep * padded_natoms(t.N);
-            } else {
+            } else if (crc == GOFR_ERR_NOMEM) {
                 // no room for the cell lists: the all-pairs form (and the failed
                 // allocation's error is not a later launch's)
                 ctx->err.clear();
                 (void)cudaGetLastError();
+            } else {
+                return crc;  // a failed cell build is a device error, not a shortage
             }
         }
     }

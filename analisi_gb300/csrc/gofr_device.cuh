@@ -62,10 +62,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
 // Iteration cap of every spin wait: each try_wait suspends for a bounded,
 // hardware-defined time, so the whole wait is bounded (well under a minute).
 constexpr unsigned WAIT_CAP = 1u << 20;
+// Cap of the waits of the debug builds' bounded-wait test (a barrier that no
+// copy completes): the wait and the abort that follows end within microseconds.
+constexpr unsigned DBG_WAIT_CAP = 256u;
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, unsigned parity,
+                                                  unsigned cap = WAIT_CAP)
 {
-    for (unsigned it = 0; it < WAIT_CAP; ++it)
+    for (unsigned it = 0; it < cap; ++it)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }

@@ -65,6 +65,9 @@ struct PairLaunch {
     int wchk;                 // batched kernel: per-pair wrap-decision check on
     int ghist;                // histogram too large for shared memory: atomics go
                               // straight to the u64 counts in global memory
+    int dbg_stall;            // GOFR_DEBUG_BOUNDS builds only: the first tile's
+                              // barrier expects bytes that no copy brings, so the
+                              // bounded wait runs out (test of that path)
 };
 
 // One work descriptor of the batched kernel: origins [k0, k1) of one

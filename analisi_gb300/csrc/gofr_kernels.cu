@@ -308,14 +308,23 @@ __device__ __forceinline__ void f32_init_barriers(const F32Views &V)
 // A bounded wait ran out: a copy may still be in flight into either buffer
 // (the one waited for, and the prefetch of the next tile).  Give both a
 // bounded chance to land before the CTA exits and its shared memory is reused.
-__device__ __forceinline__ void f32_abort(const F32Views &V, const F32Thread &th, unsigned *err)
+__device__ __forceinline__ void f32_abort(const F32Views &V, const F32Thread &th, unsigned *err,
+                                          unsigned cap = WAIT_CAP)
 {
     if (threadIdx.x == 0) {
-        mbar_wait_bounded(&V.bars[0], th.phase0);
-        mbar_wait_bounded(&V.bars[1], th.phase1);
+        mbar_wait_bounded(&V.bars[0], th.phase0, cap);
+        mbar_wait_bounded(&V.bars[1], th.phase1, cap);
         atomicOr(err, ERRW_WAIT_TIMEOUT);
     }
 }
+
+// Debug builds: the bounded-wait test (P.dbg_stall) issues no copy at all, so
+// nothing is ever in flight when its short wait gives up.
+#ifdef GOFR_DEBUG_BOUNDS
+#define GOFR_STALL(P) ((P).dbg_stall != 0)
+#else
+#define GOFR_STALL(P) false
+#endif
 
 // One item: the first atoms of tile `itile` at origin k against every second
 // atom at lag lag_idx, binned into V.hist.  Returns false if a bounded wait
@@ -366,8 +375,12 @@ __device__ __forceinline__ bool f32_item(const PairLaunch &P, const F32Views &V,
 
     const float *fj = P.pos32 + fl * 3 * NP;
     int cnt = 0;
+    const bool stall = GOFR_STALL(P);
+    const unsigned wait_cap = stall ? DBG_WAIT_CAP : WAIT_CAP;
     __syncthreads();  // previous item done with both buffers
-    if (tid == 0) {
+    if (tid == 0 && stall) {
+        mbar_arrive_expect_tx(&V.bars[0], 16u);  // bytes no copy will bring
+    } else if (tid == 0) {
         const int tj = min(TJ32, P.N);
         const unsigned fb = (unsigned)(((tj + 3) & ~3) * 4), tb = (unsigned)((tj + 15) & ~15);
         mbar_arrive_expect_tx(&V.bars[0], 3 * fb + tb);
@@ -379,7 +392,7 @@ __device__ __forceinline__ bool f32_item(const PairLaunch &P, const F32Views &V,
     for (int c = 0; c < nchunks; ++c) {
         const int b = c & 1;
         const int jbase = c * TJ32;
-        if (tid == 0 && c + 1 < nchunks) {
+        if (tid == 0 && c + 1 < nchunks && !stall) {
             const int nb = jbase + TJ32;
             const int tj = min(TJ32, P.N - nb);
             const unsigned fb = (unsigned)(((tj + 3) & ~3) * 4);
@@ -391,7 +404,7 @@ __device__ __forceinline__ bool f32_item(const PairLaunch &P, const F32Views &V,
             bulk_g2s(dst + 2 * TJ32, fj + 2 * NP + nb, fb, &V.bars[b ^ 1]);
             bulk_g2s(V.jt + (b ^ 1) * TJ32, P.types8 + nb, tb, &V.bars[b ^ 1]);
         }
-        const bool ok = mbar_wait_bounded(&V.bars[b], b ? th.phase1 : th.phase0);
+        const bool ok = mbar_wait_bounded(&V.bars[b], b ? th.phase1 : th.phase0, wait_cap);
         if (ok) { if (b) th.phase1 ^= 1u; else th.phase0 ^= 1u; }
         else atomicOr(V.sflag, 1);
         __syncthreads();
@@ -566,7 +579,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f32(const PairLaunch P)
         }
         ++since_flush;
         if (!f32_item<TRI, WCHK>(P, V, th, lag_idx, itile, k)) {
-            f32_abort(V, th, P.err);
+            f32_abort(V, th, P.err, GOFR_STALL(P) ? DBG_WAIT_CAP : WAIT_CAP);
             return;
         }
     }

@@ -38,6 +38,8 @@ constexpr int OFF_ERR = 0;    // unsigned error word
 constexpr int OFF_CHTAB = 256;  // unsigned short [MAX_TYPES][MAX_TYPES]
 constexpr int SCRATCH_BYTES = OFF_CHTAB + MAX_TYPES * MAX_TYPES * 2;
 constexpr int MAX_DEVICES = 64;
+// bit of the error word: a caller's type id outside 0..ntypes-1
+constexpr unsigned ERR_TYPE_ID = 0x100u;
 
 }  // namespace noalloc
 }  // namespace gofr
@@ -137,6 +139,12 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f64_noalloc(const Launch P)
             const double *p = P.pos + (fo * N + a) * 3;
             xi[r] = p[0]; yi[r] = p[1]; zi[r] = p[2];
             ti[r] = P.types[a];
+            // the caller's ids index the channel table: one out of 0..ntypes-1
+            // is reported and its pairs are skipped
+            if (vi[r] && (unsigned)ti[r] >= (unsigned)P.ntypes) {
+                atomicOr(err, ERR_TYPE_ID);
+                vi[r] = false;
+            }
         }
         for (int jbase = 0; jbase < P.N; jbase += TJ) {
             const int tj = min(TJ, P.N - jbase);
@@ -144,12 +152,18 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_f64_noalloc(const Launch P)
             for (int q = tid; q < tj; q += NT) {
                 const double *p = P.pos + (fl * N + jbase + q) * 3;
                 jx[q] = p[0]; jy[q] = p[1]; jz[q] = p[2];
-                jt[q] = P.types[jbase + q];
+                int t = P.types[jbase + q];
+                if ((unsigned)t >= (unsigned)P.ntypes) {
+                    atomicOr(err, ERR_TYPE_ID);
+                    t = -1;
+                }
+                jt[q] = t;
             }
             __syncthreads();
             for (int jj = 0; jj < tj; ++jj) {
                 const double x = jx[jj], y = jy[jj], z = jz[jj];
                 const int tj_ = jt[jj];
+                if (tj_ < 0) continue;  // an invalid id (reported above)
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     if (!vi[r]) continue;
@@ -333,8 +347,10 @@ extern "C" int gofr_run_f64_noalloc(const double *d_positions, const double *d_b
         return GOFR_ERR_CUDA;
     }
     if (errword) {
-        snprintf(msg, msglen, "kernel reported error word 0x%x (minimum-image iteration cap)",
-                 errword);
+        snprintf(msg, msglen, "kernel reported error word 0x%x (%s%s)", errword,
+                 (errword & ERR_TYPE_ID) ? "a type id outside 0..ntypes-1; its pairs were "
+                                           "skipped " : "",
+                 (errword & gofr::ERRW_WRAP_LOOP) ? "minimum-image iteration cap" : "");
         return GOFR_ERR_DEVICE;
     }
     return GOFR_OK;

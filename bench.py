@@ -26,10 +26,11 @@ block-average driver splits a trajectory.
   e2e     the same metric through the C ABI with host buffers: every step
           uploads its 400-frame window from pinned host memory
           (gofr_set_frames) and reads the counts back (gofr_run)
-  roofline  FP32-issue bound of the pair kernel used: 16 FP32 lane operations
-          per ordered pair for the all-pairs kernel (orthorhombic minimum
-          image), 7 per evaluated pair for the cell-list kernel, against the
-          FP32 lane-op peak measured on this GPU by gofr_measure_peaks
+  roofline  FP32-issue bound: 16 FP32 lane operations per ordered pair of
+          the reference loop (all N^2 pairs, orthorhombic minimum image) per
+          mean kernel time, against the FP32 lane-op peak measured on this GPU
+          by gofr_measure_peaks; beside it the kernel's own issue rate over
+          the pairs it evaluated (7 operations each in the cell-list kernel)
   cpu_baseline  the C restatement of the reference (oracle/gofr_oracle.c,
           same fork/join thread split as the reference) on this host's cores,
           on a bounded sample of the same workload
@@ -56,6 +57,18 @@ STEP_WINDOWS = 9  # windows of ORIGINS_PER_STEP origins in reset(1800)
 OPS_PER_PAIR = 16  # orthorhombic FP32 pair: 3 sub + 3x(ffma, fadd, ffma) + fmul + 2 ffma + cmp
 OPS_PER_PAIR_CELL = 7  # cell-list pair, images pre-shifted: 3 sub + fmul + 2 ffma + cmp
 OPS_PER_PAIR_TRI = 19  # triclinic FP32 pair: 3 sub + wrap z (5), y (4), x (3) + 3 for d2 + cmp
+
+
+def _measured_hbm_gbs():
+    """Copy bandwidth of MEASURED_PEAKS.json (GB/s), if the file is there."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+HBM_GBS = _measured_hbm_gbs()
 
 
 def parse():
@@ -588,31 +601,46 @@ def run_gpu(args):
     fp32_peak, satom_peak = engine.measure_peaks(local)
     kernel_used = max(kernels_used) if kernels_used else 0
     evaluated_per_launch = evaluated / args.steps
-    ops_per_pair = OPS_PER_PAIR_CELL if kernel_used == 3 else OPS_PER_PAIR
-    achieved = evaluated_per_launch * ops_per_pair / kernel_avg_s / 1e12
+    ops_eval = OPS_PER_PAIR_CELL if kernel_used == 3 else OPS_PER_PAIR
     peak = fp32_peak / 1e12
+    # the unit of the metric: every ordered pair of the reference loop at the
+    # all-pairs kernel's 16 FP32 operations (orthorhombic minimum image)
+    achieved = pairs_per_launch * OPS_PER_PAIR / kernel_avg_s / 1e12
+    # what the kernel itself issued: its evaluated pairs at its own cost
+    achieved_eval = evaluated_per_launch * ops_eval / kernel_avg_s / 1e12
     traffic = traffic_from_profiles(kernel_used)
+    # algorithmic bytes: each (origin, lag) item reads two FP32 frames
+    # (N x 12 B each); the items of one launch
+    items_per_launch = ORIGINS_PER_STEP * lags
+    algo_bytes = items_per_launch * 2 * N * 12
     roof = {"bound": "fp32", "achieved": round(achieved, 3), "peak": round(peak, 3),
             "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
             "traffic": traffic,
-            "notes": "FP32 lane operations (one FADD/FMUL/FFMA = 1) per evaluated ordered "
-                     "pair: 16 for the all-pairs kernel (minimum image per pair, all N^2 "
-                     "pairs), 7 for the cell-list kernel (images shifted once per tile "
-                     "element; the pairs of the cell neighbourhoods); the binning of the "
-                     "candidates (d <= rmax) is not counted; peak = FFMA issue rate measured "
-                     "on this GPU (gofr_measure_peaks, burst); traffic = ncu dram bytes per "
-                     "launch (profiles/)",
-            "ops_per_evaluated_pair": ops_per_pair,
+            "peak_source": "gofr_measure_peaks: FFMA issue rate measured on this GPU (burst); "
+                           "MEASURED_PEAKS.json holds no FP32 peak",
+            "notes": "achieved = 16 FP32 lane operations (one FADD/FMUL/FFMA = 1) x every "
+                     "ordered pair of the reference loop (N^2 per origin and lag) / mean kernel "
+                     "time: the all-pairs unit of the metric.  The cell-list kernel evaluates "
+                     "only the pairs of neighbouring cells at 7 operations each (images "
+                     "shifted once per tile element); frac_evaluated_pairs is that issue rate "
+                     "against the same peak.  Candidate binning is counted in neither.  "
+                     "traffic = ncu dram bytes per launch (profiles/)",
+            "frac_evaluated_pairs": round(achieved_eval / peak, 4),
+            "achieved_evaluated_pairs": round(achieved_eval, 3),
+            "ops_per_evaluated_pair": ops_eval,
             "kernel": KERNEL_NAMES.get(kernel_used, str(kernel_used)),
+            "pairs_per_launch": int(pairs_per_launch),
             "evaluated_pairs_per_launch": int(evaluated_per_launch),
+            "algorithmic_bytes_per_launch": int(algo_bytes),
+            "traffic_over_algorithmic_bytes": (round(traffic / algo_bytes, 1)
+                                               if traffic else None),
+            "hbm_frac_of_measured": (round(traffic / kernel_avg_s / 1e9 / HBM_GBS, 4)
+                                     if traffic and HBM_GBS else None),
             "smem_atomic_peak_per_s": satom_peak,
             "atomics_needed_per_s": round(cands / (sum(kernel_ms) / 1e3), 1),
             # the all-pairs bound: every N^2 pair at 16 FP32 operations and the
-            # measured peak; the cell-list kernel's all-pairs-equivalent rate
-            # against it says how much of that bound the algorithm recovers
-            "allpairs_bound_gpairs_per_s": round(fp32_peak / OPS_PER_PAIR / 1e9, 1),
-            "kernel_rate_vs_allpairs_bound": round(
-                pairs_per_launch / kernel_avg_s / (fp32_peak / OPS_PER_PAIR), 4)}
+            # measured peak (frac above is the kernel's rate against it)
+            "allpairs_bound_gpairs_per_s": round(fp32_peak / OPS_PER_PAIR / 1e9, 1)}
     cpu = None
     if not args.no_cpu_baseline:
         v, thr, desc, dt = cpu_sample(w, seconds=15.0)

@@ -196,8 +196,11 @@ int gofr_measure_peaks(int device, double *fp32_lane_ops_per_s, double *smem_ato
  * already.  The caller passes its own DEVICE buffers: positions
  * [nframes][natoms][3] and boxes [nframes][6 or 9] in the reference's internal
  * format (as for gofr_set_frames), type ids [natoms] in 0..ntypes-1, and the
- * output counts [leff][ntypes*(ntypes+1)][nbin] (zeroed here).  boxes is read
- * on the device only.  The same exact counts as gofr_run with GOFR_KERNEL_F64.
+ * output counts [leff][ntypes*(ntypes+1)][nbin] (zeroed here).  boxes and the
+ * type ids are read on the device only: an id outside 0..ntypes-1 is found
+ * there, its atom's pairs are skipped and the call returns GOFR_ERR_DEVICE
+ * with a type-id message.  The same exact counts as gofr_run with
+ * GOFR_KERNEL_F64.
  *
  * Nothing is allocated: the only scratch (channel table, error word) is a
  * file-scope __device__ array of 768 bytes that every GPU loading this library

@@ -13,10 +13,10 @@
 # an x86-64 build of the reference does by default; without it GCC on aarch64
 # would fuse d2+=x*x (lib/include/basetrajectory.h:215-217) into FMAs.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default: $ANALISI_REF or /root/reference)
+# Usage: oracle/build_ref.sh REFERENCE_ROOT   (or with $ANALISI_REF set)
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${1:-${ANALISI_REF:-/root/reference}}
+REF=${1:-${ANALISI_REF:?"usage: build_ref.sh REFERENCE_ROOT (or set ANALISI_REF)"}}
 OUT="$HERE/_ref"
 if [ ! -f "$REF/lib/src/gofrt.cpp" ]; then
     echo "reference sources not found at $REF; oracle/_ref not built" >&2

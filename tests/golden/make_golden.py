@@ -121,7 +121,9 @@ def cases():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=os.environ.get("ANALISI_REF", "/root/reference"))
+    ap.add_argument("--ref", default=os.environ.get("ANALISI_REF"),
+                    required="ANALISI_REF" not in os.environ,
+                    help="root of the reference tree (or set ANALISI_REF)")
     args = ap.parse_args()
     pa = load_ref(args.ref)
     for name, pos, types, box, fmt, wrap, g, n, primo in cases():

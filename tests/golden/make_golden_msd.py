@@ -69,7 +69,9 @@ def cases():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=os.environ.get("ANALISI_REF", "/root/reference"))
+    ap.add_argument("--ref", default=os.environ.get("ANALISI_REF"),
+                    required="ANALISI_REF" not in os.environ,
+                    help="root of the reference tree (or set ANALISI_REF)")
     args = ap.parse_args()
     pa = load_ref(args.ref)
     outdir = os.path.join(HERE, "msd")

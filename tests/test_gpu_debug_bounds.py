@@ -76,3 +76,27 @@ def test_debug_build_recheck_queue_overflow(debug_lib, oracle_mod, kernel, monke
         got = e.run(p["rmin"], p["rmax"], p["nbin"], p["tmax"], p["skip"], p["every"],
                     p["ntimesteps"], p["primo"], kernel=kernel)
     np.testing.assert_array_equal(got, _ref(oracle_mod, w, p))
+
+
+def test_bounded_wait_that_runs_out_reports_and_keeps_the_context(debug_lib, oracle_mod,
+                                                                   monkeypatch):
+    """ANALISI_GB300_DEBUG_STALL=1 (debug build only) arms the all-pairs
+    kernel's first tile barrier for bytes that no copy brings: no copy is ever
+    issued, so nothing is in flight when the short bounded wait gives up.  The
+    run returns GOFR_ERR_DEVICE naming the bounded wait, and the same context
+    then gives the oracle's counts."""
+    from analisi_gb300 import engine
+    w = workloads.small_case(97, 1500, 6, 18.0, 0.2, [900, 600], rmin=0.0, rmax=5.0, nbin=45,
+                             tmax=2, skip=2, every=1, ntimesteps=3, primo=0)
+    p = w["params"]
+    args = (p["rmin"], p["rmax"], p["nbin"], p["tmax"], p["skip"], p["every"], p["ntimesteps"],
+            p["primo"])
+    with engine.Engine(0, library=debug_lib) as e:
+        e.set_frames(w["positions"], w["boxes"], w["type_ids"], w["ntypes"])
+        monkeypatch.setenv("ANALISI_GB300_DEBUG_STALL", "1")
+        with pytest.raises(engine.GofrError) as err:
+            e.run(*args, kernel="f32")
+        assert err.value.code == -6 and "bounded wait ran out" in str(err.value)
+        monkeypatch.delenv("ANALISI_GB300_DEBUG_STALL")
+        got = e.run(*args, kernel="f32")
+    np.testing.assert_array_equal(got, _ref(oracle_mod, w, p))
