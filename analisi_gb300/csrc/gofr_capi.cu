@@ -64,6 +64,7 @@ struct TrajDev {
     int *d_cstart = nullptr;
     unsigned *d_sidt = nullptr;
     float *d_spos = nullptr;
+    float4 *d_wpos = nullptr;        // AoS sorted records of the warp-streamed kernel
     // MSD: atoms sorted by type, type starts, optional centres of mass
     std::vector<int> h_perm, h_tbegin, h_types;
     int *d_perm = nullptr, *d_tbegin = nullptr;
@@ -208,6 +209,8 @@ void free_traj(TrajDev &t)
     cudaFree(t.d_cstart);
     cudaFree(t.d_sidt);
     cudaFree(t.d_spos);
+    cudaFree(t.d_wpos);
+    t.d_wpos = nullptr;
     cudaFree(t.d_perm);
     cudaFree(t.d_tbegin);
     cudaFree(t.d_cm);
@@ -626,6 +629,8 @@ struct Plan {
     int reach = 1, cell_r = 4;   // neighbour reach in cells, first atoms per thread
     double cell_fraction = 1.0;  // neighbourhood cells / all cells
     double cell_time = 1e300;    // modelled time / the all-pairs kernel's
+    bool cellw = false;          // the warp-streamed form of the cell-list kernel
+    int wblk[3] = {1, 1, 1}, nw[3] = {1, 1, 1}, parts = 1;  // its warp blocks
     bool wrapcheck = false;
     bool empty = false;        // accepted window empty: nothing can be counted
     Windows w;
@@ -786,6 +791,116 @@ bool cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl)
     return make_cell_plan(t, p, pl, c);
 }
 
+// One configuration of the warp-streamed cell-list kernel: cells of edge >=
+// rmax (1 + 1e-6) / reach, warp blocks of w[0] x w[1] x w[2] cells, r first
+// atoms per lane.
+struct CellwCand {
+    int reach = 1, r = 3;
+    int nc[3] = {0, 0, 0};
+    std::array<int, 3> w{{1, 1, 1}};
+    double fraction = 1.0;  // neighbourhood cells of a warp block / all cells
+    double cost = 1e300;    // lane-pair slots evaluated / N^2 (+ per-chunk overhead)
+};
+
+// Every configuration, cheapest first.  The cost counts, over all warp
+// blocks, the first-atom lane slots a block pays for (its atoms with room for
+// two standard deviations of density fluctuation, rounded up to passes of
+// 32 r) times its neighbourhood's atoms, plus a fixed overhead per staged
+// chunk (a row of the neighbourhood, in one or two pieces), relative to N^2.
+std::vector<CellwCand> cellw_candidates(const TrajDev &t, const gofr_params &p)
+{
+    std::vector<CellwCand> all;
+    // slots carry the neighbour's type in 6 bits
+    if (!cell_eligible(t, p) || t.ntypes > 64) return all;
+    if (cellw_smem_bytes((int)(t.ntypes * (t.ntypes + 1)), (int)p.nbin, (int)t.ntypes) >
+        110 * 1024)
+        return all;  // two CTAs per SM, or not at all
+    for (int m = 1; m <= 3; ++m) {
+        int nc[3];
+        if (!cell_grid(t, p, m, nc)) continue;
+        const double ncell = (double)nc[0] * nc[1] * nc[2];
+        const double per_cell = (double)t.N / ncell;
+        for (int wx = 1; wx <= 4; ++wx)
+            for (int wy = 1; wy <= 4; ++wy)
+                for (int wz = 1; wz <= 4; ++wz) {
+                    if (wx + 2 * m > nc[0] || wy + 2 * m > nc[1] || wz + 2 * m > nc[2]) continue;
+                    if (wy * wz > 16 || (wy + 2 * m) * (wz + 2 * m) > CELLW_MAX_ROWS) continue;
+                    const double atoms = per_cell * wx * wy * wz;
+                    const double rows = (double)(wy + 2 * m) * (wz + 2 * m);
+                    const double row_atoms = per_cell * (wx + 2 * m);
+                    const double nbhd = rows * row_atoms;
+                    const double blocks = (double)((nc[0] + wx - 1) / wx) *
+                                          ((nc[1] + wy - 1) / wy) * ((nc[2] + wz - 1) / wz);
+                    for (int r = 2; r <= 4; ++r) {
+                        const int TI = cellw_warp_atoms(r);
+                        const double passes =
+                            std::ceil(std::max(atoms + 2.0 * std::sqrt(atoms), 1.0) / TI);
+                        // a chunk costs about 24 neighbour records of work beyond its own
+                        const double chunks =
+                            rows * (1.0 + std::floor(row_atoms / 128.0)) + 0.3 * rows;
+                        CellwCand c;
+                        c.reach = m;
+                        c.r = r;
+                        for (int k = 0; k < 3; ++k) c.nc[k] = nc[k];
+                        c.w = {{wx, wy, wz}};
+                        c.fraction = (double)(wx + 2 * m) * (wy + 2 * m) * (wz + 2 * m) / ncell;
+                        c.cost = blocks * passes * TI * (nbhd + 24.0 * chunks) /
+                                 ((double)t.N * t.N);
+                        all.push_back(c);
+                    }
+                }
+    }
+    std::stable_sort(all.begin(), all.end(),
+                     [](const CellwCand &a, const CellwCand &b) { return a.cost < b.cost; });
+    return all;
+}
+
+// ANALISI_GB300_CELLW_PLAN="reach,r,wx,wy,wz" fixes the warp-streamed
+// configuration (reproducible timings); it must be one the planner accepts.
+bool cellw_choice(const TrajDev &t, const gofr_params &p, CellwCand &out)
+{
+    const std::vector<CellwCand> all = cellw_candidates(t, p);
+    if (all.empty()) return false;
+    const char *env = std::getenv("ANALISI_GB300_CELLW_PLAN");
+    int v[5];
+    if (env && std::sscanf(env, "%d,%d,%d,%d,%d", &v[0], &v[1], &v[2], &v[3], &v[4]) == 5)
+        for (const CellwCand &c : all)
+            if (c.reach == v[0] && c.r == v[1] && c.w[0] == v[2] && c.w[1] == v[3] &&
+                c.w[2] == v[4]) {
+                out = c;
+                return true;
+            }
+    out = all.front();
+    return true;
+}
+
+// Turns an FP32 plan into the warp-streamed cell-list form (the block cell
+// kernel's certified bound and windows: the same wrapped coordinates and
+// image moves).
+bool make_cellw_plan(const TrajDev &t, const gofr_params &p, Plan &pl, const CellwCand &c)
+{
+    CellCand cc;
+    cc.reach = c.reach;
+    cc.r = c.r;
+    for (int k = 0; k < 3; ++k) cc.nc[k] = c.nc[k];
+    cc.fraction = c.fraction;
+    cc.time = c.cost;
+    Plan q = pl;
+    if (!make_cell_plan(t, p, q, cc)) return false;
+    q.cellw = true;
+    for (int k = 0; k < 3; ++k) {
+        q.wblk[k] = c.w[k];
+        q.nw[k] = (c.nc[k] + c.w[k] - 1) / c.w[k];
+    }
+    // parts of the warp blocks per (lag, origin): items of fewer than 2^31
+    // all-pairs-equivalent pairs (the kernel checks the evaluated ones)
+    const double n2 = (double)t.N * (double)t.N;
+    q.parts = (int)std::max(1.0, std::ceil(n2 / 2147483648.0));
+    q.parts = std::min(q.parts, q.nw[0] * q.nw[1] * q.nw[2]);
+    pl = q;
+    return true;
+}
+
 // AUTO takes the cell-list form when its modelled time is below this share of
 // the all-pairs kernel's (a margin for the model's error).
 constexpr double kCellAutoTime = 0.85;
@@ -795,7 +910,7 @@ int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl,
 {
     const int req = p.kernel;
     if (req != GOFR_KERNEL_AUTO && req != GOFR_KERNEL_F32_RECHECK && req != GOFR_KERNEL_F64 &&
-        req != GOFR_KERNEL_CELL && req != GOFR_KERNEL_TUNED)
+        req != GOFR_KERNEL_CELL && req != GOFR_KERNEL_TUNED && req != GOFR_KERNEL_CELL_WARP)
         return fail(ctx, GOFR_ERR_ARG, "unknown kernel %d", req);
     if (req == GOFR_KERNEL_TUNED) {
         gofr_params q = p;
@@ -832,7 +947,17 @@ int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl,
         if (cell_plan(t, p, c) && (req == GOFR_KERNEL_CELL || c.cell_time < kCellAutoTime))
             pl = c;
     }
-    if (req == GOFR_KERNEL_CELL && !pl.cells)
+    // the warp-streamed form: on request, and for AUTO wherever the block
+    // cell-list form was taken and the warp form is eligible (measured faster
+    // on every workload where both run)
+    if (allow_cells && !pl.wrapcheck &&
+        (req == GOFR_KERNEL_CELL_WARP || (req == GOFR_KERNEL_AUTO && pl.cells))) {
+        CellwCand c;
+        Plan q = pl;
+        q.cells = false;
+        if (cellw_choice(t, p, c) && make_cellw_plan(t, p, q, c)) pl = q;
+    }
+    if ((req == GOFR_KERNEL_CELL || req == GOFR_KERNEL_CELL_WARP) && !pl.cells)
         return fail(ctx, GOFR_ERR_UNSUPPORTED,
                     "cell lists need an orthorhombic box constant over the frames with at least "
                     "3 cells of edge >= rmax per axis, and nparts <= 1");
@@ -845,11 +970,13 @@ int check_device_error(gofr_ctx *ctx)
     CK(cudaMemcpyAsync(&e, ctx->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     if (e)
-        return fail(ctx, GOFR_ERR_DEVICE, "kernel reported error word 0x%x (%s%s%s%s)", e,
+        return fail(ctx, GOFR_ERR_DEVICE, "kernel reported error word 0x%x (%s%s%s%s%s)", e,
                     (e & ERRW_WAIT_TIMEOUT) ? "bounded wait ran out " : "",
                     (e & ERRW_WRAP_LOOP) ? "minimum-image iteration cap " : "",
                     (e & ERRW_QUEUE) ? "work queue overflow " : "",
-                    (e & ERRW_BOUNDS) ? "debug bounds check failed" : "");
+                    (e & ERRW_BOUNDS) ? "debug bounds check failed " : "",
+                    (e & ERRW_HIST_OVERFLOW) ? "an item evaluated 2^32 pairs or more (run "
+                                               "discarded; use the block cell-list kernel)" : "");
     return GOFR_OK;
 }
 
@@ -860,11 +987,13 @@ int check_device_error(gofr_ctx *ctx)
 int ensure_cells(gofr_ctx *ctx, const TrajDev &t, const Plan &pl)
 {
     TrajDev &tm = const_cast<TrajDev &>(t);
-    if (tm.cell_nc[0] == pl.nc[0] && tm.cell_nc[1] == pl.nc[1] && tm.cell_nc[2] == pl.nc[2])
+    const bool aos = pl.cellw;  // the warp-streamed kernel's records, else the SoA frames
+    if (tm.cell_nc[0] == pl.nc[0] && tm.cell_nc[1] == pl.nc[1] && tm.cell_nc[2] == pl.nc[2] &&
+        (aos ? tm.d_wpos != nullptr : tm.d_spos != nullptr))
         return GOFR_OK;
     auto drop_kept = [&tm]() {
-        cudaFree(tm.d_cstart); cudaFree(tm.d_sidt); cudaFree(tm.d_spos);
-        tm.d_cstart = nullptr; tm.d_sidt = nullptr; tm.d_spos = nullptr;
+        cudaFree(tm.d_cstart); cudaFree(tm.d_sidt); cudaFree(tm.d_spos); cudaFree(tm.d_wpos);
+        tm.d_cstart = nullptr; tm.d_sidt = nullptr; tm.d_spos = nullptr; tm.d_wpos = nullptr;
         tm.cell_nc[0] = tm.cell_nc[1] = tm.cell_nc[2] = 0;
     };
     drop_kept();
@@ -876,8 +1005,12 @@ int ensure_cells(gofr_ctx *ctx, const TrajDev &t, const Plan &pl)
         cell_of = rank_of = count = nullptr;
     };
     cudaError_t e = dev_malloc(&tm.d_cstart, t.T * (ncell + 1) * sizeof(int), "cells");
-    if (e == cudaSuccess) e = dev_malloc(&tm.d_sidt, t.T * NP * sizeof(unsigned), "cells");
-    if (e == cudaSuccess) e = dev_malloc(&tm.d_spos, t.T * 3 * NP * sizeof(float), "cells");
+    if (aos) {
+        if (e == cudaSuccess) e = dev_malloc(&tm.d_wpos, t.T * NP * sizeof(float4), "cells");
+    } else {
+        if (e == cudaSuccess) e = dev_malloc(&tm.d_sidt, t.T * NP * sizeof(unsigned), "cells");
+        if (e == cudaSuccess) e = dev_malloc(&tm.d_spos, t.T * 3 * NP * sizeof(float), "cells");
+    }
     if (e == cudaSuccess) e = dev_malloc(&cell_of, t.T * t.N * sizeof(int), "cells");
     if (e == cudaSuccess) e = dev_malloc(&rank_of, t.T * t.N * sizeof(int), "cells");
     if (e == cudaSuccess) e = dev_malloc(&count, t.T * (ncell + 1) * sizeof(int), "cells");
@@ -891,9 +1024,12 @@ int ensure_cells(gofr_ctx *ctx, const TrajDev &t, const Plan &pl)
     ctx->launches += 3;
     double centre[3];
     for (int k = 0; k < 3; ++k) centre[k] = t.h_box[k] + t.h_box[3 + k];  // xlo + L/2
-    const int brc = launch_cell_build(t.pos64, t.types8, t.T, t.N, &t.h_box[0], centre, pl.nc,
-                                      cell_of, rank_of, count, tm.d_cstart, tm.d_spos,
-                                      tm.d_sidt, ctx->stream);
+    int brc = launch_cell_build(t.pos64, t.types8, t.T, t.N, &t.h_box[0], centre, pl.nc,
+                                cell_of, rank_of, count, tm.d_cstart, tm.d_spos, tm.d_sidt,
+                                ctx->stream);
+    if (!brc && aos)
+        brc = launch_cell_scatter_w(t.pos64, t.types8, t.T, t.N, &t.h_box[0], centre, pl.nc,
+                                    cell_of, rank_of, tm.d_cstart, tm.d_wpos, ctx->stream);
     const cudaError_t se = cudaStreamSynchronize(ctx->stream);
     drop_temp();
     if (brc || se != cudaSuccess) {
@@ -972,6 +1108,36 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
         L.rmin_f = (float)p.rmin;
         L.inv_dr_f = (float)(1.0 / bm.dr);
         L.wlim = (float)(0.5 - pl.b.eta);
+    }
+    if (pl.cells && pl.cellw && !ghist) {
+        int brc = ensure_cells(ctx, t, pl);
+        if (brc) return brc;
+        CellwLaunch C{};
+        C.pair = L;
+        C.pair.a0 = 0;
+        C.pair.a1 = (int)t.N;
+        C.pair.counts = counts;
+        const int nwb = pl.nw[0] * pl.nw[1] * pl.nw[2];
+        // items: (lag, origin, part); at least 8 per SM, so few (lag, origin)
+        // pairs still fill the GPU
+        const long long lo = (long long)L.n_lags * L.n_orig;
+        long long parts = std::max<long long>(pl.parts, (8LL * ctx->num_sms + lo - 1) / lo);
+        parts = std::min<long long>(parts, nwb);
+        C.parts = (int)std::max<long long>(parts, 1);
+        C.pair.n_items = lo * C.parts;
+        C.start = t.d_cstart;
+        C.wpos = t.d_wpos;
+        for (int k = 0; k < 3; ++k) { C.nc[k] = pl.nc[k]; C.w[k] = pl.wblk[k]; C.nw[k] = pl.nw[k]; }
+        C.reach = pl.reach;
+        C.r = pl.cell_r;
+        if (cellw_smem_bytes(L.nch, L.nbin, L.ntypes) > max_smem)
+            return fail(ctx, GOFR_ERR_UNSUPPORTED, "cell-list histogram does not fit shared memory");
+        ++ctx->launches;
+        if (launch_cellw_pairs(C, ctx->num_sms, ctx->stream))
+            return fail(ctx, GOFR_ERR_CUDA, "warp-streamed cell pair kernel launch failed: %s",
+                        cudaGetErrorString(cudaGetLastError()));
+        *pairs_out = (unsigned long long)rs.n_lags * rs.n_orig * t.N * t.N;
+        return GOFR_OK;
     }
     if (pl.cells && !ghist) {
         int brc = ensure_cells(ctx, t, pl);
@@ -1213,7 +1379,7 @@ int run_common(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_d
         rc = tune_plan(ctx, t, *p, pl);
         if (rc) return rc;
     }
-    if (pl.cells && p->kernel != GOFR_KERNEL_CELL) {
+    if (pl.cells && p->kernel != GOFR_KERNEL_CELL && p->kernel != GOFR_KERNEL_CELL_WARP) {
         // a plan the engine chose (AUTO / TUNED) whose cell lists do not fit
         // the device: the all-pairs form gives the same counts
         const int crc = ensure_cells(ctx, t, pl);
@@ -1254,7 +1420,9 @@ int run_common(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_d
     std::memset(&ctx->stats, 0, sizeof ctx->stats);
     ctx->stats.pairs = pairs;
     ctx->stats.evaluated = pairs;
-    ctx->stats.kernel_used = pl.kind == 0 ? (pl.cells ? GOFR_KERNEL_CELL : GOFR_KERNEL_F32_RECHECK)
+    ctx->stats.kernel_used = pl.kind == 0 ? (pl.cells ? (pl.cellw ? GOFR_KERNEL_CELL_WARP
+                                                                  : GOFR_KERNEL_CELL)
+                                                      : GOFR_KERNEL_F32_RECHECK)
                                           : GOFR_KERNEL_F64;
     ctx->stats.wrap_checked = pl.wrapcheck ? 1 : 0;
     ctx->stats.err_bound_d2 = pl.kind == 0 ? pl.w.E_rmax : 0.0;
@@ -1804,7 +1972,9 @@ int gofr_run_windows(gofr_ctx *ctx, const gofr_params *p, unsigned nwin,
         std::memset(&ctx->stats, 0, sizeof ctx->stats);
         ctx->stats.pairs = pairs;
         ctx->stats.evaluated = pairs;
-        ctx->stats.kernel_used = pl.kind == 0 ? (pl.cells ? GOFR_KERNEL_CELL : GOFR_KERNEL_F32_RECHECK)
+        ctx->stats.kernel_used = pl.kind == 0 ? (pl.cells ? (pl.cellw ? GOFR_KERNEL_CELL_WARP
+                                                                      : GOFR_KERNEL_CELL)
+                                                          : GOFR_KERNEL_F32_RECHECK)
                                               : GOFR_KERNEL_F64;
         ctx->stats.wrap_checked = pl.wrapcheck ? 1 : 0;
         rc = gofr_sync(ctx);
@@ -1827,7 +1997,9 @@ int gofr_sync(gofr_ctx *ctx)
     CK(cudaMemcpy(st, ctx->d_stats, sizeof st, cudaMemcpyDeviceToHost));
     ctx->stats.candidates = st[ST_CANDIDATES];
     ctx->stats.rechecks = st[ST_RECHECKS];
-    if (ctx->stats.kernel_used == GOFR_KERNEL_CELL) ctx->stats.evaluated = st[ST_EVALUATED];
+    if (ctx->stats.kernel_used == GOFR_KERNEL_CELL ||
+        ctx->stats.kernel_used == GOFR_KERNEL_CELL_WARP)
+        ctx->stats.evaluated = st[ST_EVALUATED];
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]) == cudaSuccess) ctx->stats.kernel_ms = ms;
     if (cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[3]) == cudaSuccess) ctx->stats.total_ms = ms;

@@ -662,7 +662,8 @@ int launch_cell_build(const double *pos64, const unsigned char *types8, size_t T
         return -1;
     const size_t NP = padded_natoms(N);
     // padding of the sorted frames: NaN coordinates (never read as atoms)
-    if (cudaMemsetAsync(spos, 0xff, T * 3 * NP * sizeof(float), s) != cudaSuccess) return -1;
+    if (spos && cudaMemsetAsync(spos, 0xff, T * 3 * NP * sizeof(float), s) != cudaSuccess)
+        return -1;
     const size_t total = T * N;
     int blocks = (int)((total + NT - 1) / NT);
     if (blocks > 152 * 16) blocks = 152 * 16;
@@ -671,9 +672,11 @@ int launch_cell_build(const double *pos64, const unsigned char *types8, size_t T
                                         box_internal[2], Lx, Ly, Lz, nc[0], nc[1], nc[2], cell_of,
                                         rank_of, count);
     k_cell_scan<<<(unsigned)T, NT, 0, s>>>(count, start, ncell);
-    k_cell_scatter<<<blocks, NT, 0, s>>>(pos64, types8, T, N, NP, ncell, box_internal[0],
-                                         box_internal[1], box_internal[2], Lx, Ly, Lz, centre[0],
-                                         centre[1], centre[2], cell_of, rank_of, start, spos, sidt);
+    if (spos && sidt)
+        k_cell_scatter<<<blocks, NT, 0, s>>>(pos64, types8, T, N, NP, ncell, box_internal[0],
+                                             box_internal[1], box_internal[2], Lx, Ly, Lz,
+                                             centre[0], centre[1], centre[2], cell_of, rank_of,
+                                             start, spos, sidt);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

@@ -1,0 +1,593 @@
+// Warp-streamed cell-list form of the FP32 + FP64-recheck pair kernel.
+//
+// The reference evaluates all N^2 ordered pairs of every (lag, origin)
+// (lib/src/gofrt.cpp:101-102).  As in the block cell-list kernel
+// (gofr_cells.cu), the atoms of every frame are binned into cells of edge
+// >= rmax / reach and sorted by cell, so a pair the reference counts lies in
+// cells at most `reach` apart on every axis; here the unit of neighbourhood
+// is much smaller: each WARP owns a small block of cells (a few cells, about
+// 32 R first atoms) and streams only that block's own neighbourhood, so the
+// pairs evaluated per first atom shrink from the neighbourhood of a CTA-sized
+// block to the neighbourhood of a warp-sized one.
+//
+// Layout per frame (built once per upload and grid): records
+// {x, y, z, type << 24 | atom id} (float4, the coordinates wrapped into the
+// box in FP64 and rounded to FP32 about the box centre, exactly as the block
+// kernel's), sorted by cell, x fastest; cell start offsets.  A row of cells
+// of a neighbourhood is one contiguous run of 16-byte records, so a warp
+// stages it into shared memory with one 1-D bulk copy (TMA, cp.async.bulk)
+// per chunk of CH records, two chunk buffers per warp, completion tracked by
+// one mbarrier per buffer.  Cells reached across the box boundary are the
+// periodic image of the cell: after the copy lands, the warp moves the
+// chunk's records to that image (x += s fl32(L), one FP32 rounding, the
+// block kernel's arithmetic), so the pair arithmetic and its certified error
+// bound (gofr_capi.cu, error_bound_cells) are the block kernel's.
+//
+// Warps never wait for one another inside a work item (lag, origin, part of
+// the warp blocks): they pull warp blocks from a shared counter, stream
+// their own neighbourhoods and add their candidates to the CTA's shared
+// histogram; the CTA synchronises only at the end of the item, to add the
+// histogram to the counts.  Candidates (FP32 d2 <= hi_f) go to per-lane
+// slots carrying d2 and the neighbour's own type and id, so slots outlive
+// the chunk buffers and are binned (the block kernel's certified window
+// test, predicated shared-memory reductions) only when some lane's slots are
+// nearly full or the warp's first atoms change.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "gofr_device.cuh"
+#include "gofr_internal.h"
+
+namespace gofr {
+namespace cellw {
+
+constexpr int NT = 256;
+constexpr int NWARP = NT / 32;
+constexpr int CH = 128;        // neighbour records per chunk buffer
+constexpr int CHP = CH + 4;    // + room for NaN records padding a chunk to a multiple of 4
+constexpr int SLOTS = 16;
+constexpr int QW = 32;         // FP64 recheck queue of a warp
+constexpr int MAXROWS = CELLW_MAX_ROWS;  // neighbourhood rows of a warp block
+constexpr int FLUSH_ILP = 2;
+static_assert(SLOTS % FLUSH_ILP == 0, "a flush round reads rows q0 .. q0 + FLUSH_ILP - 1 < SLOTS");
+
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 f2pk(float a, float b)
+{
+    f2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2up(f2 v, float &a, float &b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2 f2sub(f2 a, f2 b)
+{
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2mul(f2 a, f2 b)
+{
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f2 f2fma(f2 a, f2 b, f2 c)
+{
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// d2 of (i, j0) and (i, j1), second atoms already in the first atom's image:
+// three differences, one multiply, two FMAs, as f32x2 (the block kernel's).
+__device__ __forceinline__ f2 pair2s(f2 xi, f2 yi, f2 zi, f2 xj, f2 yj, f2 zj)
+{
+    const f2 dx = f2sub(xi, xj), dy = f2sub(yi, yj), dz = f2sub(zi, zj);
+    f2 d2 = f2mul(dx, dx);
+    d2 = f2fma(dy, dy, d2);
+    d2 = f2fma(dz, dz, d2);
+    return d2;
+}
+
+__device__ __forceinline__ int wrapi(int a, int n)
+{
+    a %= n;
+    return a < 0 ? a + n : a;
+}
+__device__ __forceinline__ int image_of(int c, int n) { return c < 0 ? -1 : (c >= n ? 1 : 0); }
+
+// Orders this thread's generic-proxy shared-memory accesses before later
+// async-proxy (bulk copy) writes to the same buffer.
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// Shared memory of one warp.
+struct WarpArea {
+    float4 buf[2][CHP];          // chunk buffers (bulk-copy destinations, 16-byte aligned)
+    uint2 slots[SLOTS][32];      // candidates {d2 bits, r << 30 | type << 24 | atom id of j}
+    uint4 q[QW];                 // FP64 recheck queue {ia, ja, channel, 0}
+    unsigned iv[4][32];          // type << 24 | atom id of the first atoms (R <= 4)
+    int2 seg[2 * MAXROWS];       // sorted ranges of the neighbourhood rows (two halves each)
+    uint64_t bar[2];             // one mbarrier per chunk buffer
+    int n[2];                    // records in each buffer
+    int code[2];                 // image of each buffer's records
+    int qn;                      // entries in q
+    int pad[3];
+};
+
+// Chunk walker state (the same values in every lane of a warp).
+struct Walk {
+    int row, half, off;          // current segment (row, half) and offset into it
+};
+
+template <int R>
+__global__ void __launch_bounds__(NT, 2) k_pairs_cellw(const CellwLaunch C, int win_cap,
+                                                       int hist_cap)
+{
+    // first atoms between two checks of the slot counts (one warp vote each)
+    constexpr int VG = R <= 3 ? R : 2;
+    static_assert(4 * VG <= SLOTS - 4, "slots for the candidates between two checks");
+    extern __shared__ __align__(128) unsigned char smem[];
+    WarpArea *const areas = reinterpret_cast<WarpArea *>(smem);
+    float2 *const win = reinterpret_cast<float2 *>(areas + NWARP);
+    unsigned *const hist = reinterpret_cast<unsigned *>(win + win_cap);
+    unsigned short *const chtab = reinterpret_cast<unsigned short *>(hist + hist_cap);
+    __shared__ int s_next, s_abort;
+    __shared__ unsigned long long s_pairs;  // pairs evaluated in the current item
+
+    const PairLaunch &P = C.pair;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    WarpArea &A = areas[warp];
+    const int hlen = P.nch * P.nbin;
+    const int half_ch = P.nch / 2;
+    const float hi_f = P.hi_f;
+    const int ncx = C.nc[0], ncy = C.nc[1], ncz = C.nc[2];
+    const int ncell = ncx * ncy * ncz;
+    const int m = C.reach;
+    const int nwx = C.nw[0], nwy = C.nw[1], nwz = C.nw[2];
+    const int nwb = nwx * nwy * nwz;
+    const long long NP = P.NP;
+
+    for (int i = tid; i < P.nbin; i += NT) win[i] = P.win[i];
+    for (int i = tid; i < hlen; i += NT) hist[i] = 0u;
+    for (int i = tid; i < P.ntypes * P.ntypes; i += NT) chtab[i] = P.chtab[i];
+    if (lane == 0) {
+        mbar_init(&A.bar[0], 1);
+        mbar_init(&A.bar[1], 1);
+        A.qn = 0;
+        fence_mbar_init();
+    }
+    if (tid == 0) s_abort = 0;
+    __syncthreads();
+
+    unsigned ph0 = 0u, ph1 = 0u;      // mbarrier phases of the two buffers
+    bool dead = false;                // a bounded wait of this warp ran out
+    unsigned long long n_cand = 0, n_rech = 0, n_eval = 0;
+    float L32[3];
+    {
+        const Box32 b = P.box32[0];  // the box is the same in every frame
+#pragma unroll
+        for (int a = 0; a < 3; ++a) L32[a] = b.L[a];
+    }
+
+    for (long long g = blockIdx.x; g < P.n_items; g += gridDim.x) {
+        // item = (lag, origin, part): lag slowest
+        const long long per_lag = (long long)P.n_orig * C.parts;
+        const int lag_idx = (int)(g / per_lag);
+        const long long rem = g - (long long)lag_idx * per_lag;
+        const int k = (int)(rem / C.parts);
+        const int part = (int)(rem - (long long)k * C.parts);
+        const int wb0 = (int)((long long)part * nwb / C.parts);
+        const int wb1 = (int)((long long)(part + 1) * nwb / C.parts);
+        const long long fo = P.primo + (long long)k * P.skip;
+        const long long fl = fo + (long long)lag_idx * P.every;
+        const int *st_o = C.start + fo * (long long)(ncell + 1);
+        const int *st_l = C.start + fl * (long long)(ncell + 1);
+        const float4 *rec_o = C.wpos + fo * NP;
+        const float4 *rec_l = C.wpos + fl * NP;
+        if (tid == 0) {
+            s_next = wb0;
+            s_pairs = 0ull;
+        }
+        __syncthreads();
+
+        // Bins every slot of this warp's lanes (each lane its own, FLUSH_ILP
+        // per round), then empties them.
+        int cnt = 0;
+        auto flush_slots = [&]() {
+            const int maxc = __reduce_max_sync(0xffffffffu, (unsigned)cnt);
+            for (int q0 = 0; q0 < maxc; q0 += FLUSH_ILP) {
+                bool ok[FLUSH_ILP], need[FLUSH_ILP];
+                int ch[FLUSH_ILP], bi[FLUSH_ILP], ia[FLUSH_ILP], ja[FLUSH_ILP];
+#pragma unroll
+                for (int u = 0; u < FLUSH_ILP; ++u) {
+                    const bool v = q0 + u < cnt;
+                    // rows < SLOTS (q0 even, SLOTS even): load, then select
+                    const uint2 e = A.slots[q0 + u][lane];
+                    const float d2 = __uint_as_float(v ? e.x : 0x7f800000u);
+                    const unsigned meta = v ? e.y : 0u;
+                    const unsigned iv = A.iv[meta >> 30][lane];
+                    const int t_i = (int)(iv >> 24), t_j = (int)((meta >> 24) & 63u);
+                    ia[u] = (int)(iv & 0xffffffu);
+                    ja[u] = (int)(meta & 0xffffffu);
+                    ch[u] = chtab[t_i * P.ntypes + t_j] + (ia[u] == ja[u] ? half_ch : 0);
+                    const int b_ = __float2int_rd(
+                        __fmul_rn(__fsub_rn(sqrt_guess(d2), P.rmin_f), P.inv_dr_f));
+                    bi[u] = min(max(b_, 0), P.nbin - 1);
+                    const float2 w = win[bi[u]];
+                    const bool test = v && d2 >= P.lo_f;
+                    const bool inw = d2 >= w.x && d2 <= w.y;
+                    ok[u] = test && inw;
+                    need[u] = test && !inw;
+                }
+#pragma unroll
+                for (int u = 0; u < FLUSH_ILP; ++u)
+                    red_shared_add1_if(smem_u32(hist + ch[u] * P.nbin + bi[u]),
+                                       ok[u] && GOFR_CHECK(ch[u] >= 0 && ch[u] < P.nch &&
+                                                               bi[u] >= 0 && bi[u] < P.nbin,
+                                                           P.err));
+                bool any_need = false;
+#pragma unroll
+                for (int u = 0; u < FLUSH_ILP; ++u) any_need |= need[u];
+                if (__any_sync(0xffffffffu, any_need)) {
+#pragma unroll
+                    for (int u = 0; u < FLUSH_ILP; ++u) {
+                        if (!need[u]) continue;
+                        ++n_rech;
+                        const int slot = atomicAdd(&A.qn, 1);
+                        if (slot < QW) {
+                            A.q[slot] = make_uint4((unsigned)ia[u], (unsigned)ja[u],
+                                                   (unsigned)ch[u], 0u);
+                        } else {
+                            const double *xi64 = P.pos64 + (fo * P.N + ia[u]) * 3;
+                            const double *xj64 = P.pos64 + (fl * P.N + ja[u]) * 3;
+                            const double d2d = ref_d2<false>(xi64[0], xi64[1], xi64[2], xj64[0],
+                                                              xj64[1], xj64[2], P.box64 + fo * 9,
+                                                              P.err);
+                            const int bb = ref_bin(d2d, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
+                            if (bb >= 0) atomicAdd(hist + ch[u] * P.nbin + bb, 1u);
+                        }
+                    }
+                }
+            }
+            n_cand += cnt;
+            cnt = 0;
+            __syncwarp();
+        };
+        // Recomputes the warp's queued pairs in exact FP64 (reference arithmetic).
+        auto drain_queue = [&]() {
+            __syncwarp();
+            const int nq = min(A.qn, QW);
+            for (int q = lane; q < nq; q += 32) {
+                const uint4 e = A.q[q];
+                const double *xi64 = P.pos64 + (fo * P.N + (int)e.x) * 3;
+                const double *xj64 = P.pos64 + (fl * P.N + (int)e.y) * 3;
+                const double d2d = ref_d2<false>(xi64[0], xi64[1], xi64[2], xj64[0], xj64[1],
+                                                 xj64[2], P.box64 + fo * 9, P.err);
+                const int bb = ref_bin(d2d, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
+                if (bb >= 0) atomicAdd(hist + (int)e.z * P.nbin + bb, 1u);
+            }
+            __syncwarp();
+            if (lane == 0) A.qn = 0;
+            __syncwarp();
+        };
+
+        while (!dead) {
+            int wb = 0;
+            if (lane == 0) wb = atomicAdd(&s_next, 1);
+            wb = __shfl_sync(0xffffffffu, wb, 0);
+            if (wb >= wb1) break;
+            const int wz = wb / (nwx * nwy), wy = (wb / nwx) % nwy, wx = wb % nwx;
+            const int cx0 = wx * C.w[0], cy0 = wy * C.w[1], cz0 = wz * C.w[2];
+            const int cnx = min(C.w[0], ncx - cx0), cny = min(C.w[1], ncy - cy0),
+                      cnz = min(C.w[2], ncz - cz0);
+            // rows of the warp block (w_y w_z <= 16 of them): lane r holds row
+            // r's range and the inclusive prefix of the row lengths
+            const int nir = cny * cnz;
+            int ib = 0, ilen = 0;
+            if (lane < nir) {
+                const int ry = lane % cny, rz = lane / cny;
+                const int base = ((cz0 + rz) * ncy + (cy0 + ry)) * ncx + cx0;
+                ib = st_o[base];
+                ilen = st_o[base + cnx] - ib;
+            }
+            int ipre = ilen;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, ipre, o);
+                if (lane >= o) ipre += v;
+            }
+            const int n_i = __shfl_sync(0xffffffffu, ipre, 31);
+            if (n_i == 0) continue;
+            // the neighbourhood: rows (y, z) in [cy0 - m, cy0 + cny + m) x
+            // [cz0 - m, cz0 + cnz + m), each the x cells [cx0 - m, cx0 + cnx + m)
+            // in one or two sorted ranges (two when the row wraps the box)
+            const int jny = cny + 2 * m, jnz = cnz + 2 * m, jnx = cnx + 2 * m;
+            const int nrows = jny * jnz;
+            for (int rr = lane; rr < nrows; rr += 32) {
+                const int uy = cy0 - m + rr % jny, uz = cz0 - m + rr / jny;
+                const int base = (wrapi(uz, ncz) * ncy + wrapi(uy, ncy)) * ncx;
+                const int a = wrapi(cx0 - m, ncx), b = a + jnx;
+                if (b <= ncx) {
+                    A.seg[2 * rr] = make_int2(st_l[base + a], st_l[base + b]);
+                    A.seg[2 * rr + 1] = make_int2(0, 0);
+                } else {
+                    A.seg[2 * rr] = make_int2(st_l[base + a], st_l[base + ncx]);
+                    A.seg[2 * rr + 1] = make_int2(st_l[base], st_l[base + b - ncx]);
+                }
+            }
+            __syncwarp();
+            int n_j = 0;
+            for (int s = lane; s < 2 * nrows; s += 32) n_j += A.seg[s].y - A.seg[s].x;
+            n_j = __reduce_add_sync(0xffffffffu, n_j);
+            const int sx0 = image_of(cx0 - m, ncx);
+            // image code of segment (row, half): (sx + 1) | (sy + 1) << 2 | (sz + 1) << 4
+            auto seg_code = [&](int rr, int h) {
+                const int uy = cy0 - m + rr % jny, uz = cz0 - m + rr / jny;
+                return (sx0 + h + 1) | (image_of(uy, ncy) + 1) << 2 | (image_of(uz, ncz) + 1) << 4;
+            };
+            // Advances w to the next non-empty piece and (lane 0) copies it into
+            // buffer b; returns false at the end of the neighbourhood.
+            auto issue = [&](Walk &w, int b) -> bool {
+                while (w.row < nrows) {
+                    const int2 sg = A.seg[2 * w.row + w.half];
+                    const int len = sg.y - sg.x;
+                    if (w.off < len) {
+                        const int n = min(CH, len - w.off);
+                        if (lane == 0) {
+                            A.n[b] = n;
+                            A.code[b] = seg_code(w.row, w.half);
+                            mbar_arrive_expect_tx(&A.bar[b], (unsigned)(n * 16));
+                            bulk_g2s(&A.buf[b][0], rec_l + sg.x + w.off, (unsigned)(n * 16),
+                                     &A.bar[b]);
+                        }
+                        w.off += n;
+                        return true;
+                    }
+                    w.off = 0;
+                    if (++w.half == 2) { w.half = 0; ++w.row; }
+                }
+                return false;
+            };
+
+            for (int ibase = 0; ibase < n_i && !dead; ibase += 32 * R) {
+                // first atoms: r-group r holds atoms ibase + 32 r + lane
+                f2 xi[R], yi[R], zi[R];
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int q = ibase + 32 * r + lane;
+                    // row of atom q (every lane takes part in the shuffles)
+                    const int qq = min(q, n_i - 1);
+                    int row = 0;
+                    for (int rr = 0; rr < nir; ++rr)
+                        row += (qq >= __shfl_sync(0xffffffffu, ipre, rr)) ? 1 : 0;
+                    const int rb = __shfl_sync(0xffffffffu, ib, row);
+                    const int rp = __shfl_sync(0xffffffffu, ipre - ilen, row);
+                    float x, y, z;
+                    unsigned iv = 0x00ffffffu;  // type 0, no atom
+                    if (q < n_i) {
+                        const float4 v = rec_o[rb + (q - rp)];
+                        x = v.x; y = v.y; z = v.z;
+                        iv = __float_as_uint(v.w);
+                    } else {
+                        x = y = z = __int_as_float(0x7fc00000);
+                    }
+                    A.iv[r][lane] = iv;
+                    xi[r] = f2pk(x, x); yi[r] = f2pk(y, y); zi[r] = f2pk(z, z);
+                }
+                if (lane == 0) {
+                    const unsigned long long pe =
+                        (unsigned long long)min(32 * R, n_i - ibase) * (unsigned long long)n_j;
+                    n_eval += pe;
+                    atomicAdd(&s_pairs, pe);
+                }
+                // earlier generic accesses of both buffers (image moves, NaN
+                // tails, reads) before the bulk copies that refill them
+                fence_proxy_async_smem();
+                __syncwarp();
+                Walk w{0, 0, 0};
+                bool have0 = issue(w, 0);
+                bool have1 = have0 && issue(w, 1);
+                for (int c = 0; (c & 1) ? have1 : have0; ++c) {
+                    const int b = c & 1;
+                    const bool ok = mbar_wait_bounded(&A.bar[b], b ? ph1 : ph0);
+                    if (!__all_sync(0xffffffffu, ok)) {
+                        // give the other buffer's copy a bounded chance to land,
+                        // then stop this warp's work (the CTA ends at the item)
+                        if (lane == 0 && (b ? have0 : have1))
+                            mbar_wait_bounded(&A.bar[b ^ 1], b ? ph0 : ph1);
+                        if (lane == 0) {
+                            atomicOr(P.err, ERRW_WAIT_TIMEOUT);
+                            s_abort = 1;
+                        }
+                        dead = true;
+                        break;
+                    }
+                    if (b) ph1 ^= 1u; else ph0 ^= 1u;
+                    const int n = A.n[b];
+                    const int code = A.code[b];
+                    float4 *const bufp = A.buf[b];
+                    if (code != 21) {  // 21: image (0, 0, 0)
+                        const int s0 = (code & 3) - 1, s1 = ((code >> 2) & 3) - 1,
+                                  s2 = ((code >> 4) & 3) - 1;
+                        for (int e = lane; e < n; e += 32) {
+                            float4 v = bufp[e];
+                            if (s0) v.x = __fadd_rn(v.x, s0 > 0 ? L32[0] : -L32[0]);
+                            if (s1) v.y = __fadd_rn(v.y, s1 > 0 ? L32[1] : -L32[1]);
+                            if (s2) v.z = __fadd_rn(v.z, s2 > 0 ? L32[2] : -L32[2]);
+                            bufp[e] = v;
+                        }
+                    }
+                    if (lane < ((n + 3) & ~3) - n)  // no atom: NaN never passes d2 <= hi_f
+                        bufp[n + lane] = make_float4(__int_as_float(0x7fc00000),
+                                                     __int_as_float(0x7fc00000),
+                                                     __int_as_float(0x7fc00000),
+                                                     __uint_as_float(0xffffffffu));
+                    __syncwarp();
+
+                    for (int jj = 0; jj < n; jj += 4) {
+                        const float4 a0 = bufp[jj], a1 = bufp[jj + 1], a2 = bufp[jj + 2],
+                                     a3 = bufp[jj + 3];
+                        const f2 xa = f2pk(a0.x, a1.x), ya = f2pk(a0.y, a1.y), za = f2pk(a0.z, a1.z);
+                        const f2 xb = f2pk(a2.x, a3.x), yb = f2pk(a2.y, a3.y), zb = f2pk(a2.z, a3.z);
+                        const unsigned m0 = __float_as_uint(a0.w), m1 = __float_as_uint(a1.w),
+                                       m2 = __float_as_uint(a2.w), m3 = __float_as_uint(a3.w);
+#pragma unroll
+                        for (int r = 0; r < R; ++r) {
+                            const f2 da = pair2s(xi[r], yi[r], zi[r], xa, ya, za);
+                            const f2 db = pair2s(xi[r], yi[r], zi[r], xb, yb, zb);
+                            float d0, d1, d2v, d3;
+                            f2up(da, d0, d1);
+                            f2up(db, d2v, d3);
+                            const unsigned rm = (unsigned)r << 30;
+                            if (d0 <= hi_f) { A.slots[cnt][lane] = make_uint2(__float_as_uint(d0), m0 | rm); ++cnt; }
+                            if (d1 <= hi_f) { A.slots[cnt][lane] = make_uint2(__float_as_uint(d1), m1 | rm); ++cnt; }
+                            if (d2v <= hi_f) { A.slots[cnt][lane] = make_uint2(__float_as_uint(d2v), m2 | rm); ++cnt; }
+                            if (d3 <= hi_f) { A.slots[cnt][lane] = make_uint2(__float_as_uint(d3), m3 | rm); ++cnt; }
+                            if (!GOFR_CHECK(cnt <= SLOTS, P.err)) cnt = SLOTS;
+                            // room for the next VG first atoms' four candidates each
+                            if ((r + 1) % VG == 0 || r == R - 1)
+                                if (__any_sync(0xffffffffu, cnt > SLOTS - 4 * VG)) flush_slots();
+                        }
+                    }
+                    fence_proxy_async_smem();
+                    __syncwarp();  // every lane done with buffer b
+                    if (b) have1 = issue(w, 1);
+                    else have0 = issue(w, 0);
+                }
+                // the slots refer to this pass's first atoms
+                if (__any_sync(0xffffffffu, cnt > 0)) flush_slots();
+                if (A.qn > QW / 2) drain_queue();
+            }
+        }
+        if (!dead) drain_queue();
+        __syncthreads();  // every warp done with this item
+        // a u32 shared bin holds the item's hits exactly only while the item
+        // evaluated fewer than 2^32 pairs (the host sizes items far below)
+        if (tid == 0 && s_pairs > 0xffffffffull) {
+            atomicOr(P.err, ERRW_HIST_OVERFLOW);
+            s_abort = 1;
+        }
+        __syncthreads();
+        const bool abort = s_abort != 0;
+        // add the item's histogram to its lag's counts, then clear it
+        for (int i = tid; i < hlen; i += NT) {
+            const unsigned v = hist[i];
+            if (v) {
+                if (!abort)
+                    atomicAdd(P.counts + (long long)lag_idx * P.every * hlen + i,
+                              (unsigned long long)v);
+                hist[i] = 0u;
+            }
+        }
+        __syncthreads();
+        if (abort) break;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        n_cand += __shfl_xor_sync(0xffffffffu, n_cand, o);
+        n_rech += __shfl_xor_sync(0xffffffffu, n_rech, o);
+        n_eval += __shfl_xor_sync(0xffffffffu, n_eval, o);
+    }
+    if (lane == 0) {
+        if (n_cand) atomicAdd(P.stats + ST_CANDIDATES, n_cand);
+        if (n_rech) atomicAdd(P.stats + ST_RECHECKS, n_rech);
+        if (n_eval) atomicAdd(P.stats + ST_EVALUATED, n_eval);
+    }
+}
+
+}  // namespace cellw
+
+int cellw_smem_bytes(int nch, int nbin, int ntypes)
+{
+    using namespace cellw;
+    size_t b = sizeof(WarpArea) * NWARP + (size_t)nbin * 8 + (size_t)nch * nbin * 4 +
+               (size_t)ntypes * ntypes * 2;
+    return (int)((b + 127) / 128 * 128);
+}
+
+int cellw_warp_atoms(int r) { return 32 * r; }
+
+// Sorted AoS copy of every frame: {x, y, z, type << 24 | id} with the block
+// kernel's coordinates (w = x - n L, n = floor((x - xlo) / L), one FMA in
+// FP64, then fl32(fl64(w - c)), c the box centre).
+__global__ void k_cell_scatter_w(const double *__restrict__ pos64,
+                                 const unsigned char *__restrict__ types8, size_t T, size_t N,
+                                 size_t NP, int ncell, double xlo, double ylo, double zlo,
+                                 double Lx, double Ly, double Lz, double cx, double cy, double cz,
+                                 const int *__restrict__ cell_of, const int *__restrict__ rank_of,
+                                 const int *__restrict__ start, float4 *__restrict__ wpos)
+{
+    const double lo[3] = {xlo, ylo, zlo}, L[3] = {Lx, Ly, Lz}, c[3] = {cx, cy, cz};
+    for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < T * N;
+         g += (size_t)gridDim.x * blockDim.x) {
+        const size_t f = g / N, a = g - f * N;
+        const size_t d = (size_t)start[f * (size_t)(ncell + 1) + cell_of[g]] + rank_of[g];
+        const double *p = pos64 + g * 3;
+        float v[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const double n = floor(__ddiv_rn(__dsub_rn(p[k], lo[k]), L[k]));
+            const double w = __fma_rn(-n, L[k], p[k]);
+            v[k] = __double2float_rn(__dsub_rn(w, c[k]));
+        }
+        wpos[f * NP + d] =
+            make_float4(v[0], v[1], v[2], __uint_as_float(((unsigned)types8[a] << 24) | (unsigned)a));
+    }
+}
+
+int launch_cell_scatter_w(const double *pos64, const unsigned char *types8, size_t T, size_t N,
+                          const double *box_internal, const double *centre, const int *nc,
+                          const int *cell_of, const int *rank_of, const int *start, float4 *wpos,
+                          cudaStream_t s)
+{
+    const int ncell = nc[0] * nc[1] * nc[2];
+    const size_t NP = padded_natoms(N);
+    // padding records: NaN coordinates (never read as atoms)
+    if (cudaMemsetAsync(wpos, 0xff, T * NP * sizeof(float4), s) != cudaSuccess) return -1;
+    const size_t total = T * N;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    const double Lx = 2.0 * box_internal[3], Ly = 2.0 * box_internal[4], Lz = 2.0 * box_internal[5];
+    k_cell_scatter_w<<<blocks, 256, 0, s>>>(pos64, types8, T, N, NP, ncell, box_internal[0],
+                                            box_internal[1], box_internal[2], Lx, Ly, Lz,
+                                            centre[0], centre[1], centre[2], cell_of, rank_of,
+                                            start, wpos);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int R>
+static int launch_cellw_r(const CellwLaunch &C, int num_sms, cudaStream_t s)
+{
+    using namespace cellw;
+    const int smem = cellw_smem_bytes(C.pair.nch, C.pair.nbin, C.pair.ntypes);
+    if (cudaFuncSetAttribute(k_pairs_cellw<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem) != cudaSuccess)
+        return -1;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairs_cellw<R>, NT, smem) !=
+        cudaSuccess)
+        return -1;
+    if (per_sm < 1) return -2;
+    long long grid = (long long)num_sms * per_sm;
+    if (grid > C.pair.n_items) grid = C.pair.n_items;
+    k_pairs_cellw<R><<<(unsigned)grid, NT, smem, s>>>(C, C.pair.nbin, C.pair.nch * C.pair.nbin);
+    return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_cellw_pairs(const CellwLaunch &C, int num_sms, cudaStream_t s)
+{
+    if (C.pair.n_items <= 0) return 0;
+    switch (C.r) {
+    case 2: return launch_cellw_r<2>(C, num_sms, s);
+    case 3: return launch_cellw_r<3>(C, num_sms, s);
+    case 4: return launch_cellw_r<4>(C, num_sms, s);
+    default: return -3;
+    }
+}
+
+}  // namespace gofr

@@ -12,7 +12,8 @@ enum : unsigned {
     ERRW_WAIT_TIMEOUT = 1u,   // a bounded mbarrier wait ran out
     ERRW_WRAP_LOOP = 2u,      // the FP64 iterative minimum image exceeded its iteration cap
     ERRW_QUEUE = 4u,          // a work queue overflowed its capacity
-    ERRW_BOUNDS = 8u          // a debug bounds check failed (GOFR_DEBUG_BOUNDS builds only)
+    ERRW_BOUNDS = 8u,         // a debug bounds check failed (GOFR_DEBUG_BOUNDS builds only)
+    ERRW_HIST_OVERFLOW = 16u  // an item could have overflowed a u32 shared bin (run discarded)
 };
 
 // Debug builds (-DGOFR_DEBUG_BOUNDS): GOFR_CHECK(cond, err) records a failed
@@ -90,6 +91,29 @@ struct CellLaunch {
     int r;                         // first atoms per thread (2, 3 or 4)
 };
 
+// One launch of the warp-streamed cell-list kernel (gofr_cellw.cu): items
+// are (lag, origin, part), pair.n_items = n_lags * n_orig * parts; each warp
+// takes blocks of w[0] x w[1] x w[2] cells of the part's range.
+constexpr int CELLW_MAX_ROWS = 64;  // neighbourhood rows (w_y + 2 reach)(w_z + 2 reach)
+struct CellwLaunch {
+    PairLaunch pair;
+    const int *start;              // [T][ncell+1] sorted-record offset of each cell
+    const float4 *wpos;            // [T][NP] {x, y, z, type << 24 | atom id} sorted by cell
+    int nc[3];                     // cells per axis
+    int w[3];                      // cells per warp block per axis
+    int nw[3];                     // warp blocks per axis
+    int reach;                     // neighbour cells per side
+    int r;                         // first atoms per lane (2, 3 or 4)
+    int parts;                     // parts of the warp blocks per (lag, origin)
+};
+int cellw_smem_bytes(int nch, int nbin, int ntypes);
+int cellw_warp_atoms(int r);
+int launch_cell_scatter_w(const double *pos64, const unsigned char *types8, size_t T, size_t N,
+                          const double *box_internal, const double *centre, const int *nc,
+                          const int *cell_of, const int *rank_of, const int *start, float4 *wpos,
+                          cudaStream_t s);
+int launch_cellw_pairs(const CellwLaunch &C, int num_sms, cudaStream_t s);
+
 int cell_smem_bytes(int nch, int nbin, int ntypes);
 int cell_block_atoms(int r);
 int cell_max_ranges();
@@ -143,6 +167,9 @@ int launch_neigh_build(const NeighLaunch &L, int num_sms, cudaStream_t s);
 int launch_neigh_check(const NeighLaunch &L, int num_sms, cudaStream_t s);
 int launch_neigh_sort(const NeighLaunch &L, int num_sms, cudaStream_t s);
 
+// Cell assignment and per-frame cell starts (and, with spos/sidt non-null,
+// the block kernel's SoA sorted frames); cell_of and rank_of are left for
+// launch_cell_scatter_w.
 int launch_cell_build(const double *pos64, const unsigned char *types8, size_t T, size_t N,
                       const double *box_internal, const double *centre, const int *nc,
                       int *cell_of, int *rank_of, int *count, int *start, float *spos,

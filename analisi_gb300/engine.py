@@ -19,7 +19,7 @@ STATUS = {
     -8: "GOFR_ERR_NEIGH_FULL",
 }
 BOX_ORTHO, BOX_TRICLINIC = 0, 1
-KERNELS = {"auto": 0, "f32": 1, "f64": 2, "cell": 3, "tuned": 4}
+KERNELS = {"auto": 0, "f32": 1, "f64": 2, "cell": 3, "tuned": 4, "cellw": 5}
 
 # every symbol the header declares (checked by the CPU tests)
 EXPORTED = [

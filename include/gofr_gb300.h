@@ -65,13 +65,19 @@ enum gofr_kernel {
     GOFR_KERNEL_CELL = 3,        /* cell-list FP32 + recheck kernel (error if not eligible);
                                     ANALISI_GB300_CELL_PLAN="reach,r,bx,by,bz" pins its
                                     configuration when that one is eligible */
-    GOFR_KERNEL_TUNED = 4        /* AUTO, but the all-pairs / cell-list form and the cell
+    GOFR_KERNEL_TUNED = 4,       /* AUTO, but the all-pairs / cell-list form and the cell
                                     configuration are picked by timing them on a sample of
                                     the job; the choice is remembered per key
                                     (log2 N, nbin, ntypes, box kind, cell grid) in the
                                     process and, when the environment variable
                                     ANALISI_GB300_TUNE_CACHE names a file, across runs
                                     (ANALISI_GB300_TUNE_LOG: a file for every timing) */
+    GOFR_KERNEL_CELL_WARP = 5    /* warp-streamed cell-list FP32 + recheck kernel: each warp
+                                    streams the neighbourhood of its own small block of cells
+                                    (error if not eligible: the cell-list conditions and at
+                                    most 64 types); AUTO takes it wherever it would take the
+                                    block cell-list form.  ANALISI_GB300_CELLW_PLAN=
+                                    "reach,r,wx,wy,wz" pins its configuration */
 };
 
 /* Parameters of one Gofrt::calculate (lib/include/gofrt.h:37-45 constructor

@@ -65,13 +65,15 @@ def _check_samples(eng, oracle_mod, w, samples, kernels):
 
 def test_c2_16k_atoms_default_plan_all_pairs_and_fp64(gpu_engine, oracle_mod):
     """16384 atoms (16352/16/16), L=54.72, 400 bins on [0, 12]: origins 0 and
-    1000, lags {0, 1, 100, 199}.  The default plan is the cell-list kernel the
-    benchmark times (9^3 cells, reach 2)."""
+    1000, lags {0, 1, 100, 199}, through the default plan (the warp-streamed
+    cell-list kernel the benchmark times), the block cell-list kernel, the
+    all-pairs FP32 kernel and plain FP64."""
     w = workloads.c2()
     gpu_engine.set_frames(w["positions"], w["boxes"], w["type_ids"], w["ntypes"])
     samples = [(o, lag) for o in (0, 1000) for lag in (1, 100, 199)]
-    used = _check_samples(gpu_engine, oracle_mod, w, samples, ["auto", "f32", "f64"])
-    assert used == {"auto": {3}, "f32": {1}, "f64": {2}}
+    used = _check_samples(gpu_engine, oracle_mod, w, samples, ["auto", "cell", "cellw", "f32",
+                                                               "f64"])
+    assert used == {"auto": {5}, "cell": {3}, "cellw": {5}, "f32": {1}, "f64": {2}}
 
 
 def test_c3_32k_atoms_triclinic(gpu_engine, oracle_mod):
@@ -88,8 +90,8 @@ def test_c3_32k_atoms_triclinic(gpu_engine, oracle_mod):
 
 def test_c5_131k_atoms_cells_against_fp64_all_pairs(gpu_engine, oracle_mod):
     """131072 atoms (4 x 25 %), L=109.47, 250 bins on [0, 10]: origin 0, lags
-    {0, 24, 48} through the cell-list kernel and the all-pairs FP64 kernel,
-    both against the oracle."""
+    {0, 24, 48} through both cell-list kernels, the default plan and the
+    all-pairs FP64 kernel, all against the oracle."""
     w = workloads.c5()
     gpu_engine.set_frames(w["positions"], w["boxes"], w["type_ids"], w["ntypes"])
     p = dict(w["params"])
@@ -99,8 +101,11 @@ def test_c5_131k_atoms_cells_against_fp64_all_pairs(gpu_engine, oracle_mod):
     cell, st = _gpu(gpu_engine, p, "cell")
     assert st["kernel_used"] == 3 and st["evaluated"] < st["pairs"] // 10
     np.testing.assert_array_equal(cell, ref)
+    cellw, st = _gpu(gpu_engine, p, "cellw")
+    assert st["kernel_used"] == 5 and st["evaluated"] < st["pairs"] // 20
+    np.testing.assert_array_equal(cellw, ref)
     auto, st = _gpu(gpu_engine, p, "auto")
-    assert st["kernel_used"] == 3
+    assert st["kernel_used"] == 5
     np.testing.assert_array_equal(auto, ref)
     f64, st = _gpu(gpu_engine, p, "f64")
     assert st["kernel_used"] == 2

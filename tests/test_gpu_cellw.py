@@ -1,0 +1,124 @@
+"""Warp-streamed cell-list kernel (GOFR_KERNEL_CELL_WARP): each warp streams
+the neighbourhood of its own small block of cells through 1-D bulk copies.
+Counts must equal the oracle's for every configuration: reach 1, 2 and 3, 2
+to 4 first atoms per lane, warp blocks whose neighbourhood wraps the box on
+every axis, several passes of first atoms per block, shifted and non-cubic
+boxes, unwrapped coordinates far outside the box, and thousands of FP64
+rechecks (a warp's recheck queue overflowing)."""
+import numpy as np
+import pytest
+
+from analisi_gb300 import workloads
+
+from test_gpu_cells import CASES, copies_on_thresholds
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(eng, w, kernel):
+    p = w["params"]
+    eng.set_frames(w["positions"], w["boxes"], w["type_ids"], w["ntypes"])
+    c = eng.run(p["rmin"], p["rmax"], p["nbin"], p["tmax"], p["skip"], p["every"],
+                p["ntimesteps"], p["primo"], kernel=kernel)
+    return c, eng.stats()
+
+
+def _ref(oracle_mod, w):
+    p = w["params"]
+    return oracle_mod.gofrt_counts(w["positions"], w["boxes"], w["type_ids"], w["ntypes"],
+                                   p["rmin"], p["rmax"], p["nbin"], p["tmax"], 8, p["skip"],
+                                   p["every"], p["ntimesteps"], p["primo"])
+
+
+# "reach,r,wx,wy,wz" through ANALISI_GB300_CELLW_PLAN (None: the planner's
+# choice); (1,2,1,1,1) with few first atoms per lane makes several passes
+PLANS = [None, "1,2,1,1,1", "1,4,2,2,1", "2,3,1,2,2", "2,2,3,1,1", "2,4,2,2,2", "3,3,2,2,2"]
+
+
+@pytest.mark.parametrize("plan", PLANS, ids=[str(p) for p in PLANS])
+@pytest.mark.parametrize("case", CASES, ids=[str(c[0]) for c in CASES])
+def test_cellw_matches_oracle(gpu_engine, oracle_mod, case, plan, monkeypatch):
+    if plan is None:
+        monkeypatch.delenv("ANALISI_GB300_CELLW_PLAN", raising=False)
+    else:
+        monkeypatch.setenv("ANALISI_GB300_CELLW_PLAN", plan)
+    seed, N, T, L, sigma, counts, params = case
+    w = workloads.small_case(seed, N, T, L, sigma, counts, **params)
+    if seed == 62:  # shifted, non-cubic box
+        w["boxes"] = w["boxes"].copy()
+        w["boxes"][:, 0] -= 3.0
+        w["boxes"][:, 4] *= 1.08
+    ref = _ref(oracle_mod, w)
+    got, st = _run(gpu_engine, w, "cellw")
+    assert st["kernel_used"] == 5
+    assert st["evaluated"] <= st["pairs"]
+    np.testing.assert_array_equal(got, ref)
+
+
+@pytest.mark.parametrize("plan", [None, "1,3,1,1,1", "2,2,2,1,2"])
+def test_cellw_far_unwrapped_coordinates(gpu_engine, oracle_mod, plan, monkeypatch):
+    """Atoms several box lengths outside a box that is not at the origin."""
+    if plan is None:
+        monkeypatch.delenv("ANALISI_GB300_CELLW_PLAN", raising=False)
+    else:
+        monkeypatch.setenv("ANALISI_GB300_CELLW_PLAN", plan)
+    w = workloads.small_case(65, 2400, 7, 26.0, 0.4, [1500, 900], rmin=0.3, rmax=5.0, nbin=45,
+                             tmax=3, skip=2, every=1, ntimesteps=4, primo=0)
+    rng = np.random.default_rng(650)
+    L = 26.0
+    w["positions"] = w["positions"] + L * rng.integers(-4, 5, size=(1, 2400, 3))
+    w["boxes"] = w["boxes"].copy()
+    w["boxes"][:, 0:3] += np.array([-7.5, 3.25, 11.0])
+    w["positions"] = w["positions"] + np.array([-7.5, 3.25, 11.0])
+    ref = _ref(oracle_mod, w)
+    assert ref.sum() > 0
+    got, st = _run(gpu_engine, w, "cellw")
+    assert st["kernel_used"] == 5
+    np.testing.assert_array_equal(got, ref)
+
+
+@pytest.mark.parametrize("plan", ["2,3,2,2,2", "1,4,1,1,1"])
+def test_cellw_many_rechecks(gpu_engine, oracle_mod, plan, monkeypatch):
+    """Copies of every atom on bin thresholds: thousands of FP64 rechecks per
+    item, far more than a warp's queue holds between drains."""
+    monkeypatch.setenv("ANALISI_GB300_CELLW_PLAN", plan)
+    copies = 12
+    w = copies_on_thresholds(copies)
+    N = w["positions"].shape[1]
+    ref = _ref(oracle_mod, w)
+    got, st = _run(gpu_engine, w, "cellw")
+    assert st["kernel_used"] == 5
+    assert st["rechecks"] >= N * (copies - 1)
+    np.testing.assert_array_equal(got, ref)
+
+
+def test_cellw_small_boxes(gpu_engine, oracle_mod):
+    """L = 10 with rmax = 4 has a grid only at reach 3 (7 cells of 1.43): the
+    warp kernel takes it and counts exactly; L = 7 (L/2 < rmax) has none, and
+    the forced kernel refuses."""
+    from analisi_gb300 import engine
+    w = workloads.small_case(64, 200, 6, 10.0, 0.1, [200], rmin=0.0, rmax=4.0, nbin=10, tmax=2,
+                             skip=1, every=1, ntimesteps=3, primo=0)
+    got, st = _run(gpu_engine, w, "cellw")
+    assert st["kernel_used"] == 5
+    np.testing.assert_array_equal(got, _ref(oracle_mod, w))
+    w = workloads.small_case(64, 100, 6, 7.0, 0.1, [100], rmin=0.0, rmax=4.0, nbin=10, tmax=2,
+                             skip=1, every=1, ntimesteps=3, primo=0)
+    with pytest.raises(engine.GofrError):
+        _run(gpu_engine, w, "cellw")
+
+
+def test_cellw_windows_and_debug_free_stats(gpu_engine, oracle_mod):
+    """Several calculate(primo) windows of one trajectory through the warp
+    kernel (one launch per window) equal the oracle's windows."""
+    seed, N, T, L, sigma, counts, params = CASES[0]
+    w = workloads.small_case(seed, N, T, L, sigma, counts, **params)
+    p = w["params"]
+    gpu_engine.set_frames(w["positions"], w["boxes"], w["type_ids"], w["ntypes"])
+    primos = [0, 1, 3]
+    got = gpu_engine.run_windows(p["rmin"], p["rmax"], p["nbin"], 2, 2, 1, 4, primos,
+                                 kernel="cellw")
+    for k, pr in enumerate(primos):
+        ref = oracle_mod.gofrt_counts(w["positions"], w["boxes"], w["type_ids"], w["ntypes"],
+                                      p["rmin"], p["rmax"], p["nbin"], 2, 4, 2, 1, 4, pr)
+        np.testing.assert_array_equal(got[k], ref)
