@@ -98,6 +98,10 @@ struct gofr_ctx {
     double *d_minmax = nullptr;
     unsigned *d_nonfinite = nullptr;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // a second stream for the batch's warp-streamed cell-list members, forked
+    // from and joined back into `stream` (also inside a captured graph)
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     gofr_stats stats{};
     size_t batch_total = 0;
     unsigned long long launches = 0;  // kernels launched on this context
@@ -123,6 +127,9 @@ struct gofr_ctx {
         CellLaunch *d_cells = nullptr;
         long long *d_cell_end = nullptr;
         long long cell_items = 0;
+        // members run by the warp-streamed cell-list kernel, one launch each,
+        // largest first, on the second stream
+        std::vector<CellwLaunch> cellw;
         unsigned long long allpairs_pairs = 0;  // pairs of the members not run with cells
         int cell_r = 3, cell_max_nbin = 1, cell_max_nch = 1, cell_max_ntypes = 1, cell_grid = 0;
     } batch;
@@ -1606,7 +1613,49 @@ int build_batch(gofr_ctx *ctx)
         L.tric = t.tric;
         L.wchk = pl.wrapcheck ? 1 : 0;
     }
-    // cell-list members: sorted frames, one record each, their items back to back
+    // cell-list members: the warp-streamed kernel where it is eligible (one
+    // launch per member), else the block kernel (all such members' items back
+    // to back in one launch)
+    std::vector<int> block_members;
+    std::vector<std::pair<unsigned long long, CellwLaunch>> wl;
+    for (int k : B.cell_trajs) {
+        TrajDev &t = ctx->trajs[k];
+        const RunShape &rs = shapes[k];
+        gofr_params p = t.params;
+        p.kernel = GOFR_KERNEL_AUTO;
+        p.nparts = 1;
+        CellwCand cw;
+        Plan q = plans[k];
+        q.cells = false;
+        if (!(cellw_choice(t, p, cw) && make_cellw_plan(t, p, q, cw))) {
+            block_members.push_back(k);
+            continue;
+        }
+        int rc = ensure_cells(ctx, t, q);
+        if (rc) return rc;
+        CellwLaunch C{};
+        C.pair = B.launches[k];
+        C.pair.win = B.d_win + win_off[k];  // the windows of the block plan: same bound
+        const long long lo = (long long)rs.n_lags * rs.n_orig;
+        const int nwb = q.nw[0] * q.nw[1] * q.nw[2];
+        long long parts = std::max<long long>(q.parts, (8LL * ctx->num_sms + lo - 1) / lo);
+        C.parts = (int)std::max<long long>(std::min<long long>(parts, nwb), 1);
+        C.pair.n_items = lo * C.parts;
+        C.start = t.d_cstart;
+        C.wpos = t.d_wpos;
+        for (int a = 0; a < 3; ++a) { C.nc[a] = q.nc[a]; C.w[a] = q.wblk[a]; C.nw[a] = q.nw[a]; }
+        C.reach = q.reach;
+        C.r = q.cell_r;
+        wl.push_back({(unsigned long long)work[k], C});
+        B.launches[k] = PairLaunch{};  // not in the all-pairs queue
+    }
+    std::stable_sort(wl.begin(), wl.end(),
+                     [](const std::pair<unsigned long long, CellwLaunch> &a,
+                        const std::pair<unsigned long long, CellwLaunch> &b) {
+                         return a.first > b.first;
+                     });
+    for (auto &e : wl) B.cellw.push_back(e.second);
+    B.cell_trajs = block_members;
     std::vector<long long> cell_end;
     for (int k : B.cell_trajs) {
         TrajDev &t = ctx->trajs[k];
@@ -1677,6 +1726,18 @@ int enqueue_batch(gofr_ctx *ctx)
     CK(cudaMemsetAsync(ctx->d_stats, 0, ST_COUNT * sizeof(unsigned long long), ctx->stream));
     CK(cudaMemsetAsync(B.d_head, 0, 2 * sizeof(unsigned), ctx->stream));
     CK(cudaMemsetAsync(B.d_counts, 0, std::max<size_t>(ctx->batch_total, 1) * 8, ctx->stream));
+    if (!B.cellw.empty()) {
+        // the warp-streamed members on the second stream, alongside the rest
+        CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
+        CK(cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0));
+        for (const CellwLaunch &C : B.cellw) {
+            ++ctx->launches;
+            if (launch_cellw_pairs(C, ctx->num_sms, ctx->stream2))
+                return fail(ctx, GOFR_ERR_CUDA, "batched warp cell-list launch failed: %s",
+                            cudaGetErrorString(cudaGetLastError()));
+        }
+        CK(cudaEventRecord(ctx->ev_join, ctx->stream2));
+    }
     for (int v = 0; v < 2; ++v) {
         if (B.work[v].empty()) continue;
         ++ctx->launches;
@@ -1709,6 +1770,7 @@ int enqueue_batch(gofr_ctx *ctx)
         rc = enqueue_run(ctx, t, p, rs, pl, B.d_counts + t.out_offset, &pairs);
         if (rc) return rc;
     }
+    if (!B.cellw.empty()) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
     CK(cudaMemcpyAsync(B.h_stage, B.d_counts, ctx->batch_total * 8, cudaMemcpyDeviceToHost,
                        ctx->stream));
     return GOFR_OK;
@@ -1742,6 +1804,9 @@ int gofr_ctx_create(gofr_ctx **out, int device)
         }
         bool ok = true;
         for (auto &e : ctx->ev) ok = ok && cudaEventCreate(&e) == cudaSuccess;
+        ok = ok && cudaStreamCreateWithFlags(&ctx->stream2, cudaStreamNonBlocking) == cudaSuccess;
+        ok = ok && cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) == cudaSuccess;
+        ok = ok && cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) == cudaSuccess;
         ok = ok && dev_malloc(&ctx->d_err, sizeof(unsigned)) == cudaSuccess;
         ok = ok && dev_malloc(&ctx->d_stats, ST_COUNT * sizeof(unsigned long long)) == cudaSuccess;
         ok = ok && dev_malloc(&ctx->d_minmax, 256 * 6 * sizeof(double)) == cudaSuccess;
@@ -1779,8 +1844,12 @@ void gofr_ctx_destroy(gofr_ctx *ctx)
         cudaFree(ctx->d_nl_cut2);
         cudaFree(ctx->d_nl_full);
 
+        if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
         for (auto &e : ctx->ev)
             if (e) cudaEventDestroy(e);
+        if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+        if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+        if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
         if (ctx->stream) cudaStreamDestroy(ctx->stream);
     }
     delete ctx;
@@ -2158,7 +2227,7 @@ int gofr_batch_run(gofr_ctx *ctx, int use_graph, unsigned long long *counts_host
     if (use_graph) {
         CK(cudaGraphLaunch(B.graph, ctx->stream));
         ctx->launches += (B.work[0].empty() ? 0 : 1) + (B.work[1].empty() ? 0 : 1) +
-                         (B.cells.empty() ? 0 : 1) + B.f64_trajs.size();
+                         (B.cells.empty() ? 0 : 1) + B.f64_trajs.size() + B.cellw.size();
     } else {
         int rc = enqueue_batch(ctx);
         if (rc) return rc;
@@ -2168,11 +2237,12 @@ int gofr_batch_run(gofr_ctx *ctx, int use_graph, unsigned long long *counts_host
     std::memset(&ctx->stats, 0, sizeof ctx->stats);
     ctx->stats.pairs = B.pairs;
     ctx->stats.evaluated = B.pairs;
-    ctx->stats.kernel_used = B.cells.empty() ? GOFR_KERNEL_AUTO : GOFR_KERNEL_CELL;
+    const bool any_cells = !B.cells.empty() || !B.cellw.empty();
+    ctx->stats.kernel_used = any_cells ? GOFR_KERNEL_CELL : GOFR_KERNEL_AUTO;
     int rc = gofr_sync(ctx);
     if (rc) return rc;
     // evaluated: every pair of the all-pairs members, the cell members' own count
-    if (!B.cells.empty()) ctx->stats.evaluated += B.allpairs_pairs;
+    if (any_cells) ctx->stats.evaluated += B.allpairs_pairs;
     std::memcpy(counts_host, B.h_stage, ctx->batch_total * sizeof(unsigned long long));
     return GOFR_OK;
 }

@@ -82,8 +82,9 @@ def parse():
     ap.add_argument("--no-f64", action="store_true")
     ap.add_argument("--workload", default="c2", choices=["c2", "batch", "cells", "msd", "neigh"],
                     help="c2: the headline line (default); batch / cells: only that measurement")
-    ap.add_argument("--batch-origins", type=int, default=20,
-                    help="origins per trajectory of the batched measurement")
+    ap.add_argument("--batch-origins", type=int, default=0,
+                    help="origins per trajectory of the batched measurement (0: every origin "
+                         "of the workload, stride 5)")
     ap.add_argument("--kernel", default="auto", choices=["auto", "f32", "cell", "tuned"],
                     help="pair kernel of the headline line (auto: what a user gets)")
     ap.add_argument("--no-extra", action="store_true",
@@ -257,8 +258,10 @@ class Clocks:
 
 
 KERNEL_NAMES = {1: "k_pairs_f32 (all pairs)", 2: "k_pairs_f64 (all pairs)",
-                3: "k_pairs_cell (cell lists)"}
-PROFILE_OF = {1: "k_pairs_f32_c2_n16384.md", 3: "k_pairs_cell_c2_n16384.md"}
+                3: "k_pairs_cell (block cell lists)",
+                5: "k_pairs_cellw (warp-streamed cell lists)"}
+PROFILE_OF = {1: "k_pairs_f32_c2_n16384.md", 3: "k_pairs_cell_c2_n16384.md",
+              5: "k_pairs_cellw_c2_n16384.md"}
 
 
 def traffic_from_profiles(kernel_used):
@@ -276,66 +279,69 @@ def traffic_from_profiles(kernel_used):
     return None
 
 
-def bench_batch(engine, workloads, device, origins=20, reps=5):
-    """The 64 uneven trajectories (seeds 2000+k) in one graph-captured batch
-    (the all-pairs members in one persistent launch, the members the planner
-    gives cell lists in one multi-trajectory cell-list launch), against the
-    same trajectories run one by one with the same plans (and, for reference,
-    all with the all-pairs kernel).  Bounded: `origins` origins per trajectory
-    (all its lags)."""
+def bench_batch(engine, workloads, device, origins=0, reps=2):
+    """The 64 uneven trajectories (seeds 2000+k) in one graph-captured batch:
+    the members the planner gives cell lists run the warp-streamed cell-list
+    kernel (one launch each, on a second stream), the rest share one
+    persistent all-pairs launch with a device work queue.  Against the same
+    trajectories run one by one with the same plans.  origins=0: every origin
+    of every member (stride 5, lags up to min(100, T/2)), as the workload
+    states; the all-pairs comparison runs on 20 origins per member."""
     import numpy as np
     mem = workloads.c4(64)
-    trajs = []
-    for m in mem:
+
+    def params_of(m, n_orig):
         p = m["params"]
-        trajs.append(dict(positions=m["positions"], boxes=m["boxes"], type_ids=m["type_ids"],
-                          ntypes=m["ntypes"],
-                          params=engine.make_params(p["rmin"], p["rmax"], p["nbin"], p["tmax"],
-                                                    p["skip"], p["every"],
-                                                    min(p["ntimesteps"], origins * p["skip"]), 0)))
+        n = p["ntimesteps"] if not n_orig else min(p["ntimesteps"], n_orig * p["skip"])
+        return engine.make_params(p["rmin"], p["rmax"], p["nbin"], p["tmax"], p["skip"],
+                                  p["every"], n, 0)
+
+    trajs = [dict(positions=m["positions"], boxes=m["boxes"], type_ids=m["type_ids"],
+                  ntypes=m["ntypes"], params=params_of(m, origins)) for m in mem]
     e = engine.Engine(device)
     e.batch_set(trajs)
-    for _ in range(3):
-        outs = e.batch_run(use_graph=True)
+    outs = e.batch_run(use_graph=True)  # warm-up (graph capture)
     ms = []
     for _ in range(reps):
         e.batch_run(use_graph=True)
         ms.append(e.stats()["kernel_ms"])
     st = e.stats()
     batch_rate = st["pairs"] / (sum(ms) / len(ms)) / 1e6
-    # the same trajectories one by one: with the batch's kernel (all pairs), and
-    # with the kernel a single run picks by itself (cell lists where they pay)
+    e.close()
+    # the same trajectories one by one: with the kernel a single run picks by
+    # itself, and (on 20 origins each) with the all-pairs kernel
     seq = {}
     same = True
     e2 = engine.Engine(device)
-    for kern in ("f32", "auto"):
+    for kern, n_orig in (("auto", origins), ("f32", 20)):
         ms_sum, pairs_sum, best = 0.0, 0, 0.0
-        for k, (m, t) in enumerate(zip(mem, trajs)):
+        for k, m in enumerate(mem):
             e2.set_frames(m["positions"], m["boxes"], m["type_ids"], m["ntypes"])
-            P = t["params"]
-            for _ in range(2):  # the first run of a trajectory builds its cell lists
-                c = e2.run(P.rmin, P.rmax, P.nbin, P.tmax, P.skip, P.every, P.ntimesteps,
-                           P.primo, kernel=kern)
+            P = params_of(m, n_orig)
+            c = e2.run(P.rmin, P.rmax, P.nbin, P.tmax, P.skip, P.every, P.ntimesteps, P.primo,
+                       kernel=kern)
             s2 = e2.stats()
             ms_sum += s2["kernel_ms"]
             pairs_sum += s2["pairs"]
             best = max(best, s2["pairs"] / s2["kernel_ms"] / 1e6)
-            same &= bool(np.array_equal(c, outs[k]))
+            if kern == "auto":
+                same &= bool(np.array_equal(c, outs[k]))
         seq[kern] = (pairs_sum / ms_sum / 1e6, best)
-    e.close()
     e2.close()
+    desc = "every origin (stride 5)" if not origins else f"{origins} origins"
     return {"workload": "64 trajectories, N log-uniform 256..16384, T 100..1000, 1-4 types, "
-                        f"300 bins on [0,10], {origins} origins x all lags each",
+                        f"300 bins on [0,10], {desc} x lags up to min(100, T/2) each",
             "pairs": st["pairs"], "value": round(batch_rate, 2), "unit": UNIT,
-            "kernel": "one graph: k_pairs_batch (all-pairs members, persistent work queue) + "
-                      "k_pairs_cell<R,multi> (cell-list members, one launch)",
+            "ms": round(sum(ms) / len(ms), 1),
+            "kernel": "one graph: k_pairs_cellw per cell-list member (second stream) + "
+                      "k_pairs_batch (all-pairs members, persistent work queue)",
             "evaluated_fraction": round(st["evaluated"] / st["pairs"], 4),
             "sequential_same_plans": round(seq["auto"][0], 2),
             "best_single_same_plans": round(seq["auto"][1], 2),
             "ratio_vs_sequential": round(batch_rate / seq["auto"][0], 3),
             "ratio_vs_best_single": round(batch_rate / seq["auto"][1], 3),
-            "sequential_all_pairs_kernel": round(seq["f32"][0], 2),
-            "best_single_all_pairs_kernel": round(seq["f32"][1], 2),
+            "sequential_all_pairs_kernel_20_origins": round(seq["f32"][0], 2),
+            "best_single_all_pairs_kernel_20_origins": round(seq["f32"][1], 2),
             "counts_identical_to_single_runs": same, "cuda_graph": True}
 
 
@@ -430,26 +436,37 @@ def bench_neigh(eng, w, frames=3):
 
 
 def bench_cells(engine, workloads, device):
-    """131072 atoms, 4 types, 250 bins on [0,10]: the cell-list kernel on a sample
-    (10 origins x 50 lags), its counts checked against the all-pairs FP32 kernel on
-    a sub-sample (1 origin x 5 lags)."""
+    """131072 atoms, 4 types, 250 bins on [0,10]: the default plan (the
+    warp-streamed cell-list kernel) and the block cell-list kernel on a sample
+    (10 origins x 50 lags), their counts checked against each other and, on a
+    sub-sample (1 origin x 5 lags), against the all-pairs FP32 kernel."""
     import numpy as np
     w = workloads.c5(T=150)
     p = w["params"]
     e = engine.Engine(device)
     e.set_frames(w["positions"], w["boxes"], w["type_ids"], w["ntypes"])
-    for _ in range(2):
-        e.run(p["rmin"], p["rmax"], p["nbin"], 50, p["skip"], 1, 100, 0, kernel="cell")
-    st = e.stats()
-    a = e.run(p["rmin"], p["rmax"], p["nbin"], 5, p["skip"], 1, 5, 0, kernel="cell")
+    res = {}
+    for kern in ("auto", "cell"):
+        for _ in range(2):
+            c = e.run(p["rmin"], p["rmax"], p["nbin"], 50, p["skip"], 1, 100, 0, kernel=kern)
+        res[kern] = (c, e.stats())
+    st = res["auto"][1]
+    a = e.run(p["rmin"], p["rmax"], p["nbin"], 5, p["skip"], 1, 5, 0)
     b = e.run(p["rmin"], p["rmax"], p["nbin"], 5, p["skip"], 1, 5, 0, kernel="f32")
     sf = e.stats()
     e.close()
+    sc = res["cell"][1]
     return {"workload": "c5: N=131072, 4 types, L=109.47, rmax=10, 250 bins; 10 origins x 50 lags",
-            "value": round(st["pairs"] / st["kernel_ms"] / 1e6, 1), "unit": UNIT + " (all-pairs equivalent)",
+            "value": round(st["pairs"] / st["kernel_ms"] / 1e6, 1),
+            "unit": UNIT + " (all-pairs equivalent)",
+            "kernel": KERNEL_NAMES.get(st["kernel_used"], str(st["kernel_used"])),
             "evaluated_gpairs_per_s": round(st["evaluated"] / st["kernel_ms"] / 1e6, 1),
             "evaluated_fraction": round(st["evaluated"] / st["pairs"], 5),
+            "block_cell_kernel_gpairs_per_s": round(sc["pairs"] / sc["kernel_ms"] / 1e6, 1),
+            "block_cell_evaluated_fraction": round(sc["evaluated"] / sc["pairs"], 5),
             "all_pairs_f32_gpairs_per_s": round(sf["pairs"] / sf["kernel_ms"] / 1e6, 1),
+            "counts_identical_block_vs_warp": bool(np.array_equal(res["auto"][0],
+                                                                  res["cell"][0])),
             "counts_identical_to_all_pairs": bool(np.array_equal(a, b))}
 
 
@@ -601,7 +618,7 @@ def run_gpu(args):
     fp32_peak, satom_peak = engine.measure_peaks(local)
     kernel_used = max(kernels_used) if kernels_used else 0
     evaluated_per_launch = evaluated / args.steps
-    ops_eval = OPS_PER_PAIR_CELL if kernel_used == 3 else OPS_PER_PAIR
+    ops_eval = OPS_PER_PAIR_CELL if kernel_used in (3, 5) else OPS_PER_PAIR
     peak = fp32_peak / 1e12
     # the unit of the metric: every ordered pair of the reference loop at the
     # all-pairs kernel's 16 FP32 operations (orthorhombic minimum image)
