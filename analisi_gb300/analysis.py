@@ -5,8 +5,11 @@ Restates pyanalisi/analysis.py:77-86 (max_l), :101-105 (hist2gofr) and
 (analyze_gofr) -- for a trajectory of this package's `pyanalisi` module.
 The segmented form (n_segments > 1), a loop of Gofrt::calculate calls in the
 reference, runs every segment of the resident frames in one persistent
-launch (gofr_run_windows).  Results carry the reference's exact doubles: the
-counts of each reference thread partition are folded as its threads add incr.
+launch (gofr_run_normalized).  The histograms are the reference's exact
+doubles: the counts of each reference thread partition are folded as its
+threads add incr, on the GPU; the shell-volume normalisation runs there too,
+in FP64, within a stated bound of the reference's numpy evaluation.  The
+frames of the last trajectory stay resident between calls.
 
 One deliberate difference: the reference passes debug=1 to Gofrt here
 (positional `False, 1` = every, debug), which appends every histogram to a
@@ -44,33 +47,71 @@ def _frames(traj):
             int(traj.get_ntypes()), bool(traj.is_triclinic()))
 
 
+# The engine holding the frames of the last trajectory used, kept resident
+# across calls: the notebook pattern of several compute_gofr calls on one
+# trajectory copies its frames to the GPU once.  The key is the trajectory's
+# data version (a process-wide counter, new for every trajectory built), so a
+# different or rebuilt trajectory is uploaded again.
+_resident = {"key": None, "engine": None, "traj": None}
+
+# bound on the relative difference of the last compute_gofr result from the
+# reference's own host evaluation (numpy hist2gofr on the same buffer); 0.0
+# when the histogram itself was returned (bit for bit the reference's)
+last_error_bound = 0.0
+
+
+def _resident_engine(traj, device):
+    version = traj.data_version() if hasattr(traj, "data_version") else id(traj)
+    key = (version, int(device))
+    if _resident["engine"] is None or _resident["key"] != key:
+        release_resident()
+        pos, boxes, tids, ntypes, tric = _frames(traj)
+        eng = _engine.Engine(device)
+        eng.set_frames(pos, boxes, tids, ntypes, triclinic=tric)
+        _resident.update(key=key, engine=eng, traj=traj)
+    return _resident["engine"]
+
+
+def release_resident():
+    """Frees the device copy of the last trajectory's frames."""
+    eng = _resident.get("engine")
+    if eng is not None:
+        eng.close()
+    _resident.update(key=None, engine=None, traj=None)
+
+
 def compute_gofr(traj, startr, endr, nbin, start=0, stop=None, tmax=1, tskip=10, n_segments=1,
-                 nthreads=1, return_histogram=False, device=0):
+                 nthreads=1, return_histogram=False, device=0, density=False,
+                 return_error_bound=False):
     """g(r,t) of a pyanalisi.Trajectory (this package's module) as
     Analysis.compute_gofr: one array, or a list of n_segments arrays, each the
     reference Gofrt buffer (shape (leff, ntypes(ntypes+1), nbin)) or its
-    shell-volume normalisation."""
+    shell-volume normalisation.  The frames stay on the GPU between calls on
+    the same trajectory, and the normalisation runs there in FP64.
+
+    density=True also divides by each channel's pair density (a g(r,t) that
+    tends to 1; self channels: a probability density of the displacement).
+    The result's bound on the relative difference from the reference's host
+    evaluation is in `last_error_bound`, or returned as (result, bound) with
+    return_error_bound=True."""
+    global last_error_bound
     if stop is None:
         stop = traj.get_nloaded_timesteps()
     nthreads = max(1, int(nthreads or 1))
     tmax, n_ave = max_l(start, stop, tmax)
-    pos, boxes, tids, ntypes, tric = _frames(traj)
-    dr = (endr - startr) / nbin
-
-    def finish(counts, n):
-        parts = counts if nthreads > 1 else counts[None]
-        buf = _engine.counts_to_buffer(parts, n, tskip, nparts=nthreads)
-        return buf if return_histogram else hist2gofr(nbin, dr, startr, buf)
-
-    with _engine.Engine(device) as eng:
-        eng.set_frames(pos, boxes, tids, ntypes, triclinic=tric)
-        if n_segments == 1:
-            c = eng.run(startr, endr, nbin, tmax, tskip, 1, n_ave, start, nparts=nthreads)
-            return finish(c, n_ave)
-        if n_segments > 1:
-            segment_size = max(1, n_ave // n_segments)
-            offsets = list(range(0, min(segment_size * n_segments, n_ave), segment_size))
-            c = eng.run_windows(startr, endr, nbin, tmax, tskip, 1, segment_size,
-                                [start + i for i in offsets], nparts=nthreads)
-            return [finish(c[k], segment_size) for k in range(len(offsets))]
-    raise IndexError(f"n_segments must be > 0 ({n_segments})")
+    if n_segments < 1:
+        raise IndexError(f"n_segments must be > 0 ({n_segments})")
+    norm = "buffer" if return_histogram else ("density" if density else "shell")
+    eng = _resident_engine(traj, device)
+    if n_segments == 1:
+        res, bound = eng.gofr(startr, endr, nbin, tmax, tskip, 1, n_ave, [start], norm=norm,
+                              nparts=nthreads)
+        res = res[0]
+    else:
+        segment_size = max(1, n_ave // n_segments)
+        offsets = list(range(0, min(segment_size * n_segments, n_ave), segment_size))
+        out, bound = eng.gofr(startr, endr, nbin, tmax, tskip, 1, segment_size,
+                              [start + i for i in offsets], norm=norm, nparts=nthreads)
+        res = [out[k] for k in range(len(offsets))]
+    last_error_bound = bound
+    return (res, bound) if return_error_bound else res

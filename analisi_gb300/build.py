@@ -34,7 +34,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", "-Xptxas", "-v"]
 CU_SOURCES = ["gofr_kernels.cu", "gofr_cells.cu", "gofr_cellw.cu", "gofr_capi.cu", "gofr_peaks.cu",
-              "gofr_noalloc.cu", "gofr_msd.cu", "gofr_neigh.cu"]
+              "gofr_noalloc.cu", "gofr_msd.cu", "gofr_neigh.cu", "gofr_norm.cu"]
 LIB_NAME = "libgofr_gb300.so"
 
 

@@ -103,6 +103,11 @@ struct gofr_ctx {
     cudaStream_t stream2 = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     gofr_stats stats{};
+    unsigned long long h2d_bytes = 0;  // bytes copied host -> device since creation
+    double *d_gofr = nullptr;           // normalised results (gofr_run_normalized)
+    size_t cap_gofr = 0;
+    double *d_chfac = nullptr;
+    size_t cap_chfac = 0;
     size_t batch_total = 0;
     unsigned long long launches = 0;  // kernels launched on this context
     // batched trajectories (gofr_batch_set / gofr_batch_run)
@@ -559,6 +564,8 @@ int upload_traj(gofr_ctx *ctx, TrajDev &t, const double *positions, const double
     CK(dev_malloc(&t.types, natoms * sizeof(int)));
     CK(cudaMemcpyAsync(t.pos64, positions, n3 * sizeof(double), cudaMemcpyHostToDevice,
                        ctx->stream));
+    ctx->h2d_bytes += n3 * sizeof(double) + nframes * (9 * sizeof(double) + sizeof(Box32)) +
+                      natoms * sizeof(int);
     CK(cudaMemcpyAsync(t.box64, t.h_box.data(), nframes * 9 * sizeof(double),
                        cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(t.box32, b32.data(), nframes * sizeof(Box32), cudaMemcpyHostToDevice,
@@ -1830,6 +1837,8 @@ void gofr_ctx_destroy(gofr_ctx *ctx)
         for (auto &t : ctx->trajs) free_traj(t);
         free_batch(ctx);
         cudaFree(ctx->d_counts);
+        cudaFree(ctx->d_gofr);
+        cudaFree(ctx->d_chfac);
         cudaFree(ctx->d_win);
         cudaFree(ctx->d_chtab);
         cudaFree(ctx->d_err);
@@ -1907,11 +1916,17 @@ int gofr_run_device(gofr_ctx *ctx, const gofr_params *p, unsigned long long *cou
     return run_common(ctx, p, counts_device, nullptr);
 }
 
-int gofr_run_windows(gofr_ctx *ctx, const gofr_params *p, unsigned nwin,
+}  // extern "C"
+
+namespace {
+
+// Runs the windows; the counts [nwin][nparts][leff][nch][nbin] stay in
+// ctx->d_counts and are copied to counts_host when it is not null.
+int run_windows_impl(gofr_ctx *ctx, const gofr_params *p, unsigned nwin,
                      const unsigned long long *primos, unsigned long long *counts_host)
 {
     if (!ctx) return GOFR_ERR_ARG;
-    if (!p || !primos || !counts_host || nwin == 0)
+    if (!p || !primos || nwin == 0)
         return fail(ctx, GOFR_ERR_ARG, "null argument or no windows");
     if (ctx->trajs.size() != 1) return fail(ctx, GOFR_ERR_STATE, "no frames uploaded");
     DevGuard g(ctx->device);
@@ -2034,7 +2049,7 @@ int gofr_run_windows(gofr_ctx *ctx, const gofr_params *p, unsigned nwin,
     }
     if (rc == GOFR_OK) {
         CK(cudaEventRecord(ctx->ev[2], ctx->stream));
-        if (n_out)
+        if (n_out && counts_host)
             CK(cudaMemcpyAsync(counts_host, ctx->d_counts, n_out * sizeof(unsigned long long),
                                cudaMemcpyDeviceToHost, ctx->stream));
         CK(cudaEventRecord(ctx->ev[3], ctx->stream));
@@ -2053,6 +2068,228 @@ int gofr_run_windows(gofr_ctx *ctx, const gofr_params *p, unsigned nwin,
     cudaFree(d_w);
     cudaFree(d_head);
     return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gofr_run_windows(gofr_ctx *ctx, const gofr_params *p, unsigned nwin,
+                     const unsigned long long *primos, unsigned long long *counts_host)
+{
+    if (ctx && !counts_host) return fail(ctx, GOFR_ERR_ARG, "null output buffer");
+    return run_windows_impl(ctx, p, nwin, primos, counts_host);
+}
+
+int gofr_run_normalized(gofr_ctx *ctx, const gofr_params *p, unsigned nwin,
+                      const unsigned long long *primos, int norm, double *out_host,
+                      double *rel_err_bound)
+{
+    if (!ctx) return GOFR_ERR_ARG;
+    if (!p || !out_host) return fail(ctx, GOFR_ERR_ARG, "null argument");
+    if (norm < 0 || norm > 2) return fail(ctx, GOFR_ERR_ARG, "unknown normalisation %d", norm);
+    if (ctx->trajs.size() != 1) return fail(ctx, GOFR_ERR_STATE, "no frames uploaded");
+    const unsigned long long one = p->primo;
+    if (nwin == 0) nwin = 1;
+    if (!primos) {
+        if (nwin != 1) return fail(ctx, GOFR_ERR_ARG, "several windows need their primos");
+        primos = &one;
+    }
+    DevGuard g(ctx->device);
+    int rc = run_windows_impl(ctx, p, nwin, primos, nullptr);
+    if (rc) return rc;
+    const TrajDev &t = ctx->trajs[0];
+    RunShape rs;
+    rc = shape_of(ctx, t, *p, rs);
+    if (rc) return rc;
+    const size_t n = rs.data_length;
+    rc = ensure(ctx, ctx->d_gofr, ctx->cap_gofr, std::max<size_t>(n * nwin, 1));
+    if (rc) return rc;
+    // pair-density factors per channel (mode 2): box volume averaged over the
+    // windows' origin frames, atoms per type
+    const unsigned nt = t.ntypes, half = nt * (nt + 1) / 2;
+    std::vector<double> chfac(2 * half, 1.0);
+    if (norm == 2) {
+        double vsum = 0.0;
+        size_t nv = 0;
+        for (unsigned w = 0; w < nwin; ++w)
+            for (unsigned k = 0; k < rs.n_orig; ++k) {
+                const double *b = &t.h_box[(primos[w] + (size_t)k * rs.skip) * 9];
+                vsum += 8.0 * b[3] * b[4] * b[5];
+                ++nv;
+            }
+        const double V = nv ? vsum / nv : 8.0 * t.h_box[3] * t.h_box[4] * t.h_box[5];
+        const std::vector<unsigned short> tab = channel_table(nt);
+        for (unsigned a = 0; a < nt; ++a)
+            for (unsigned c = a; c < nt; ++c) {
+                const double na = t.h_tbegin[a + 1] - t.h_tbegin[a];
+                const double nc = t.h_tbegin[c + 1] - t.h_tbegin[c];
+                const unsigned ch = tab[a * nt + c];
+                chfac[ch] = (a == c ? na * (na - 1.0) : 2.0 * na * nc) / V;
+                if (a == c) chfac[ch + half] = na;
+            }
+        rc = ensure(ctx, ctx->d_chfac, ctx->cap_chfac, chfac.size());
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(ctx->d_chfac, chfac.data(), chfac.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, ctx->stream));
+    }
+    NormLaunch L{};
+    L.counts = ctx->d_counts;
+    L.out = ctx->d_gofr;
+    L.chfac = ctx->d_chfac;
+    L.n = n;
+    L.nwin = (int)nwin;
+    L.nparts = p->nparts > 1 ? (int)p->nparts : 1;
+    L.nbin = (int)p->nbin;
+    L.nch = (int)rs.nch;
+    L.mode = norm;
+    L.incr = (rs.ntimesteps / rs.skip > 0) ? 1.0 / (int)(rs.ntimesteps / rs.skip) : 1.0;
+    L.r0 = p->rmin;
+    L.dr = (p->rmax - p->rmin) / p->nbin;
+    L.c43pi = 4.0 * 3.141592653589793 / 3.0;  // numpy: 4 * np.pi / 3
+    ++ctx->launches;
+    if (launch_counts_to_gofr(L, ctx->num_sms, ctx->stream))
+        return fail(ctx, GOFR_ERR_CUDA, "normalisation launch failed: %s",
+                    cudaGetErrorString(cudaGetLastError()));
+    if (n)
+        CK(cudaMemcpyAsync(out_host, ctx->d_gofr, n * nwin * sizeof(double),
+                           cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (rel_err_bound) {
+        // the cubes here are correctly rounded, a host's within one unit in
+        // the last place: per bin the relative difference of the shell volume
+        // is at most (ulp(r+^3) + ulp(r-^3)) / (r+^3 - r-^3), plus the
+        // roundings of the difference, the product and the divisions
+        const double u = std::ldexp(1.0, -53);
+        auto ulp = [](double x) {
+            if (x == 0.0) return std::ldexp(1.0, -1074);
+            int e;
+            std::frexp(std::fabs(x), &e);
+            return std::ldexp(1.0, e - 53);
+        };
+        double worst = 0.0;
+        if (norm >= 1) {
+            for (unsigned b = 0; b < p->nbin; ++b) {
+                const double rm = (double)b * L.dr + L.r0, rp = (double)(b + 1) * L.dr + L.r0;
+                const double cm = rm * rm * rm, cp = rp * rp * rp;
+                const double d = std::fabs(cp - cm);
+                const double e = d > 0.0 ? (ulp(cp) + ulp(cm)) * (1.0 + 4.0 * u) / d : INFINITY;
+                worst = std::max(worst, e + (norm == 2 ? 8.0 : 6.0) * u);
+            }
+        }
+        *rel_err_bound = worst;  // 0 for the buffer itself: bit for bit
+    }
+    return GOFR_OK;
+}
+
+// Device bytes one frame of natoms takes in a run: FP64 positions, FP32
+// frames, the cell-sorted records and starts, with room for the boxes.
+static size_t frame_device_bytes(size_t natoms)
+{
+    return padded_natoms(natoms) * (3 * 8 + 3 * 4 + 16 + 4 + 8) + 512;
+}
+
+int gofr_run_streamed(gofr_ctx *ctx, const double *positions, const double *boxes, int box_kind,
+                      const int *type_ids, unsigned ntypes, size_t natoms, size_t nframes,
+                      const gofr_params *p, size_t max_device_bytes,
+                      unsigned long long *counts_host)
+{
+    if (!ctx) return GOFR_ERR_ARG;
+    if (!p || !positions || !boxes || !type_ids || !counts_host)
+        return fail(ctx, GOFR_ERR_ARG, "null argument");
+    if (box_kind != GOFR_BOX_ORTHO && box_kind != GOFR_BOX_TRICLINIC)
+        return fail(ctx, GOFR_ERR_ARG, "invalid box kind %d", box_kind);
+    if (p->nparts > 1 && p->kernel != GOFR_KERNEL_AUTO && p->kernel != GOFR_KERNEL_F32_RECHECK &&
+        p->kernel != GOFR_KERNEL_F64)
+        return fail(ctx, GOFR_ERR_UNSUPPORTED, "per-partition counts need an all-pairs kernel");
+    DevGuard g(ctx->device);
+    // the whole calculation's shape, checked against every frame
+    TrajDev whole;
+    whole.T = nframes;
+    whole.N = natoms;
+    whole.ntypes = ntypes;
+    RunShape rs;
+    int rc = shape_of(ctx, whole, *p, rs);
+    if (rc) return rc;
+    const unsigned nparts = p->nparts > 1 ? p->nparts : 1;
+    const size_t n_out = rs.data_length * nparts;
+    const size_t stride = box_kind == GOFR_BOX_TRICLINIC ? 9 : 6;
+    unsigned long long pairs = 0;
+    double kernel_ms = 0.0;
+    if (rs.n_lags > 0 && rs.n_orig > 0) {
+        // origins per chunk: its frames [first origin, last origin + last lag]
+        const size_t span = (size_t)(rs.n_lags - 1) * rs.every + 1;
+        const size_t budget_frames = max_device_bytes / frame_device_bytes(natoms);
+        if (budget_frames < span)
+            return fail(ctx, GOFR_ERR_UNSUPPORTED,
+                        "a device budget of %zu bytes holds %zu frames of %zu atoms, fewer than "
+                        "the %zu frames of one origin's lags", max_device_bytes, budget_frames,
+                        natoms, span);
+        const size_t per_chunk = (budget_frames - span) / rs.skip + 1;
+        std::vector<unsigned long long> chunk(n_out ? n_out : 1);
+        std::vector<unsigned long long> total(n_out ? n_out : 1, 0ull);
+        for (size_t k0 = 0; k0 < rs.n_orig; k0 += per_chunk) {
+            const size_t k1 = std::min<size_t>(rs.n_orig, k0 + per_chunk);
+            const size_t f0 = (size_t)p->primo + k0 * rs.skip;
+            const size_t f1 = (size_t)p->primo + (k1 - 1) * rs.skip + span;
+            ctx->trajs.resize(1);
+            rc = upload_traj(ctx, ctx->trajs[0], positions + f0 * natoms * 3, boxes + f0 * stride,
+                             box_kind, type_ids, ntypes, natoms, f1 - f0);
+            if (rc) return rc;
+            const TrajDev &t = ctx->trajs[0];
+            // this chunk: origins 0, skip, ... of the uploaded frames, every lag
+            gofr_params q = *p;
+            q.primo = 0;
+            RunShape rc_shape = rs;
+            rc_shape.n_orig = (unsigned)(k1 - k0);
+            Plan pl;
+            rc = make_plan(ctx, t, q, pl, q.kernel != GOFR_KERNEL_TUNED);
+            if (rc) return rc;
+            if (pl.cells && q.kernel != GOFR_KERNEL_CELL && q.kernel != GOFR_KERNEL_CELL_WARP &&
+                ensure_cells(ctx, t, pl) == GOFR_ERR_NOMEM) {
+                ctx->err.clear();
+                (void)cudaGetLastError();
+                gofr_params a = q;
+                a.kernel = GOFR_KERNEL_AUTO;
+                Plan ap;
+                rc = make_plan(ctx, t, a, ap, false);
+                if (rc) return rc;
+                pl = ap;
+            }
+            rc = ensure(ctx, ctx->d_counts, ctx->cap_counts, std::max<size_t>(n_out, 1));
+            if (rc) return rc;
+            CK(cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), ctx->stream));
+            CK(cudaMemsetAsync(ctx->d_stats, 0, ST_COUNT * sizeof(unsigned long long),
+                               ctx->stream));
+            if (n_out)
+                CK(cudaMemsetAsync(ctx->d_counts, 0, n_out * sizeof(unsigned long long),
+                                   ctx->stream));
+            CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+            unsigned long long pw = 0;
+            rc = enqueue_run(ctx, t, q, rc_shape, pl, ctx->d_counts, &pw);
+            if (rc) return rc;
+            CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+            if (n_out)
+                CK(cudaMemcpyAsync(chunk.data(), ctx->d_counts, n_out * sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            rc = check_device_error(ctx);
+            if (rc) return rc;
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]) == cudaSuccess) kernel_ms += ms;
+            for (size_t i = 0; i < n_out; ++i) total[i] += chunk[i];
+            pairs += pw;
+        }
+        if (n_out) std::memcpy(counts_host, total.data(), n_out * sizeof(unsigned long long));
+    } else if (n_out) {
+        std::memset(counts_host, 0, n_out * sizeof(unsigned long long));
+    }
+    std::memset(&ctx->stats, 0, sizeof ctx->stats);
+    ctx->stats.pairs = pairs;
+    ctx->stats.evaluated = pairs;
+    ctx->stats.kernel_ms = kernel_ms;
+    ctx->stats.total_ms = kernel_ms;
+    return GOFR_OK;
 }
 
 int gofr_sync(gofr_ctx *ctx)
@@ -2080,6 +2317,7 @@ int gofr_get_stats(const gofr_ctx *ctx, gofr_stats *out)
     if (!ctx || !out) return GOFR_ERR_ARG;
     *out = ctx->stats;
     out->launches = ctx->launches;
+    out->h2d_bytes = ctx->h2d_bytes;
     return GOFR_OK;
 }
 

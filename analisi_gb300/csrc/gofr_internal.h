@@ -114,6 +114,20 @@ int launch_cell_scatter_w(const double *pos64, const unsigned char *types8, size
                           cudaStream_t s);
 int launch_cellw_pairs(const CellwLaunch &C, int num_sms, cudaStream_t s);
 
+// FP64 normalisation of window counts on the device (gofr_norm.cu).
+struct NormLaunch {
+    const unsigned long long *counts;  // [nwin][nparts][n] exact counts
+    double *out;                       // [nwin][n]
+    const double *chfac;               // [nch] pair-density factors (mode 2)
+    size_t n;                          // leff * nch * nbin
+    int nwin, nparts, nbin, nch;
+    int mode;                          // 0 buffer, 1 / shell volume, 2 / shell volume / density
+    double incr;                       // 1 / int(ntimesteps / skip)
+    double r0, dr;                     // bin b spans [b dr + r0, (b + 1) dr + r0)
+    double c43pi;                      // fl(fl(4 pi) / 3)
+};
+int launch_counts_to_gofr(const NormLaunch &L, int num_sms, cudaStream_t s);
+
 int cell_smem_bytes(int nch, int nbin, int ntypes);
 int cell_block_atoms(int r);
 int cell_max_ranges();

@@ -28,7 +28,8 @@ EXPORTED = [
     "gofr_counts_to_buffer", "gofr_bin_thresholds", "gofr_batch_set",
     "gofr_batch_output_layout", "gofr_batch_run", "gofr_measure_peaks",
     "gofr_run_f64_noalloc", "gofr_run_windows", "gofr_set_centres", "gofr_msd_output_size",
-    "gofr_msd_run", "gofr_neigh_layout", "gofr_neigh_run",
+    "gofr_msd_run", "gofr_neigh_layout", "gofr_neigh_run", "gofr_run_normalized",
+    "gofr_run_streamed",
 ]
 
 
@@ -104,7 +105,8 @@ class Stats(ctypes.Structure):
                 ("candidates", ctypes.c_ulonglong), ("rechecks", ctypes.c_ulonglong),
                 ("kernel_ms", ctypes.c_double), ("total_ms", ctypes.c_double),
                 ("kernel_used", ctypes.c_int), ("wrap_checked", ctypes.c_int),
-                ("err_bound_d2", ctypes.c_double), ("launches", ctypes.c_ulonglong)]
+                ("err_bound_d2", ctypes.c_double), ("launches", ctypes.c_ulonglong),
+                ("h2d_bytes", ctypes.c_ulonglong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -156,6 +158,10 @@ def load_library(path=None):
     L.gofr_batch_run.argtypes = [vp, ctypes.c_int, up]
     L.gofr_measure_peaks.argtypes = [ctypes.c_int, dp, dp]
     L.gofr_run_windows.argtypes = [vp, ctypes.POINTER(Params), ctypes.c_uint, up, up]
+    L.gofr_run_streamed.argtypes = [vp, dp, dp, ctypes.c_int, ip, ctypes.c_uint, ctypes.c_size_t,
+                                    ctypes.c_size_t, ctypes.POINTER(Params), ctypes.c_size_t, up]
+    L.gofr_run_normalized.argtypes = [vp, ctypes.POINTER(Params), ctypes.c_uint, up, ctypes.c_int,
+                                    dp, dp]
     L.gofr_set_centres.argtypes = [vp, dp, ctypes.c_size_t, ctypes.c_uint]
     L.gofr_msd_output_size.argtypes = [vp, ctypes.POINTER(MsdParams),
                                        ctypes.POINTER(ctypes.c_size_t)]
@@ -171,7 +177,7 @@ def load_library(path=None):
                  "gofr_run_device", "gofr_sync", "gofr_get_stats", "gofr_counts_to_buffer",
                  "gofr_bin_thresholds", "gofr_batch_set", "gofr_batch_output_layout",
                  "gofr_batch_run", "gofr_measure_peaks", "gofr_run_f64_noalloc",
-                 "gofr_run_windows"):
+                 "gofr_run_windows", "gofr_run_normalized", "gofr_run_streamed"):
         getattr(L, name).restype = ctypes.c_int
     if path is None:
         _lib = L
@@ -348,6 +354,51 @@ class Engine:
         shape = (len(primos), leff, nch, int(nbin)) if nparts <= 1 else \
             (len(primos), int(nparts), leff, nch, int(nbin))
         return out[:n * len(primos)].reshape(shape)
+
+    def run_streamed(self, positions, boxes, type_ids, ntypes, max_device_bytes, rmin, rmax, nbin,
+                     tmax=0, skip=1, every=1, ntimesteps=0, primo=0, kernel="auto", nparts=1):
+        """gofr_run on host frames streamed through the device in chunks of
+        origins whose frames fit max_device_bytes (the context's resident
+        frames are replaced by the last chunk's)."""
+        pos = np.ascontiguousarray(positions, dtype=np.float64)
+        bx = np.ascontiguousarray(boxes, dtype=np.float64)
+        ty = np.ascontiguousarray(type_ids, dtype=np.int32)
+        p = make_params(rmin, rmax, nbin, tmax, skip, every, ntimesteps, primo, kernel, nparts)
+        leff = ntimesteps if (ntimesteps < tmax or tmax == 0) else tmax
+        nch = int(ntypes) * (int(ntypes) + 1)
+        shape = (leff, nch, int(nbin)) if nparts <= 1 else (int(nparts), leff, nch, int(nbin))
+        out = np.zeros(max(int(np.prod(shape)), 1), dtype=np.uint64)
+        self._check(self.L.gofr_run_streamed(
+            self._ctx, _dp(pos), _dp(bx), BOX_TRICLINIC if bx.shape[1] == 9 else BOX_ORTHO,
+            ty.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), int(ntypes), pos.shape[1],
+            pos.shape[0], ctypes.byref(p), int(max_device_bytes),
+            out.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong))))
+        self.ntypes, self.natoms, self.nframes = int(ntypes), pos.shape[1], pos.shape[0]
+        return out[:int(np.prod(shape))].reshape(shape)
+
+    NORMS = {"buffer": 0, "shell": 1, "density": 2}
+
+    def gofr(self, rmin, rmax, nbin, tmax, skip, every, ntimesteps, primos, norm="shell",
+             nparts=1, kernel="auto"):
+        """calculate(primo) for each primo of `primos` with the result made into
+        doubles on the GPU: norm "buffer" (the reference's Gofrt buffer, bit for
+        bit), "shell" (divided by the shell volumes: the reference's hist2gofr)
+        or "density" (also by each channel's pair density).  Returns
+        ([nwin][leff][nch][nbin] float64, bound on the relative difference from
+        a host FP64 evaluation of the same formula)."""
+        primos = np.ascontiguousarray(np.atleast_1d(primos), dtype=np.uint64)
+        p = make_params(rmin, rmax, nbin, tmax, skip, every, ntimesteps, 0, kernel, nparts)
+        leff = ntimesteps if (ntimesteps < tmax or tmax == 0) else tmax
+        nch = self.ntypes * (self.ntypes + 1)
+        out = np.zeros(max(len(primos) * leff * nch * int(nbin), 1))
+        bound = ctypes.c_double()
+        self._check(self.L.gofr_run_normalized(
+            self._ctx, ctypes.byref(p), len(primos),
+            primos.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong)),
+            self.NORMS[norm] if isinstance(norm, str) else int(norm), _dp(out),
+            ctypes.byref(bound)))
+        return out[:len(primos) * leff * nch * int(nbin)].reshape(
+            len(primos), leff, nch, int(nbin)), bound.value
 
     def run_params(self, p, out):
         """gofr_run with prepared Params and a preallocated uint64 output (hot loop form)."""

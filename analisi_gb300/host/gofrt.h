@@ -21,12 +21,21 @@
 #include <stdexcept>
 #include <string>
 #include <sys/types.h>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
 #include "gofr_gb300.h"
 
 namespace analisi_gb300 {
+
+// Trajectories that hold a window of their frames (TrajWindow: window_start,
+// window_frames, ensure_window) rather than all of them.
+template <class T, class = void>
+struct has_window : std::false_type {};
+template <class T>
+struct has_window<T, std::void_t<decltype(std::declval<T &>().window_start())>>
+    : std::true_type {};
 
 template <class TFLOAT, class T>
 class Gofrt {
@@ -42,6 +51,10 @@ public:
         // (lib/include/calculatemultithread.h:41-47)
         if (const char *k = std::getenv("ANALISI_GB300_KERNEL")) kernel = std::atoi(k);
         if (const char *d = std::getenv("ANALISI_GB300_DEVICE")) device = std::atoi(d);
+        // frames beyond this many device bytes are streamed through the GPU in
+        // chunks of origins instead of being held resident (0: no limit)
+        if (const char *b = std::getenv("ANALISI_GB300_DEVICE_BUDGET"))
+            device_budget = (size_t)std::strtod(b, nullptr);
     }
     ~Gofrt()
     {
@@ -93,7 +106,18 @@ public:
     // (lib/include/calculatemultithread.h:106-162, lib/src/gofrt.cpp:74-155)
     void calculate(size_t primo)
     {
-        ensure_frames();
+        size_t rel = primo;
+        if constexpr (has_window<T>::value) {
+            // the frames of every origin and lag: [primo, primo + n + leff - 1)
+            const size_t need = ntimesteps + leff > 1 ? ntimesteps + leff - 1 : 1;
+            traiettoria->ensure_window(primo, need);
+            rel = primo - traiettoria->window_start();
+        }
+        const size_t nframes = frames();
+        const bool stream = device_budget > 0 &&
+                            (double)nframes * traiettoria->get_natoms() * 64.0 > (double)device_budget;
+        if (stream) make_ctx();
+        else ensure_frames();
         gofr_params p{};
         p.rmin = rmin;
         p.rmax = rmax;
@@ -102,13 +126,25 @@ public:
         p.skip = skip;
         p.every = every;
         p.ntimesteps = ntimesteps;
-        p.primo = primo;
+        p.primo = rel;
         p.kernel = kernel;
         p.nparts = nthreads;
         size_t n = 0;
-        check(gofr_output_size(ctx, &p, &n));
-        counts.resize(n ? n : 1);
-        check(gofr_run(ctx, &p, counts.data()));
+        if (stream) {
+            const unsigned nt = ntypes();
+            n = (size_t)leff * nt * (nt + 1) * nbin * (nthreads > 1 ? nthreads : 1);
+            counts.resize(n ? n : 1);
+            check(gofr_run_streamed(ctx, traiettoria->positions_data(), traiettoria->box(0),
+                                    traiettoria->is_triclinic() ? GOFR_BOX_TRICLINIC
+                                                                : GOFR_BOX_ORTHO,
+                                    traiettoria->type_ids(), nt, traiettoria->get_natoms(),
+                                    nframes, &p, device_budget, counts.data()));
+            uploaded_version = ~0ull;  // the context holds the last chunk's frames
+        } else {
+            check(gofr_output_size(ctx, &p, &n));
+            counts.resize(n ? n : 1);
+            check(gofr_run(ctx, &p, counts.data()));
+        }
         const size_t dl = vdata.size();
         if (n == 0 || dl == 0) return;
         std::vector<double> tmp;
@@ -169,6 +205,7 @@ public:
         return s;
     }
     void set_kernel(int k) { kernel = k; }
+    void set_device_budget(size_t bytes) { device_budget = bytes; }
 
 private:
     unsigned ntypes() const { return (unsigned)traiettoria->get_ntypes(); }
@@ -195,20 +232,32 @@ private:
         if (rc != GOFR_OK) throw std::runtime_error(gofr_last_error(ctx));
     }
 
-    void ensure_frames()
+    // frames held by the trajectory: its window, or all of them
+    size_t frames() const
+    {
+        if constexpr (has_window<T>::value) return traiettoria->window_frames();
+        else return traiettoria->get_ntimesteps();
+    }
+
+    void make_ctx()
     {
         if (!ctx) {
             if (gofr_ctx_create(&ctx, device) != GOFR_OK)
                 throw std::runtime_error(std::string("gofr: cannot create a GPU context: ") +
                                          gofr_last_error(nullptr));
         }
+    }
+
+    void ensure_frames()
+    {
+        make_ctx();
         const auto ver = traiettoria->data_version();
         if (uploaded_version != ver) {
             check(gofr_set_frames(ctx, traiettoria->positions_data(), traiettoria->box(0),
                                   traiettoria->is_triclinic() ? GOFR_BOX_TRICLINIC
                                                               : GOFR_BOX_ORTHO,
                                   traiettoria->type_ids(), ntypes(), traiettoria->get_natoms(),
-                                  traiettoria->get_ntimesteps()));
+                                  frames()));
             uploaded_version = ver;
         }
     }
@@ -240,6 +289,7 @@ private:
     gofr_ctx *ctx = nullptr;
     int device = 0;
     int kernel = GOFR_KERNEL_AUTO;
+    size_t device_budget = 0;
     unsigned long long uploaded_version = ~0ull;
 };
 

@@ -32,6 +32,37 @@ struct LammpsFrames {
     std::vector<int64_t> timesteps;  // LAMMPS timestep of each frame
 };
 
+// A binary trajectory file mapped into memory (mmap, read-only) with an
+// index of its frames, built by walking the headers and chunk sizes once
+// (the reference's Trajectory, lib/src/trajectory.cpp:261-345,450-690, which
+// also maps the file and indexes it).  Frames are decoded on request, a
+// window at a time, so the file is never copied whole.
+class LammpsMmap {
+public:
+    explicit LammpsMmap(const std::string &path);  // throws std::runtime_error
+    ~LammpsMmap();
+    LammpsMmap(const LammpsMmap &) = delete;
+    LammpsMmap &operator=(const LammpsMmap &) = delete;
+
+    size_t nframes() const { return offsets_.size(); }
+    size_t natoms() const { return natoms_; }
+    bool triclinic() const { return triclinic_; }
+    const std::vector<int> &types() const { return types_; }  // raw labels (first frame)
+    const std::vector<int64_t> &timesteps() const { return steps_; }
+    // Decodes frames [first, first + count) (atoms in first-frame order).
+    LammpsFrames read(size_t first, size_t count) const;
+
+private:
+    const char *data_ = nullptr;
+    size_t size_ = 0;
+    size_t natoms_ = 0;
+    bool triclinic_ = false;
+    std::vector<size_t> offsets_;     // byte offset of each frame's header
+    std::vector<int64_t> steps_;
+    std::vector<int> types_;
+    std::vector<long long> ids_;      // atom id of each first-frame slot
+};
+
 // Throws std::runtime_error on a malformed file.
 LammpsFrames read_lammps_binary(const std::string &path);
 

@@ -20,12 +20,15 @@
 #include "lammps_file.h"
 #include "msd.h"
 #include "neighbour.h"
+#include "traj_window.h"
 #include "trajectory.h"
 
 namespace py = pybind11;
 using analisi_gb300::BoxFormat;
 using analisi_gb300::Trajectory;
+using analisi_gb300::TrajWindow;
 using GofrtT = analisi_gb300::Gofrt<double, Trajectory>;
+using GofrtW = analisi_gb300::Gofrt<double, TrajWindow>;
 using MsdT = analisi_gb300::MeanSquareDisplacement<Trajectory>;
 using NeighT = analisi_gb300::Neighbours<Trajectory, double>;
 
@@ -102,6 +105,57 @@ py::array_t<double> copy3(const double *p, size_t a, size_t b, size_t c)
     return out;
 }
 
+// The reference's Gofrt binding (pyanalisi/src/pyanalisi.cpp:66-82) for a
+// trajectory type T: `Gofrt` over Trajectory, `Gofrt_lammps` over Traj.
+template <class G, class T>
+void define_gofrt(py::module &m, const char *name)
+{
+    py::class_<G>(m, name, py::buffer_protocol())
+        .def(py::init<T *, double, double, unsigned int, unsigned int, unsigned int,
+                      unsigned int, unsigned int, bool>(),
+             py::arg("trajectory"), py::arg("rmin"), py::arg("rmax"), py::arg("nbin"),
+             py::arg("tmax") = 0, py::arg("nthreads") = 0, py::arg("skip") = 1,
+             py::arg("every") = 1, py::arg("debug") = false, py::keep_alive<1, 2>(),
+             R"doc(calculates g(r) and, in general, g(r,t) on the GPU
+
+Parameters
+----------
+Trajectory instance, rmin, rmax, nbin, maximum time lag, number of threads
+(the reference's atom split; its per-thread sums are reproduced exactly),
+time skip, every time, debug flag)doc")
+        .def("reset", &G::reset)
+        .def("getNumberOfExtraTimestepsNeeded", &G::nExtraTimesteps)
+        .def("calculate", [](G &g, size_t primo) {
+            py::gil_scoped_release release;
+            g.calculate(primo);
+        })
+        .def("get_columns_description", &G::get_columns_description)
+        .def("set_device_budget", &G::set_device_budget,
+             "frames beyond this many device bytes are streamed through the GPU in chunks "
+             "of origins (0: all resident)")
+        .def("set_kernel", &G::set_kernel,
+             "0 auto (FP32 + FP64 edge recheck), 1 FP32 forced, 2 plain FP64")
+        .def("last_stats", [](G &g) {
+            gofr_stats s = g.last_stats();
+            py::dict d;
+            d["pairs"] = s.pairs;
+            d["evaluated"] = s.evaluated;
+            d["candidates"] = s.candidates;
+            d["rechecks"] = s.rechecks;
+            d["kernel_ms"] = s.kernel_ms;
+            d["total_ms"] = s.total_ms;
+            d["kernel_used"] = s.kernel_used;
+            d["wrap_checked"] = s.wrap_checked;
+            d["err_bound_d2"] = s.err_bound_d2;
+            return d;
+        })
+        .def_buffer([](G &g) -> py::buffer_info {
+            return py::buffer_info(g.access_vdata(), sizeof(double),
+                                   py::format_descriptor<double>::format(), g.get_shape().size(),
+                                   g.get_shape(), g.get_stride());
+        });
+}
+
 }  // namespace
 
 PYBIND11_MODULE(pyanalisi, m)
@@ -160,49 +214,62 @@ save rotation matrix if triclinic format is used and a rotation is needed)doc")
         .def("get_nloaded_timesteps", &Trajectory::get_nloaded_timesteps)
         .def("getNtimesteps", &Trajectory::get_ntimesteps)
         .def("get_current_timestep", [](Trajectory &) { return (ssize_t)0; })
-        .def("getWrapPbc", &Trajectory::get_pbc_wrap);
+        .def("getWrapPbc", &Trajectory::get_pbc_wrap)
+        .def("data_version", &Trajectory::data_version,
+             "changes whenever the internal buffers change (device copies follow it)");
 
-    py::class_<GofrtT>(m, "Gofrt", py::buffer_protocol())
-        .def(py::init<Trajectory *, double, double, unsigned int, unsigned int, unsigned int,
-                      unsigned int, unsigned int, bool>(),
-             py::arg("trajectory"), py::arg("rmin"), py::arg("rmax"), py::arg("nbin"),
-             py::arg("tmax") = 0, py::arg("nthreads") = 0, py::arg("skip") = 1,
-             py::arg("every") = 1, py::arg("debug") = false, py::keep_alive<1, 2>(),
-             R"doc(calculates g(r) and, in general, g(r,t) on the GPU
+    define_gofrt<GofrtT, Trajectory>(m, "Gofrt");
 
-Parameters
+    // the reference's memory-mapped trajectory (pyanalisi/src/pyanalisi.cpp:376-418)
+    py::class_<TrajWindow>(m, "Traj", py::buffer_protocol())
+        .def(py::init<std::string>(), R"doc(Parameters
 ----------
-Trajectory instance, rmin, rmax, nbin, maximum time lag, number of threads
-(the reference's atom split; its per-thread sums are reproduced exactly),
-time skip, every time, debug flag)doc")
-        .def("reset", &GofrtT::reset)
-        .def("getNumberOfExtraTimestepsNeeded", &GofrtT::nExtraTimesteps)
-        .def("calculate", [](GofrtT &g, size_t primo) {
-            py::gil_scoped_release release;
-            g.calculate(primo);
+name of the binary file to open)doc")
+        .def("setWrapPbc", &TrajWindow::set_pbc_wrap,
+             "wrap all the atomic coordinates inside the simulation box (True/False)")
+        .def("setAccessWindowSize", [](TrajWindow &t, int ts) {
+            return ts > 0 ? t.set_data_access_block_size((size_t)ts) : 0;
+        }, "sets the number of frames of the read window; 1 success, 0 failure")
+        .def("setAccessStart", [](TrajWindow &t, int ts) {
+            return ts >= 0 ? t.set_access_at((size_t)ts) : 0;
+        }, "reads the window starting at this frame; 1 success, 2 beyond the end of the file")
+        .def("serving_pos", &TrajWindow::serving_pos)
+        .def("toggle_pos_vel", &TrajWindow::toggle_pos_vel)
+        .def("get_positions_copy", [](TrajWindow &t) {
+            return copy3(t.positions_data(), t.window_frames(), t.get_natoms(), 3);
         })
-        .def("get_columns_description", &GofrtT::get_columns_description)
-        .def("set_kernel", &GofrtT::set_kernel,
-             "0 auto (FP32 + FP64 edge recheck), 1 FP32 forced, 2 plain FP64")
-        .def("last_stats", [](GofrtT &g) {
-            gofr_stats s = g.last_stats();
-            py::dict d;
-            d["pairs"] = s.pairs;
-            d["evaluated"] = s.evaluated;
-            d["candidates"] = s.candidates;
-            d["rechecks"] = s.rechecks;
-            d["kernel_ms"] = s.kernel_ms;
-            d["total_ms"] = s.total_ms;
-            d["kernel_used"] = s.kernel_used;
-            d["wrap_checked"] = s.wrap_checked;
-            d["err_bound_d2"] = s.err_bound_d2;
-            return d;
+        .def("get_velocities_copy", [](TrajWindow &t) {
+            return copy3(t.velocity_data(), t.window_frames(), t.get_natoms(), 3);
         })
-        .def_buffer([](GofrtT &g) -> py::buffer_info {
-            return py::buffer_info(g.access_vdata(), sizeof(double),
-                                   py::format_descriptor<double>::format(), g.get_shape().size(),
-                                   g.get_shape(), g.get_stride());
+        .def("get_box_copy", [](TrajWindow &t) {
+            const size_t st = t.get_box_stride(), n = t.window_frames();
+            py::array_t<double> b({n, st});
+            if (n) std::memcpy(b.mutable_data(), t.box(0), sizeof(double) * n * st);
+            return b;
+        })
+        .def("get_type_ids", [](TrajWindow &t) {
+            return py::array_t<int>(t.get_natoms(), t.type_ids());
+        })
+        .def("get_ntypes", &TrajWindow::get_ntypes)
+        .def("get_natoms", &TrajWindow::get_natoms)
+        .def("is_triclinic", &TrajWindow::is_triclinic)
+        .def("get_nloaded_timesteps", &TrajWindow::get_nloaded_timesteps)
+        .def("getNtimesteps", &TrajWindow::get_ntimesteps)
+        .def("get_current_timestep", &TrajWindow::window_start)
+        .def("getWrapPbc", &TrajWindow::get_pbc_wrap)
+        .def("get_lammps_timesteps", [](TrajWindow &t) {
+            const auto &v = t.lammps_timesteps();
+            return py::array_t<long long>(v.size(), reinterpret_cast<const long long *>(v.data()));
+        })
+        .def_buffer([](TrajWindow &t) -> py::buffer_info {
+            const ssize_t n = (ssize_t)t.window_frames(), na = (ssize_t)t.get_natoms();
+            const double *d = t.serving_pos() ? t.positions_data() : t.velocity_data();
+            return py::buffer_info(const_cast<double *>(d), sizeof(double),
+                                   py::format_descriptor<double>::format(), 3, {n, na, (ssize_t)3},
+                                   {(ssize_t)(na * 3 * sizeof(double)),
+                                    (ssize_t)(3 * sizeof(double)), (ssize_t)sizeof(double)});
         });
+    define_gofrt<GofrtW, TrajWindow>(m, "Gofrt_lammps");
 
     py::class_<MsdT>(m, "MeanSquareDisplacement", py::buffer_protocol())
         .def(py::init<Trajectory *, unsigned int, unsigned int, unsigned int, bool, bool, bool>(),
@@ -286,5 +353,5 @@ debug flag)doc")
         return d;
     }, "reads analisi's binary trajectory format (the CLI's -i input)");
     m.def("info", []() { return std::string("analisi_gb300: Gofrt on GB300 (sm_103a)"); });
-    m.def("has_mmap", []() { return false; });
+    m.def("has_mmap", []() { return true; });
 }

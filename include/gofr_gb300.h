@@ -109,6 +109,7 @@ typedef struct gofr_stats {
     int wrap_checked;                /* 1 if the per-pair wrap-decision check was on */
     double err_bound_d2;             /* FP32 error bound on d2 at rmax (A^2) */
     unsigned long long launches;     /* kernels launched on this context since its creation */
+    unsigned long long h2d_bytes;    /* frame bytes copied host -> device since its creation */
 } gofr_stats;
 
 /* Creates a context on CUDA device `device` (replaces the construction of a
@@ -164,6 +165,46 @@ int gofr_sync(gofr_ctx *ctx);
  * that need the FP64 or cell-list kernel run one launch per window. */
 int gofr_run_windows(gofr_ctx *ctx, const gofr_params *p, unsigned nwin,
                      const unsigned long long *primos, unsigned long long *counts_host);
+
+/* One or several Gofrt::calculate windows (as gofr_run_windows; nwin = 0 or
+ * primos = NULL: one window, calculate(p->primo)) with the result made into
+ * doubles on the GPU in FP64, out_host receiving [nwin][leff][nch][nbin]:
+ *   norm 0: the reference's result buffer, bit for bit: each reference
+ *           thread partition's bin is incr added count times, the partitions
+ *           folded in order (lib/src/gofrt.cpp:118,127-132; nparts <= 1: one
+ *           partition);
+ *   norm 1: that buffer divided by the shell volume 4 pi/3 (r+^3 - r-^3),
+ *           r- = b dr + rmin, r+ = (b+1) dr + rmin: the reference's Python
+ *           hist2gofr (pyanalisi/analysis.py:101-105, the normalisation of
+ *           Analysis.compute_gofr, :108-145);
+ *   norm 2: norm 1 further divided by each channel's pair density (distinct
+ *           pairs of types a != b: 2 N_a N_b / V, of one type a:
+ *           N_a (N_a - 1) / V; the self channel of type a: N_a), V the box
+ *           volume averaged over the windows' origin frames (no counterpart in
+ *           the reference, which leaves this to the caller).
+ * rel_err_bound (optional) receives a bound on the relative difference of any
+ * element from the same formula evaluated on the host in FP64 with cubes
+ * within one unit in the last place of exact (numpy's `r ** 3`): 0 for
+ * norm 0.  The frames stay resident: only the doubles come back. */
+int gofr_run_normalized(gofr_ctx *ctx, const gofr_params *p, unsigned nwin,
+                      const unsigned long long *primos, int norm, double *out_host,
+                      double *rel_err_bound);
+
+/* One Gofrt::calculate(primo) (as gofr_run) on frames that stay in the
+ * caller's host memory, for trajectories larger than the device should hold:
+ * the reference bounds its memory the same way, with a window of frames
+ * loaded at a time (Trajectory::set_data_access_block_size / set_access_at,
+ * lib/src/trajectory.cpp:349-384,450-690).  The origins are split into chunks
+ * whose frames (first origin to last origin + last lag) fit max_device_bytes;
+ * each chunk's frames are copied to the device (replacing the context's
+ * resident frames), run, and its exact counts added: the counts equal
+ * gofr_run's on the whole trajectory.  Arguments as gofr_set_frames and
+ * gofr_run; GOFR_ERR_UNSUPPORTED when the budget cannot hold one origin's
+ * lags. */
+int gofr_run_streamed(gofr_ctx *ctx, const double *positions, const double *boxes, int box_kind,
+                      const int *type_ids, unsigned ntypes, size_t natoms, size_t nframes,
+                      const gofr_params *p, size_t max_device_bytes,
+                      unsigned long long *counts_host);
 
 /* Statistics of the last completed run.  No reference counterpart: the
  * reference reports no per-run statistics. */
