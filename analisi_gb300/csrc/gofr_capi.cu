@@ -645,6 +645,7 @@ struct Plan {
     double cell_time = 1e300;    // modelled time / the all-pairs kernel's
     bool cellw = false;          // the warp-streamed form of the cell-list kernel
     int wblk[3] = {1, 1, 1}, nw[3] = {1, 1, 1}, parts = 1;  // its warp blocks
+    int cta_warps = 8, hcopy = 1;  // its CTA size and histogram privatisation depth
     bool wrapcheck = false;
     bool empty = false;        // accepted window empty: nothing can be counted
     Windows w;
@@ -1144,7 +1145,9 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
         for (int k = 0; k < 3; ++k) { C.nc[k] = pl.nc[k]; C.w[k] = pl.wblk[k]; C.nw[k] = pl.nw[k]; }
         C.reach = pl.reach;
         C.r = pl.cell_r;
-        if (cellw_smem_bytes(L.nch, L.nbin, L.ntypes) > max_smem)
+        C.cta_warps = pl.cta_warps;
+        C.hcopy = pl.hcopy;
+        if (cellw_smem_bytes(L.nch, L.nbin, L.ntypes, C.cta_warps, C.hcopy) > max_smem)
             return fail(ctx, GOFR_ERR_UNSUPPORTED, "cell-list histogram does not fit shared memory");
         ++ctx->launches;
         if (launch_cellw_pairs(C, ctx->num_sms, ctx->stream))
@@ -1205,9 +1208,10 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
 // lags) and keeps the fastest per key.
 // ---------------------------------------------------------------------------
 struct TuneChoice {
-    bool cells = false;
+    int kind = 0;               // 0 all pairs, 1 block cell lists, 2 warp-streamed cell lists
     int reach = 1, r = 4;
-    std::array<int, 3> blk{{1, 1, 1}};
+    std::array<int, 3> blk{{1, 1, 1}};  // cells per block (1) or per warp block (2)
+    int cta_warps = 8, hcopy = 1;       // warp-streamed form: CTA size, histogram copies
 };
 
 std::mutex g_tune_mutex;
@@ -1228,7 +1232,9 @@ std::string tune_key(const TrajDev &t, const gofr_params &p)
     return k.str();
 }
 
-// Cache file lines: key cells reach r bx by bz (other lines are skipped).
+// Cache file lines: key kind reach r b0 b1 b2 cta_warps hcopy (lines of an
+// older form, key cells reach r b0 b1 b2, are read as kinds 0/1; other lines
+// are skipped).
 void tune_load_file()
 {
     if (g_tune_loaded) return;
@@ -1240,13 +1246,19 @@ void tune_load_file()
     while (std::getline(in, line)) {
         std::istringstream ls(line);
         std::string key;
-        int cells, m, r, b0, b1, b2;
-        if (!(ls >> key >> cells >> m >> r >> b0 >> b1 >> b2)) continue;
+        int kind, m, r, b0, b1, b2;
+        if (!(ls >> key >> kind >> m >> r >> b0 >> b1 >> b2)) continue;
         TuneChoice c;
-        c.cells = cells != 0;
+        c.kind = kind;
         c.reach = m;
         c.r = r;
         c.blk = {{b0, b1, b2}};
+        int cw, hc;
+        if (ls >> cw >> hc) {
+            c.cta_warps = cw;
+            c.hcopy = hc;
+        }
+        if (c.kind < 0 || c.kind > 2) continue;
         g_tune[key] = c;
     }
 }
@@ -1256,20 +1268,22 @@ void tune_store_file(const std::string &key, const TuneChoice &c)
     const char *path = std::getenv("ANALISI_GB300_TUNE_CACHE");
     if (!path) return;
     std::ofstream out(path, std::ios::app);
-    out << key << " " << (c.cells ? 1 : 0) << " " << c.reach << " " << c.r << " " << c.blk[0]
-        << " " << c.blk[1] << " " << c.blk[2] << "\n";
+    out << key << " " << c.kind << " " << c.reach << " " << c.r << " " << c.blk[0] << " "
+        << c.blk[1] << " " << c.blk[2] << " " << c.cta_warps << " " << c.hcopy << "\n";
 }
 
 // ANALISI_GB300_TUNE_LOG=path appends each timed configuration of the tuner.
-void tune_log(const std::string &key, const char *what, const CellCand *c, double ms)
+void tune_log(const std::string &key, const TuneChoice &c, double ms)
 {
     const char *path = std::getenv("ANALISI_GB300_TUNE_LOG");
     if (!path) return;
     std::ofstream out(path, std::ios::app);
-    out << key << " " << what;
-    if (c)
-        out << " reach=" << c->reach << " r=" << c->r << " blk=" << c->blk[0] << "x" << c->blk[1]
-            << "x" << c->blk[2] << " cost=" << c->cost << " model=" << c->time;
+    static const char *names[3] = {"all-pairs", "block-cells", "warp-cells"};
+    out << key << " " << names[c.kind];
+    if (c.kind)
+        out << " reach=" << c.reach << " r=" << c.r << " blk=" << c.blk[0] << "x" << c.blk[1]
+            << "x" << c.blk[2];
+    if (c.kind == 2) out << " cta_warps=" << c.cta_warps << " hcopy=" << c.hcopy;
     out << " ms=" << ms << "\n";
 }
 
@@ -1288,7 +1302,11 @@ double tune_time(gofr_ctx *ctx, const TrajDev &t, const gofr_params &q, const Pl
             return -1.0;
         cudaEventRecord(ctx->ev[1], ctx->stream);
         unsigned long long pairs = 0;
-        if (enqueue_run(ctx, t, q, rs, pl, ctx->d_counts, &pairs)) return -1.0;
+        if (enqueue_run(ctx, t, q, rs, pl, ctx->d_counts, &pairs)) {
+            ctx->err.clear();
+            (void)cudaGetLastError();
+            return -1.0;
+        }
         cudaEventRecord(ctx->ev[2], ctx->stream);
         if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return -1.0;
         float ms = 0.f;
@@ -1298,36 +1316,71 @@ double tune_time(gofr_ctx *ctx, const TrajDev &t, const gofr_params &q, const Pl
     return best;
 }
 
-// Applies (and if needed measures) the tuned choice for p into pl.
+// The plan of a tuned choice, built on the all-pairs plan base.
+bool plan_of_choice(const TrajDev &t, const gofr_params &p, const Plan &base, const TuneChoice &c,
+                    Plan &out)
+{
+    out = base;
+    out.cells = false;
+    out.cellw = false;
+    if (c.kind == 0) return true;
+    if (c.kind == 1) {
+        for (const CellCand &cc : cell_candidates(t, p))
+            if (cc.reach == c.reach && cc.r == c.r && cc.blk == c.blk) {
+                Plan q = base;
+                if (!make_cell_plan(t, p, q, cc)) return false;
+                out = q;
+                return true;
+            }
+        return false;
+    }
+    for (const CellwCand &cw : cellw_candidates(t, p))
+        if (cw.reach == c.reach && cw.r == c.r && cw.w == c.blk) {
+            Plan q = base;
+            q.cells = false;
+            if (!make_cellw_plan(t, p, q, cw)) return false;
+            q.cta_warps = c.cta_warps;
+            q.hcopy = c.hcopy;
+            out = q;
+            return true;
+        }
+    return false;
+}
+
+// True when the tuner has a choice for this job's key (in this process, or in
+// the file that ANALISI_GB300_TUNE_CACHE names).
+bool tune_known(const TrajDev &t, const gofr_params &p)
+{
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    tune_load_file();
+    return g_tune.count(tune_key(t, p)) != 0;
+}
+
+// Applies the tuned choice for p to the all-pairs plan pl, measuring the
+// candidates first when the key has no choice yet: the all-pairs kernel, the
+// block cell-list kernel in its best modelled configurations, and the
+// warp-streamed cell-list kernel in its best modelled configurations, each
+// with CTAs of 8 and 16 warps and one or two copies of the shared histogram.
 int tune_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
 {
     if (pl.kind != 0 || pl.wrapcheck || pl.empty) return GOFR_OK;  // nothing to choose
-    const std::vector<CellCand> all = cell_candidates(t, p);
-    if (all.empty()) {
-        pl.cells = false;
-        return GOFR_OK;
-    }
     const std::string key = tune_key(t, p);
     const Plan base_pl = pl;
-    auto apply = [&](const TuneChoice &c) {
-        pl = base_pl;
-        pl.cells = false;
-        if (!c.cells) return;
-        for (const CellCand &cc : all)
-            if (cc.reach == c.reach && cc.r == c.r && cc.blk == c.blk) {
-                Plan q = base_pl;
-                if (make_cell_plan(t, p, q, cc)) pl = q;
-                return;
-            }
-    };
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         tune_load_file();
         auto it = g_tune.find(key);
         if (it != g_tune.end()) {
-            apply(it->second);
+            Plan q;
+            if (plan_of_choice(t, p, base_pl, it->second, q)) pl = q;
             return GOFR_OK;
         }
+    }
+    const std::vector<CellCand> all = cell_candidates(t, p);
+    const std::vector<CellwCand> allw = cellw_candidates(t, p);
+    if (all.empty() && allw.empty()) {
+        pl.cells = false;
+        return GOFR_OK;
     }
     // sample of the job: its first origin and the first lags, at least four
     // and enough for ~1.5e10 pairs (the device full several times over)
@@ -1339,31 +1392,52 @@ int tune_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
     q.tmax = (unsigned)std::min<double>(leff, std::max(4.0, want));
     q.ntimesteps = std::max<unsigned>(q.tmax, 1);
     q.skip = q.ntimesteps;
-    Plan base = base_pl;
-    base.cells = false;
-    double best_ms = tune_time(ctx, t, q, base);
-    tune_log(key, "all-pairs", nullptr, best_ms);
-    // the four cheapest estimates, and the cheapest of each reach
-    std::vector<const CellCand *> tries;
-    for (size_t c = 0; c < all.size() && tries.size() < 4; ++c) tries.push_back(&all[c]);
+    std::vector<TuneChoice> tries;
+    tries.push_back(TuneChoice{});  // all pairs
+    // block cell lists: the four cheapest estimates, and the cheapest of each reach
+    std::vector<const CellCand *> bc;
+    for (size_t c = 0; c < all.size() && bc.size() < 4; ++c) bc.push_back(&all[c]);
     for (int m = 1; m <= 2; ++m)
         for (const CellCand &c : all)
             if (c.reach == m) {
-                if (std::find(tries.begin(), tries.end(), &c) == tries.end()) tries.push_back(&c);
+                if (std::find(bc.begin(), bc.end(), &c) == bc.end()) bc.push_back(&c);
                 break;
             }
+    for (const CellCand *c : bc) {
+        TuneChoice tc;
+        tc.kind = 1;
+        tc.reach = c->reach;
+        tc.r = c->r;
+        tc.blk = c->blk;
+        tries.push_back(tc);
+    }
+    // warp-streamed: the three cheapest estimates x CTA size x histogram copies
+    int max_smem = 0;
+    cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device);
+    const int nch = (int)(t.ntypes * (t.ntypes + 1));
+    for (size_t c = 0; c < allw.size() && c < 3; ++c)
+        for (int cw : {8, 16})
+            for (int hc : {1, 2}) {
+                if (cellw_smem_bytes(nch, (int)p.nbin, (int)t.ntypes, cw, hc) > max_smem) continue;
+                TuneChoice tc;
+                tc.kind = 2;
+                tc.reach = allw[c].reach;
+                tc.r = allw[c].r;
+                tc.blk = allw[c].w;
+                tc.cta_warps = cw;
+                tc.hcopy = hc;
+                tries.push_back(tc);
+            }
     TuneChoice choice;
-    for (const CellCand *c : tries) {
-        Plan cp = base_pl;
-        if (!make_cell_plan(t, p, cp, *c)) continue;
+    double best_ms = -1.0;
+    for (const TuneChoice &tc : tries) {
+        Plan cp;
+        if (!plan_of_choice(t, p, base_pl, tc, cp)) continue;
         const double ms = tune_time(ctx, t, q, cp);
-        tune_log(key, "cells", c, ms);
+        tune_log(key, tc, ms);
         if (ms > 0 && (best_ms < 0 || ms < best_ms)) {
             best_ms = ms;
-            choice.cells = true;
-            choice.reach = c->reach;
-            choice.r = c->r;
-            choice.blk = c->blk;
+            choice = tc;
         }
     }
     {
@@ -1371,7 +1445,8 @@ int tune_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
         g_tune[key] = choice;
         tune_store_file(key, choice);
     }
-    apply(choice);
+    Plan chosen;
+    if (plan_of_choice(t, p, base_pl, choice, chosen)) pl = chosen;
     return GOFR_OK;
 }
 
@@ -1386,10 +1461,14 @@ int run_common(gofr_ctx *ctx, const gofr_params *p, unsigned long long *counts_d
     int rc = shape_of(ctx, t, *p, rs);
     if (rc) return rc;
     Plan pl;
-    // the tuner starts from the all-pairs plan and decides on cells itself
-    rc = make_plan(ctx, t, *p, pl, p->kernel != GOFR_KERNEL_TUNED);
+    // the tuner starts from the all-pairs plan and decides on cells itself;
+    // AUTO takes the tuner's choice when it has one for this job's key
+    const bool tuned = p->nparts <= 1 &&
+                       (p->kernel == GOFR_KERNEL_TUNED ||
+                        (p->kernel == GOFR_KERNEL_AUTO && tune_known(t, *p)));
+    rc = make_plan(ctx, t, *p, pl, !tuned);
     if (rc) return rc;
-    if (p->kernel == GOFR_KERNEL_TUNED && p->nparts <= 1) {
+    if (tuned) {
         rc = tune_plan(ctx, t, *p, pl);
         if (rc) return rc;
     }
@@ -1653,6 +1732,8 @@ int build_batch(gofr_ctx *ctx)
         for (int a = 0; a < 3; ++a) { C.nc[a] = q.nc[a]; C.w[a] = q.wblk[a]; C.nw[a] = q.nw[a]; }
         C.reach = q.reach;
         C.r = q.cell_r;
+        C.cta_warps = 8;
+        C.hcopy = 1;
         wl.push_back({(unsigned long long)work[k], C});
         B.launches[k] = PairLaunch{};  // not in the all-pairs queue
     }

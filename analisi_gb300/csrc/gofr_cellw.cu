@@ -41,8 +41,6 @@
 namespace gofr {
 namespace cellw {
 
-constexpr int NT = 256;
-constexpr int NWARP = NT / 32;
 constexpr int CH = 128;        // neighbour records per chunk buffer
 constexpr int CHP = CH + 4;    // + room for NaN records padding a chunk to a multiple of 4
 constexpr int SLOTS = 16;
@@ -125,10 +123,14 @@ struct Walk {
     int row, half, off;          // current segment (row, half) and offset into it
 };
 
-template <int R>
-__global__ void __launch_bounds__(NT, 2) k_pairs_cellw(const CellwLaunch C, int win_cap,
-                                                       int hist_cap)
+// NWARP warps per CTA (8: two CTAs per SM, 16: one), HCOPY copies of the
+// shared histogram (warp w adds to copy w HCOPY / NWARP: the privatisation
+// depth, fewer warps contending for each bin).
+template <int R, int NWARP, int HCOPY>
+__global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const CellwLaunch C,
+                                                                        int win_cap, int hist_cap)
 {
+    constexpr int NT = NWARP * 32;
     // first atoms between two checks of the slot counts (one warp vote each)
     constexpr int VG = R <= 3 ? R : 2;
     static_assert(4 * VG <= SLOTS - 4, "slots for the candidates between two checks");
@@ -136,7 +138,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cellw(const CellwLaunch C, int 
     WarpArea *const areas = reinterpret_cast<WarpArea *>(smem);
     float2 *const win = reinterpret_cast<float2 *>(areas + NWARP);
     unsigned *const hist = reinterpret_cast<unsigned *>(win + win_cap);
-    unsigned short *const chtab = reinterpret_cast<unsigned short *>(hist + hist_cap);
+    unsigned short *const chtab = reinterpret_cast<unsigned short *>(hist + HCOPY * hist_cap);
     __shared__ int s_next, s_abort;
     __shared__ unsigned long long s_pairs;  // pairs evaluated in the current item
 
@@ -144,6 +146,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cellw(const CellwLaunch C, int 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     WarpArea &A = areas[warp];
     const int hlen = P.nch * P.nbin;
+    unsigned *const whist = hist + (warp * HCOPY / NWARP) * hist_cap;  // this warp's copy
     const int half_ch = P.nch / 2;
     const float hi_f = P.hi_f;
     const int ncx = C.nc[0], ncy = C.nc[1], ncz = C.nc[2];
@@ -154,7 +157,8 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cellw(const CellwLaunch C, int 
     const long long NP = P.NP;
 
     for (int i = tid; i < P.nbin; i += NT) win[i] = P.win[i];
-    for (int i = tid; i < hlen; i += NT) hist[i] = 0u;
+    for (int c = 0; c < HCOPY; ++c)
+        for (int i = tid; i < hlen; i += NT) hist[c * hist_cap + i] = 0u;
     for (int i = tid; i < P.ntypes * P.ntypes; i += NT) chtab[i] = P.chtab[i];
     if (lane == 0) {
         mbar_init(&A.bar[0], 1);
@@ -227,7 +231,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cellw(const CellwLaunch C, int 
                 }
 #pragma unroll
                 for (int u = 0; u < FLUSH_ILP; ++u)
-                    red_shared_add1_if(smem_u32(hist + ch[u] * P.nbin + bi[u]),
+                    red_shared_add1_if(smem_u32(whist + ch[u] * P.nbin + bi[u]),
                                        ok[u] && GOFR_CHECK(ch[u] >= 0 && ch[u] < P.nch &&
                                                                bi[u] >= 0 && bi[u] < P.nbin,
                                                            P.err));
@@ -250,7 +254,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cellw(const CellwLaunch C, int 
                                                               xj64[1], xj64[2], P.box64 + fo * 9,
                                                               P.err);
                             const int bb = ref_bin(d2d, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
-                            if (bb >= 0) atomicAdd(hist + ch[u] * P.nbin + bb, 1u);
+                            if (bb >= 0) atomicAdd(whist + ch[u] * P.nbin + bb, 1u);
                         }
                     }
                 }
@@ -270,7 +274,7 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cellw(const CellwLaunch C, int 
                 const double d2d = ref_d2<false>(xi64[0], xi64[1], xi64[2], xj64[0], xj64[1],
                                                  xj64[2], P.box64 + fo * 9, P.err);
                 const int bb = ref_bin(d2d, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
-                if (bb >= 0) atomicAdd(hist + (int)e.z * P.nbin + bb, 1u);
+                if (bb >= 0) atomicAdd(whist + (int)e.z * P.nbin + bb, 1u);
             }
             __syncwarp();
             if (lane == 0) A.qn = 0;
@@ -475,15 +479,16 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cellw(const CellwLaunch C, int 
         }
         __syncthreads();
         const bool abort = s_abort != 0;
-        // add the item's histogram to its lag's counts, then clear it
+        // add the item's histogram copies to its lag's counts, then clear them
         for (int i = tid; i < hlen; i += NT) {
-            const unsigned v = hist[i];
-            if (v) {
-                if (!abort)
-                    atomicAdd(P.counts + (long long)lag_idx * P.every * hlen + i,
-                              (unsigned long long)v);
-                hist[i] = 0u;
+            unsigned long long v = 0;
+#pragma unroll
+            for (int c = 0; c < HCOPY; ++c) {
+                v += hist[c * hist_cap + i];
+                hist[c * hist_cap + i] = 0u;
             }
+            if (v && !abort)
+                atomicAdd(P.counts + (long long)lag_idx * P.every * hlen + i, v);
         }
         __syncthreads();
         if (abort) break;
@@ -502,11 +507,11 @@ __global__ void __launch_bounds__(NT, 2) k_pairs_cellw(const CellwLaunch C, int 
 
 }  // namespace cellw
 
-int cellw_smem_bytes(int nch, int nbin, int ntypes)
+int cellw_smem_bytes(int nch, int nbin, int ntypes, int cta_warps, int hcopy)
 {
     using namespace cellw;
-    size_t b = sizeof(WarpArea) * NWARP + (size_t)nbin * 8 + (size_t)nch * nbin * 4 +
-               (size_t)ntypes * ntypes * 2;
+    size_t b = sizeof(WarpArea) * cta_warps + (size_t)nbin * 8 +
+               (size_t)hcopy * nch * nbin * 4 + (size_t)ntypes * ntypes * 2;
     return (int)((b + 127) / 128 * 128);
 }
 
@@ -560,34 +565,46 @@ int launch_cell_scatter_w(const double *pos64, const unsigned char *types8, size
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-template <int R>
+template <int R, int NWARP, int HCOPY>
 static int launch_cellw_r(const CellwLaunch &C, int num_sms, cudaStream_t s)
 {
     using namespace cellw;
-    const int smem = cellw_smem_bytes(C.pair.nch, C.pair.nbin, C.pair.ntypes);
-    if (cudaFuncSetAttribute(k_pairs_cellw<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem) != cudaSuccess)
+    constexpr int NT = NWARP * 32;
+    auto kern = k_pairs_cellw<R, NWARP, HCOPY>;
+    const int smem = cellw_smem_bytes(C.pair.nch, C.pair.nbin, C.pair.ntypes, NWARP, HCOPY);
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+        cudaSuccess)
         return -1;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairs_cellw<R>, NT, smem) !=
-        cudaSuccess)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem) != cudaSuccess)
         return -1;
     if (per_sm < 1) return -2;
     long long grid = (long long)num_sms * per_sm;
     if (grid > C.pair.n_items) grid = C.pair.n_items;
-    k_pairs_cellw<R><<<(unsigned)grid, NT, smem, s>>>(C, C.pair.nbin, C.pair.nch * C.pair.nbin);
+    kern<<<(unsigned)grid, NT, smem, s>>>(C, C.pair.nbin, C.pair.nch * C.pair.nbin);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int NWARP, int HCOPY>
+static int launch_cellw_shape(const CellwLaunch &C, int num_sms, cudaStream_t s)
+{
+    switch (C.r) {
+    case 2: return launch_cellw_r<2, NWARP, HCOPY>(C, num_sms, s);
+    case 3: return launch_cellw_r<3, NWARP, HCOPY>(C, num_sms, s);
+    case 4: return launch_cellw_r<4, NWARP, HCOPY>(C, num_sms, s);
+    default: return -3;
+    }
 }
 
 int launch_cellw_pairs(const CellwLaunch &C, int num_sms, cudaStream_t s)
 {
     if (C.pair.n_items <= 0) return 0;
-    switch (C.r) {
-    case 2: return launch_cellw_r<2>(C, num_sms, s);
-    case 3: return launch_cellw_r<3>(C, num_sms, s);
-    case 4: return launch_cellw_r<4>(C, num_sms, s);
-    default: return -3;
+    if (C.cta_warps == 16) {
+        return C.hcopy == 2 ? launch_cellw_shape<16, 2>(C, num_sms, s)
+                            : launch_cellw_shape<16, 1>(C, num_sms, s);
     }
+    return C.hcopy == 2 ? launch_cellw_shape<8, 2>(C, num_sms, s)
+                        : launch_cellw_shape<8, 1>(C, num_sms, s);
 }
 
 }  // namespace gofr

@@ -105,8 +105,10 @@ struct CellwLaunch {
     int reach;                     // neighbour cells per side
     int r;                         // first atoms per lane (2, 3 or 4)
     int parts;                     // parts of the warp blocks per (lag, origin)
+    int cta_warps;                 // warps per CTA: 8 (two CTAs per SM) or 16 (one)
+    int hcopy;                     // copies of the shared histogram (privatisation depth: 1, 2)
 };
-int cellw_smem_bytes(int nch, int nbin, int ntypes);
+int cellw_smem_bytes(int nch, int nbin, int ntypes, int cta_warps = 8, int hcopy = 1);
 int cellw_warp_atoms(int r);
 int launch_cell_scatter_w(const double *pos64, const unsigned char *types8, size_t T, size_t N,
                           const double *box_internal, const double *centre, const int *nc,

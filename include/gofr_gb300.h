@@ -65,12 +65,17 @@ enum gofr_kernel {
     GOFR_KERNEL_CELL = 3,        /* cell-list FP32 + recheck kernel (error if not eligible);
                                     ANALISI_GB300_CELL_PLAN="reach,r,bx,by,bz" pins its
                                     configuration when that one is eligible */
-    GOFR_KERNEL_TUNED = 4,       /* AUTO, but the all-pairs / cell-list form and the cell
-                                    configuration are picked by timing them on a sample of
-                                    the job; the choice is remembered per key
-                                    (log2 N, nbin, ntypes, box kind, cell grid) in the
-                                    process and, when the environment variable
-                                    ANALISI_GB300_TUNE_CACHE names a file, across runs
+    GOFR_KERNEL_TUNED = 4,       /* AUTO, but the kernel and its configuration are picked
+                                    by timing them on a sample of the job: the all-pairs
+                                    kernel, the block cell-list kernel (cell size, block
+                                    shape, first atoms per thread) and the warp-streamed
+                                    cell-list kernel (cell size, warp block shape, first
+                                    atoms per lane, CTA size 8 or 16 warps, one or two
+                                    copies of the shared histogram); the choice is
+                                    remembered per key (log2 N, nbin, ntypes, box kind,
+                                    cell grid) in the process and, when the environment
+                                    variable ANALISI_GB300_TUNE_CACHE names a file, across
+                                    runs; AUTO takes a remembered choice for its key
                                     (ANALISI_GB300_TUNE_LOG: a file for every timing) */
     GOFR_KERNEL_CELL_WARP = 5    /* warp-streamed cell-list FP32 + recheck kernel: each warp
                                     streams the neighbourhood of its own small block of cells

@@ -110,7 +110,7 @@ def test_tuned_kernel_choice_is_exact_and_cached(gpu_engine, oracle_mod, tmp_pat
                                   p["every"], p["ntimesteps"], p["primo"])
     a, st = _run(gpu_engine, w, "tuned")
     np.testing.assert_array_equal(a, ref)
-    assert st["kernel_used"] in (1, 3)
+    assert st["kernel_used"] in (1, 3, 5)
     b, st2 = _run(gpu_engine, w, "tuned")
     np.testing.assert_array_equal(b, ref)
     assert st2["kernel_used"] == st["kernel_used"]

@@ -122,3 +122,68 @@ def test_cellw_windows_and_debug_free_stats(gpu_engine, oracle_mod):
         ref = oracle_mod.gofrt_counts(w["positions"], w["boxes"], w["type_ids"], w["ntypes"],
                                       p["rmin"], p["rmax"], p["nbin"], 2, 4, 2, 1, 4, pr)
         np.testing.assert_array_equal(got[k], ref)
+
+
+def _child(kernel, env):
+    import json
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    out = subprocess.run([sys.executable, os.path.join(here, "tune_child.py"), kernel],
+                         env={**os.environ, **env}, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    return json.loads(out.stdout.strip().splitlines()[-1])
+
+
+def _want(oracle_mod):
+    from tune_child import case
+    w = case()
+    p = w["params"]
+    c = oracle_mod.gofrt_counts(w["positions"], w["boxes"], w["type_ids"], w["ntypes"],
+                                p["rmin"], p["rmax"], p["nbin"], p["tmax"], 8, p["skip"],
+                                p["every"], p["ntimesteps"], p["primo"])
+    return {"sum": int(c.sum()),
+            "weighted": int((c.astype(object) * (1 + np.arange(c.size).reshape(c.shape))).sum())}
+
+
+def test_tuned_choice_is_persisted_and_reused_by_auto(built_engine, oracle_mod, tmp_path):
+    """GOFR_KERNEL_TUNED times the all-pairs kernel and both cell-list forms
+    (the warp-streamed one with CTAs of 8 and 16 warps and one or two
+    histogram copies), writes its choice to ANALISI_GB300_TUNE_CACHE; a new
+    process running AUTO on the same key takes that choice without timing
+    anything.  Counts are the oracle's every time."""
+    want = _want(oracle_mod)
+    cache, log1, log2 = (str(tmp_path / n) for n in ("cache.txt", "log1.txt", "log2.txt"))
+    a = _child("tuned", {"ANALISI_GB300_TUNE_CACHE": cache, "ANALISI_GB300_TUNE_LOG": log1})
+    assert {k: a[k] for k in want} == want
+    timed = open(log1).read()
+    assert "all-pairs" in timed and "block-cells" in timed
+    assert "cta_warps=16 hcopy=2" in timed and "cta_warps=8 hcopy=1" in timed
+    lines = open(cache).read().split("\n")
+    key, kind = lines[0].split()[0], int(lines[0].split()[1])
+    assert len(lines[0].split()) == 9
+    b = _child("auto", {"ANALISI_GB300_TUNE_CACHE": cache, "ANALISI_GB300_TUNE_LOG": log2})
+    assert {k: b[k] for k in want} == want
+    assert b["kernel_used"] == {0: 1, 1: 3, 2: 5}[kind]
+    import os
+    assert not os.path.exists(log2) or open(log2).read() == ""  # nothing timed again
+    assert open(cache).read().count("\n") == 1                   # nothing stored again
+
+
+@pytest.mark.parametrize("shape", ["8 1", "8 2", "16 1", "16 2"])
+def test_every_cta_size_and_histogram_depth_is_exact(built_engine, oracle_mod, tmp_path, shape):
+    """A cache line pins the warp-streamed kernel's CTA size and histogram
+    copies (through AUTO's use of the cache); each variant counts exactly."""
+    want = _want(oracle_mod)
+    cache = str(tmp_path / "cache.txt")
+    first = _child("tuned", {"ANALISI_GB300_TUNE_CACHE": cache})
+    key = open(cache).read().split()[0]
+    # the warp-streamed planner's first choice for this job, with this shape
+    from analisi_gb300 import engine  # noqa: F401
+    with open(cache, "w") as f:
+        f.write(f"{key} 2 2 2 1 1 2 {shape}\n")
+    b = _child("auto", {"ANALISI_GB300_TUNE_CACHE": cache})
+    assert first["sum"] == want["sum"]
+    assert b["kernel_used"] == 5
+    assert {k: b[k] for k in want} == want
