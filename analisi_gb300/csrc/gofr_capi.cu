@@ -1382,16 +1382,23 @@ int tune_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl)
         pl.cells = false;
         return GOFR_OK;
     }
-    // sample of the job: its first origin and the first lags, at least four
-    // and enough for ~1.5e10 pairs (the device full several times over)
+    // sample of the job: its first origins and first lags, about eight
+    // (lag, origin) items per SM (as many as a long job keeps in flight, so
+    // no kernel is timed on items split finer than the job's) and at most
+    // 3e11 ordered pairs
     const unsigned leff = (p.ntimesteps < p.tmax || p.tmax == 0) ? p.ntimesteps : p.tmax;
-    const double want = std::ceil(1.5e10 / ((double)t.N * (double)t.N));
+    const unsigned skip = p.skip ? p.skip : 1;
+    const double n2 = (double)t.N * (double)t.N;
+    const double items = std::max(16.0, std::min(8.0 * ctx->num_sms, std::floor(3e11 / n2)));
+    const unsigned n_l = (unsigned)std::max<double>(
+        1.0, std::min<double>(leff, std::max(4.0, std::ceil(std::sqrt(items)))));
+    const unsigned n_o = (unsigned)std::ceil(items / n_l);
     gofr_params q = p;
     q.kernel = GOFR_KERNEL_AUTO;
     q.nparts = 1;
-    q.tmax = (unsigned)std::min<double>(leff, std::max(4.0, want));
-    q.ntimesteps = std::max<unsigned>(q.tmax, 1);
-    q.skip = q.ntimesteps;
+    q.every = 1;
+    q.tmax = n_l;
+    q.ntimesteps = std::min<unsigned>(p.ntimesteps, std::max<unsigned>(n_l, n_o * skip));
     std::vector<TuneChoice> tries;
     tries.push_back(TuneChoice{});  // all pairs
     // block cell lists: the four cheapest estimates, and the cheapest of each reach
