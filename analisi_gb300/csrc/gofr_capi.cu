@@ -442,6 +442,206 @@ Bound error_bound_cells(const TrajDev &t)
     return b;
 }
 
+// FP64-level slop of the cell lists, per axis (v = 2^-53; the box is the
+// same in every frame; X >= |x - xlo| over the coordinates):
+//   eref  the reference's own rounding of its difference and of its wrap
+//         steps (triclinic: the tilt steps the z and y wraps add to y and x)
+//   ew    rounding of the FP64 reduction w of a coordinate into the cell
+//   Mw    bound on |w - c|, c the box centre (a quotient rounding across an
+//         integer leaves w just outside [lo, lo + L))
+// Triclinic reduction (wrap_tric64): |n_z| <= nz = floor(X_z / Lz) + 2, the
+// y input y1 = y - n_z yz has |y1 - ylo| <= Y1 = X_y + nz |yz|, |n_y| <= ny
+// likewise, and the x inputs x1 = x - n_z xz, x2 = x1 - n_y xy have
+// |x2 - xlo| <= X2 = X_x + nz |xz| + ny |xy|; each FMA rounds once.
+struct CellSlop {
+    double eref[3], ew[3], Mw[3], kmax[3];
+};
+
+CellSlop cell_slop(const TrajDev &t)
+{
+    CellSlop c{};
+    const double v = std::ldexp(1.0, -53), g40 = 1.0 + std::ldexp(1.0, -40);
+    const BoxStats &s = t.bs;
+    double D[3];
+    for (int k = 0; k < 3; ++k) D[k] = 2.0 * t.M[k] * g40;
+    auto kmax_of = [](double Dk, double Lmin) { return std::floor(Dk / Lmin + 0.5) + 1.0; };
+    if (!t.tric) {
+        for (int k = 0; k < 3; ++k) {
+            c.kmax[k] = kmax_of(D[k], s.Lmin[k]);
+            c.eref[k] = v * D[k] + c.kmax[k] * v * (D[k] + s.Lmax[k]);
+        }
+    } else {
+        c.kmax[2] = kmax_of(D[2], s.Lmin[2]);
+        c.eref[2] = v * D[2] + c.kmax[2] * v * (D[2] + s.Lmax[2]);
+        const double Dy = D[1] + c.kmax[2] * s.tmax[2];
+        c.kmax[1] = kmax_of(Dy, s.Lmin[1]);
+        c.eref[1] = v * D[1] + c.kmax[2] * v * Dy + c.kmax[1] * v * (Dy + s.Lmax[1]);
+        const double Dx = D[0] + c.kmax[2] * s.tmax[1] + c.kmax[1] * s.tmax[0];
+        c.kmax[0] = kmax_of(Dx, s.Lmin[0]);
+        c.eref[0] = v * D[0] + (c.kmax[2] + c.kmax[1]) * v * Dx + c.kmax[0] * v * (Dx + s.Lmax[0]);
+    }
+    double lo[3], L[3], X[3], ctr[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = t.h_box[k];
+        L[k] = 2.0 * t.h_box[3 + k];
+        X[k] = t.M[k] + std::fabs(t.shift[k] - lo[k]);
+        ctr[k] = lo[k] + 0.5 * L[k];
+    }
+    double Xin[3] = {X[0], X[1], X[2]};  // bound on |input - lo| of each axis's reduction
+    double ein[3] = {0.0, 0.0, 0.0};     // rounding of that input
+    if (t.tric) {
+        const double xy = std::fabs(t.h_box[6]), xz = std::fabs(t.h_box[7]),
+                     yz = std::fabs(t.h_box[8]);
+        const double nz = std::floor(X[2] / L[2]) + 2.0;
+        const double Y1 = (X[1] + nz * yz) * g40;
+        const double ny = std::floor(Y1 / L[1]) + 2.0;
+        const double X1 = (X[0] + nz * xz) * g40;
+        const double X2 = (X[0] + nz * xz + ny * xy) * g40;
+        Xin[1] = Y1;
+        Xin[0] = X2;
+        ein[1] = v * (std::fabs(lo[1]) + Y1);
+        ein[0] = v * (std::fabs(lo[0]) + X1) + v * (std::fabs(lo[0]) + X2);
+    }
+    for (int k = 0; k < 3; ++k) {
+        c.Mw[k] = 0.5 * L[k] + 3.0 * v * (Xin[k] + L[k]) + v * (std::fabs(lo[k]) + L[k]);
+        c.ew[k] = ein[k] + v * (std::fabs(ctr[k]) + c.Mw[k]);
+    }
+    return c;
+}
+
+// Neighbourhood geometry of the warp-streamed kernel on one cell grid (the
+// tables of CellwLaunch) and the FP32 image vectors with their error.
+struct CellwGeom {
+    int nz_lo = 0, nz_hi = 0, ny_lo[3] = {0, 0, 0}, ny_hi[3] = {0, 0, 0};
+    int nx_lo[15] = {}, nx_hi[15] = {};
+    int nz_span = 0, ny_span = 0, nx_span = 0;  // widest layer range, row range, cell range
+    float4 shift[CELLW_NSHIFT] = {};
+    double S[3] = {0, 0, 0};   // max |FP32 image vector| per axis over the images reached
+    double eT[3] = {0, 0, 0};  // max |FP32 image vector - lattice vector| per axis
+};
+
+inline int floordiv_h(int a, int n) { return a >= 0 ? a / n : -((n - 1 - a) / n); }
+
+// The rows and cells a warp block must reach: every lattice image of a cell
+// that comes within rm of the block on each axis, rm = rmax plus the FP64
+// slop (the reference's rounding, the reduction's, the cell assignment's
+// quotient), so every pair the reference counts is evaluated.  A cell's
+// image under (sx, sy, sz) is shifted by sz (xz, yz, Lz) + sy (xy, Ly, 0) +
+// sx (Lx, 0, 0): in cells of edge h, a layer's rows start (sz yz / h_y) cells
+// off and a row's cells (sz xz + sy xy) / h_x.  Orthorhombic grids (cell
+// edge >= rmax (1 + 1e-6) / reach) give lo = -reach, hi = reach - 1 on every
+// axis.  False when an image falls outside the table (sx, sy in -2..2,
+// sz in -1..1; orthorhombic: every s in -1..1, the block kernel's bound).
+bool cellw_geometry(const TrajDev &t, const gofr_params &p, const int nc[3], CellwGeom &g)
+{
+    g = CellwGeom{};
+    const double v = std::ldexp(1.0, -53);
+    const CellSlop cs = cell_slop(t);
+    const double erefn =
+        std::sqrt(cs.eref[0] * cs.eref[0] + cs.eref[1] * cs.eref[1] + cs.eref[2] * cs.eref[2]);
+    double L[3], h[3], rho[3];
+    for (int k = 0; k < 3; ++k) {
+        L[k] = 2.0 * t.h_box[3 + k];
+        h[k] = L[k] / nc[k];
+        const double rm = (p.rmax + erefn + 2.0 * cs.ew[k] +
+                           8.0 * v * (std::fabs(t.h_box[k]) + 2.0 * L[k])) *
+                          (1.0 + std::ldexp(1.0, -40));
+        rho[k] = rm / h[k];
+    }
+    const double xy = t.tric ? t.h_box[6] : 0.0, xz = t.tric ? t.h_box[7] : 0.0,
+                 yz = t.tric ? t.h_box[8] : 0.0;
+    const double tiny = 1e-12;  // floor of a value next to an integer: take the wider range
+    g.nz_lo = (int)std::floor(-rho[2] - tiny);
+    g.nz_hi = (int)std::floor(rho[2] + tiny);
+    g.nz_span = g.nz_hi - g.nz_lo + 1;
+    const int smax = t.tric ? 2 : 1;
+    const int sz_lo = floordiv_h(g.nz_lo, nc[2]), sz_hi = floordiv_h(nc[2] + g.nz_hi, nc[2]);
+    if (sz_lo < -1 || sz_hi > 1) return false;
+    int sx_lo = 0, sx_hi = 0, sy_lo = 0, sy_hi = 0;
+    for (int sz = sz_lo; sz <= sz_hi; ++sz) {
+        const double oy = sz * yz / h[1];
+        const int a = (int)std::floor(-rho[1] - oy - tiny), b = (int)std::floor(rho[1] - oy + tiny);
+        g.ny_lo[sz + 1] = a;
+        g.ny_hi[sz + 1] = b;
+        g.ny_span = std::max(g.ny_span, b - a + 1);
+        const int ylo = floordiv_h(a, nc[1]), yhi = floordiv_h(nc[1] + b, nc[1]);
+        if (ylo < -smax || yhi > smax) return false;
+        sy_lo = std::min(sy_lo, ylo);
+        sy_hi = std::max(sy_hi, yhi);
+        for (int sy = ylo; sy <= yhi; ++sy) {
+            const double ox = (sz * xz + sy * xy) / h[0];
+            const int c0 = (int)std::floor(-rho[0] - ox - tiny),
+                      c1 = (int)std::floor(rho[0] - ox + tiny);
+            const int k = (sz + 1) * 5 + sy + 2;
+            g.nx_lo[k] = c0;
+            g.nx_hi[k] = c1;
+            g.nx_span = std::max(g.nx_span, c1 - c0 + 1);
+            const int xlo = floordiv_h(c0, nc[0]), xhi = floordiv_h(nc[0] + c1, nc[0]);
+            if (xlo < -smax || xhi > smax) return false;
+            sx_lo = std::min(sx_lo, xlo);
+            sx_hi = std::max(sx_hi, xhi);
+        }
+    }
+    // image vectors: FP64 sum of exact products (|s| <= 2), rounded to FP32
+    for (int sz = -1; sz <= 1; ++sz)
+        for (int sy = -2; sy <= 2; ++sy)
+            for (int sx = -2; sx <= 2; ++sx) {
+                double T[3] = {sx * L[0], sy * L[1], sz * L[2]};
+                T[0] = T[0] + sy * xy;
+                T[0] = T[0] + sz * xz;
+                T[1] = T[1] + sz * yz;
+                const double mag[3] = {std::fabs(sx * L[0]) + std::fabs(sy * xy) +
+                                           std::fabs(sz * xz),
+                                       std::fabs(sy * L[1]) + std::fabs(sz * yz),
+                                       std::fabs(sz * L[2])};
+                float f[3];
+                for (int k = 0; k < 3; ++k) f[k] = (float)T[k];
+                g.shift[(sx + 2) + 5 * (sy + 2) + 25 * (sz + 1)] =
+                    make_float4(f[0], f[1], f[2], 0.0f);
+                if (sx < sx_lo || sx > sx_hi || sy < sy_lo || sy > sy_hi || sz < sz_lo ||
+                    sz > sz_hi)
+                    continue;
+                for (int k = 0; k < 3; ++k) {
+                    g.S[k] = std::max(g.S[k], (double)std::fabs(f[k]));
+                    g.eT[k] = std::max(g.eT[k], std::fabs((double)f[k] - T[k]) + 2.0 * v * mag[k]);
+                }
+            }
+    return true;
+}
+
+// Per-axis error bound of the warp-streamed kernel's FP32 differences in a
+// triclinic box (the same in every frame), with the slop of cell_slop and
+// the image vectors of g (u = 2^-24):
+//   a = fl32(fl64(w - c)):              |a - (w - c)| <= (u + 2v) Mw = d3
+//   b = fl32(a_j + sh), sh the FP32 image vector (|sh| <= S, |sh - T| <= eT):
+//                                       |b - (a_j + sh)| <= u (A + S) = d4
+//   a_i - b = the lattice image d*_K of the reference's difference (K the
+//     lattice vector of the two reductions and the image) + the reductions'
+//     rounding (ew each) + the conversions (d3 each) + (T - sh) + d4
+//   dx = fl32(a_i - b):                 |dx - (a_i - b)| <= u (2 A + S + d4)
+// plus the reference's own rounding (eref).  For a pair the reference counts
+// its image is d*_K itself (the one lattice translate within half the box on
+// every axis), so these are its component errors; d2 is then formed as in
+// the all-pairs kernel and Efun applies.
+Bound error_bound_cells_tric(const TrajDev &t, const CellwGeom &g)
+{
+    Bound b{};
+    const double u = std::ldexp(1.0, -24), v = std::ldexp(1.0, -53);
+    const CellSlop cs = cell_slop(t);
+    for (int k = 0; k < 3; ++k) {
+        const double d3 = (u + 2.0 * v) * cs.Mw[k];
+        const double A = cs.Mw[k] * (1.0 + 2.0 * u) + d3;
+        const double d4 = u * (A + g.S[k]);
+        const double ea = g.eT[k] + 2.0 * cs.ew[k] + 2.0 * d3 + d4;
+        const double esub = u * (2.0 * A + g.S[k] + d4);
+        b.e[k] = (ea + esub + cs.eref[k]) * (1.0 + std::ldexp(1.0, -20));
+        b.kmax[k] = cs.kmax[k];
+    }
+    b.enorm = std::sqrt(b.e[0] * b.e[0] + b.e[1] * b.e[1] + b.e[2] * b.e[2]);
+    b.eta = 0.0;
+    return b;
+}
+
 inline double Efun(const Bound &b, double s)
 {
     if (s < 0) s = 0;
@@ -646,6 +846,7 @@ struct Plan {
     bool cellw = false;          // the warp-streamed form of the cell-list kernel
     int wblk[3] = {1, 1, 1}, nw[3] = {1, 1, 1}, parts = 1;  // its warp blocks
     int cta_warps = 8, hcopy = 1;  // its CTA size and histogram privatisation depth
+    CellwGeom geom;                // its neighbourhood tables and image vectors
     bool wrapcheck = false;
     bool empty = false;        // accepted window empty: nothing can be counted
     Windows w;
@@ -666,9 +867,12 @@ struct CellCand {
     double time = 1e300;    // modelled time / the all-pairs kernel's
 };
 
-bool cell_eligible(const TrajDev &t, const gofr_params &p)
+// Cell lists need a box that is the same in every frame (the frames share
+// one grid) and one reference thread partition; the block kernel also an
+// orthorhombic box (the warp-streamed kernel takes triclinic ones).
+bool cell_eligible(const TrajDev &t, const gofr_params &p, bool allow_tric = false)
 {
-    if (t.tric || !t.box_constant || p.nparts > 1) return false;
+    if ((t.tric && !allow_tric) || !t.box_constant || p.nparts > 1) return false;
     if (!(p.rmax > 0.0)) return false;
     if (t.N >= (1u << 24)) return false;  // sorted slots pack type << 24 | atom id
     // large histograms use the global-memory form of the all-pairs kernel
@@ -778,12 +982,14 @@ bool cell_override(const TrajDev &t, const gofr_params &p, CellCand &out)
 // Turns an FP32 plan (thresholds set) into the cell-list form of configuration
 // c, with the cell kernel's own bound and windows.  False when the minimum
 // image of the candidates is not certain without a per-pair wrap test.
-bool make_cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl, const CellCand &c)
+bool make_cell_plan(const TrajDev &t, const gofr_params &p, Plan &pl, const CellCand &c,
+                    const Bound *bound = nullptr)
 {
     if (pl.kind != 0 || pl.th.empty()) return false;
+    if (t.tric && !bound) return false;  // the block kernel's bound is orthorhombic
     Plan q = pl;
     apply_cell(q, c);
-    q.b = error_bound_cells(t);
+    q.b = bound ? *bound : error_bound_cells(t);
     certify(q.b, q.th.data(), p.nbin, q.w);
     const double emax = std::max(q.b.e[0], std::max(q.b.e[1], q.b.e[2]));
     const double reach = std::sqrt((double)q.w.hi_f) * (1.0 + std::ldexp(1.0, -20)) +
@@ -822,27 +1028,33 @@ struct CellwCand {
 // two standard deviations of density fluctuation, rounded up to passes of
 // 32 r) times its neighbourhood's atoms, plus a fixed overhead per staged
 // chunk (a row of the neighbourhood, in one or two pieces), relative to N^2.
+// Triclinic neighbourhoods take the widest row and cell ranges of their
+// geometry (one more than the orthorhombic 2 reach where a tilt shifts them).
 std::vector<CellwCand> cellw_candidates(const TrajDev &t, const gofr_params &p)
 {
     std::vector<CellwCand> all;
     // slots carry the neighbour's type in 6 bits
-    if (!cell_eligible(t, p) || t.ntypes > 64) return all;
+    if (!cell_eligible(t, p, true) || t.ntypes > 64) return all;
     if (cellw_smem_bytes((int)(t.ntypes * (t.ntypes + 1)), (int)p.nbin, (int)t.ntypes) >
         110 * 1024)
         return all;  // two CTAs per SM, or not at all
     for (int m = 1; m <= 3; ++m) {
         int nc[3];
-        if (!cell_grid(t, p, m, nc)) continue;
+        CellwGeom g;
+        if (!cell_grid(t, p, m, nc) || !cellw_geometry(t, p, nc, g)) continue;
         const double ncell = (double)nc[0] * nc[1] * nc[2];
         const double per_cell = (double)t.N / ncell;
         for (int wx = 1; wx <= 4; ++wx)
             for (int wy = 1; wy <= 4; ++wy)
                 for (int wz = 1; wz <= 4; ++wz) {
                     if (wx + 2 * m > nc[0] || wy + 2 * m > nc[1] || wz + 2 * m > nc[2]) continue;
-                    if (wy * wz > 16 || (wy + 2 * m) * (wz + 2 * m) > CELLW_MAX_ROWS) continue;
+                    // a row wraps the box at most once
+                    if (wx + g.nx_span > nc[0]) continue;
+                    const int nrow = (wy + g.ny_span) * (wz + g.nz_span);
+                    if (wy * wz > 16 || nrow > CELLW_MAX_ROWS) continue;
                     const double atoms = per_cell * wx * wy * wz;
-                    const double rows = (double)(wy + 2 * m) * (wz + 2 * m);
-                    const double row_atoms = per_cell * (wx + 2 * m);
+                    const double rows = (double)nrow;
+                    const double row_atoms = per_cell * (wx + g.nx_span);
                     const double nbhd = rows * row_atoms;
                     const double blocks = (double)((nc[0] + wx - 1) / wx) *
                                           ((nc[1] + wy - 1) / wy) * ((nc[2] + wz - 1) / wz);
@@ -858,7 +1070,7 @@ std::vector<CellwCand> cellw_candidates(const TrajDev &t, const gofr_params &p)
                         c.r = r;
                         for (int k = 0; k < 3; ++k) c.nc[k] = nc[k];
                         c.w = {{wx, wy, wz}};
-                        c.fraction = (double)(wx + 2 * m) * (wy + 2 * m) * (wz + 2 * m) / ncell;
+                        c.fraction = rows * (wx + g.nx_span) / ncell;
                         c.cost = blocks * passes * TI * (nbhd + 24.0 * chunks) /
                                  ((double)t.N * t.N);
                         all.push_back(c);
@@ -900,9 +1112,17 @@ bool make_cellw_plan(const TrajDev &t, const gofr_params &p, Plan &pl, const Cel
     for (int k = 0; k < 3; ++k) cc.nc[k] = c.nc[k];
     cc.fraction = c.fraction;
     cc.time = c.cost;
+    CellwGeom g;
+    if (!cellw_geometry(t, p, c.nc, g)) return false;
     Plan q = pl;
-    if (!make_cell_plan(t, p, q, cc)) return false;
+    if (t.tric) {
+        const Bound b = error_bound_cells_tric(t, g);
+        if (!make_cell_plan(t, p, q, cc, &b)) return false;
+    } else if (!make_cell_plan(t, p, q, cc)) {
+        return false;
+    }
     q.cellw = true;
+    q.geom = g;
     for (int k = 0; k < 3; ++k) {
         q.wblk[k] = c.w[k];
         q.nw[k] = (c.nc[k] + c.w[k] - 1) / c.w[k];
@@ -919,6 +1139,9 @@ bool make_cellw_plan(const TrajDev &t, const gofr_params &p, Plan &pl, const Cel
 // AUTO takes the cell-list form when its modelled time is below this share of
 // the all-pairs kernel's (a margin for the model's error).
 constexpr double kCellAutoTime = 0.85;
+// ... and the warp-streamed form in a triclinic box when its modelled
+// evaluated pairs are below this share of the all-pairs kernel's.
+constexpr double kCellwTricAuto = 0.5;
 
 int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl,
               bool allow_cells = true)
@@ -964,18 +1187,28 @@ int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl,
     }
     // the warp-streamed form: on request, and for AUTO wherever the block
     // cell-list form was taken and the warp form is eligible (measured faster
-    // on every workload where both run)
+    // on every workload where both run), and for triclinic boxes (which the
+    // block form does not take) where its modelled cost is below
+    // kCellwTricAuto of the all-pairs pairs
     if (allow_cells && !pl.wrapcheck &&
-        (req == GOFR_KERNEL_CELL_WARP || (req == GOFR_KERNEL_AUTO && pl.cells))) {
+        (req == GOFR_KERNEL_CELL_WARP || (req == GOFR_KERNEL_AUTO && (pl.cells || t.tric)))) {
         CellwCand c;
         Plan q = pl;
         q.cells = false;
-        if (cellw_choice(t, p, c) && make_cellw_plan(t, p, q, c)) pl = q;
+        if (cellw_choice(t, p, c) &&
+            (req != GOFR_KERNEL_AUTO || pl.cells || c.cost < kCellwTricAuto) &&
+            make_cellw_plan(t, p, q, c))
+            pl = q;
     }
-    if ((req == GOFR_KERNEL_CELL || req == GOFR_KERNEL_CELL_WARP) && !pl.cells)
+    if (req == GOFR_KERNEL_CELL && !pl.cells)
         return fail(ctx, GOFR_ERR_UNSUPPORTED,
-                    "cell lists need an orthorhombic box constant over the frames with at least "
-                    "3 cells of edge >= rmax per axis, and nparts <= 1");
+                    "the block cell-list kernel needs an orthorhombic box constant over the "
+                    "frames with at least 3 cells of edge >= rmax per axis, and nparts <= 1");
+    if (req == GOFR_KERNEL_CELL_WARP && !pl.cells)
+        return fail(ctx, GOFR_ERR_UNSUPPORTED,
+                    "cell lists need a box constant over the frames with at least 3 cells of "
+                    "edge >= rmax per axis (triclinic: tilts that keep every image reached "
+                    "within two cells' widths of the box), and nparts <= 1");
     return GOFR_OK;
 }
 
@@ -989,10 +1222,20 @@ int check_device_error(gofr_ctx *ctx)
                     (e & ERRW_WAIT_TIMEOUT) ? "bounded wait ran out " : "",
                     (e & ERRW_WRAP_LOOP) ? "minimum-image iteration cap " : "",
                     (e & ERRW_QUEUE) ? "work queue overflow " : "",
-                    (e & ERRW_BOUNDS) ? "debug bounds check failed " : "",
+                    (e & ERRW_BOUNDS) ? "bounds check failed " : "",
                     (e & ERRW_HIST_OVERFLOW) ? "an item evaluated 2^32 pairs or more (run "
                                                "discarded; use the block cell-list kernel)" : "");
     return GOFR_OK;
+}
+
+void set_cellw_geometry(CellwLaunch &C, const CellwGeom &g)
+{
+    C.nz_lo = g.nz_lo;
+    C.nz_hi = g.nz_hi;
+    for (int k = 0; k < 3; ++k) { C.ny_lo[k] = g.ny_lo[k]; C.ny_hi[k] = g.ny_hi[k]; }
+    for (int k = 0; k < 15; ++k) { C.nx_lo[k] = g.nx_lo[k]; C.nx_hi[k] = g.nx_hi[k]; }
+    C.ny_span = g.ny_span;
+    for (int k = 0; k < CELLW_NSHIFT; ++k) C.shift[k] = g.shift[k];
 }
 
 // Builds (once per grid and frames) the cell-sorted copy of t's frames.  On
@@ -1003,6 +1246,8 @@ int ensure_cells(gofr_ctx *ctx, const TrajDev &t, const Plan &pl)
 {
     TrajDev &tm = const_cast<TrajDev &>(t);
     const bool aos = pl.cellw;  // the warp-streamed kernel's records, else the SoA frames
+    if (t.tric && !aos)
+        return fail(ctx, GOFR_ERR_UNSUPPORTED, "the block cell-list kernel is orthorhombic");
     if (tm.cell_nc[0] == pl.nc[0] && tm.cell_nc[1] == pl.nc[1] && tm.cell_nc[2] == pl.nc[2] &&
         (aos ? tm.d_wpos != nullptr : tm.d_spos != nullptr))
         return GOFR_OK;
@@ -1040,11 +1285,12 @@ int ensure_cells(gofr_ctx *ctx, const TrajDev &t, const Plan &pl)
     double centre[3];
     for (int k = 0; k < 3; ++k) centre[k] = t.h_box[k] + t.h_box[3 + k];  // xlo + L/2
     int brc = launch_cell_build(t.pos64, t.types8, t.T, t.N, &t.h_box[0], centre, pl.nc,
-                                cell_of, rank_of, count, tm.d_cstart, tm.d_spos, tm.d_sidt,
-                                ctx->stream);
+                                t.tric != 0, cell_of, rank_of, count, tm.d_cstart, tm.d_spos,
+                                tm.d_sidt, ctx->stream);
     if (!brc && aos)
         brc = launch_cell_scatter_w(t.pos64, t.types8, t.T, t.N, &t.h_box[0], centre, pl.nc,
-                                    cell_of, rank_of, tm.d_cstart, tm.d_wpos, ctx->stream);
+                                    t.tric != 0, cell_of, rank_of, tm.d_cstart, tm.d_wpos,
+                                    ctx->stream);
     const cudaError_t se = cudaStreamSynchronize(ctx->stream);
     drop_temp();
     if (brc || se != cudaSuccess) {
@@ -1147,6 +1393,7 @@ int enqueue_run(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, const Run
         C.r = pl.cell_r;
         C.cta_warps = pl.cta_warps;
         C.hcopy = pl.hcopy;
+        set_cellw_geometry(C, pl.geom);
         if (cellw_smem_bytes(L.nch, L.nbin, L.ntypes, C.cta_warps, C.hcopy) > max_smem)
             return fail(ctx, GOFR_ERR_UNSUPPORTED, "cell-list histogram does not fit shared memory");
         ++ctx->launches;
@@ -1225,9 +1472,9 @@ std::string tune_key(const TrajDev &t, const gofr_params &p)
     std::ostringstream k;
     k << "n2^" << lg << "_bins" << p.nbin << "_types" << t.ntypes << (t.tric ? "_tric" : "_ortho");
     int nc[3];
-    if (cell_eligible(t, p) && cell_grid(t, p, 2, nc))
+    if (cell_eligible(t, p, true) && cell_grid(t, p, 2, nc))
         k << "_halfcells" << nc[0] << "x" << nc[1] << "x" << nc[2];
-    else if (cell_eligible(t, p) && cell_grid(t, p, 1, nc))
+    else if (cell_eligible(t, p, true) && cell_grid(t, p, 1, nc))
         k << "_cells" << nc[0] << "x" << nc[1] << "x" << nc[2];
     return k.str();
 }
@@ -1741,6 +1988,7 @@ int build_batch(gofr_ctx *ctx)
         C.r = q.cell_r;
         C.cta_warps = 8;
         C.hcopy = 1;
+        set_cellw_geometry(C, q.geom);
         wl.push_back({(unsigned long long)work[k], C});
         B.launches[k] = PairLaunch{};  // not in the all-pairs queue
     }

@@ -94,25 +94,41 @@ __device__ __forceinline__ int wrapi(int a, int n)
 // ---------------------------------------------------------------------------
 // cell build
 // ---------------------------------------------------------------------------
+// tric: the cell of the coordinates reduced into the axis-aligned cell by
+// the lattice (wrap_tric64, as the warp-streamed records are), else of the
+// fractional part of each coordinate's quotient.
 __global__ void k_cell_assign(const double *__restrict__ pos, size_t T, size_t N, double xlo,
-                              double ylo, double zlo, double Lx, double Ly, double Lz, int ncx,
-                              int ncy, int ncz, int *__restrict__ cell_of,
-                              int *__restrict__ rank_of, int *__restrict__ count)
+                              double ylo, double zlo, double Lx, double Ly, double Lz, double xy,
+                              double xz, double yz, int tric, int ncx, int ncy, int ncz,
+                              int *__restrict__ cell_of, int *__restrict__ rank_of,
+                              int *__restrict__ count)
 {
     const int ncell = ncx * ncy * ncz;
     for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < T * N;
          g += (size_t)gridDim.x * blockDim.x) {
         const size_t f = g / N;
         const double *p = pos + g * 3;
-        double u[3] = {__ddiv_rn(__dsub_rn(p[0], xlo), Lx), __ddiv_rn(__dsub_rn(p[1], ylo), Ly),
-                       __ddiv_rn(__dsub_rn(p[2], zlo), Lz)};
         const int nc[3] = {ncx, ncy, ncz};
         int c[3];
+        if (tric) {
+            const double lo[3] = {xlo, ylo, zlo}, L[3] = {Lx, Ly, Lz}, tilt[3] = {xy, xz, yz};
+            double w[3];
+            wrap_tric64(p, lo, L, tilt, w);
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            double w = u[k] - floor(u[k]);
-            int ck = (int)(w * nc[k]);
-            c[k] = ck < 0 ? 0 : (ck >= nc[k] ? nc[k] - 1 : ck);
+            for (int k = 0; k < 3; ++k) {
+                const double u = __ddiv_rn(__dsub_rn(w[k], lo[k]), L[k]);
+                const int ck = (int)floor(u * nc[k]);
+                c[k] = ck < 0 ? 0 : (ck >= nc[k] ? nc[k] - 1 : ck);
+            }
+        } else {
+            double u[3] = {__ddiv_rn(__dsub_rn(p[0], xlo), Lx), __ddiv_rn(__dsub_rn(p[1], ylo), Ly),
+                           __ddiv_rn(__dsub_rn(p[2], zlo), Lz)};
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                double w = u[k] - floor(u[k]);
+                int ck = (int)(w * nc[k]);
+                c[k] = ck < 0 ? 0 : (ck >= nc[k] ? nc[k] - 1 : ck);
+            }
         }
         const int cell = (c[2] * ncy + c[1]) * ncx + c[0];
         cell_of[g] = cell;
@@ -652,11 +668,12 @@ int cell_block_atoms(int r) { return cells::NT * r; }
 int cell_max_ranges() { return cells::MAXR; }
 
 int launch_cell_build(const double *pos64, const unsigned char *types8, size_t T, size_t N,
-                      const double *box_internal, const double *centre, const int *nc,
+                      const double *box_internal, const double *centre, const int *nc, bool tric,
                       int *cell_of, int *rank_of, int *count, int *start, float *spos,
                       unsigned *sidt, cudaStream_t s)
 {
     using namespace cells;
+    if (tric && (spos || sidt)) return -1;  // the block kernel's frames are orthorhombic
     const int ncell = nc[0] * nc[1] * nc[2];
     if (cudaMemsetAsync(count, 0, T * (size_t)(ncell + 1) * sizeof(int), s) != cudaSuccess)
         return -1;
@@ -669,8 +686,9 @@ int launch_cell_build(const double *pos64, const unsigned char *types8, size_t T
     if (blocks > 152 * 16) blocks = 152 * 16;
     const double Lx = 2.0 * box_internal[3], Ly = 2.0 * box_internal[4], Lz = 2.0 * box_internal[5];
     k_cell_assign<<<blocks, NT, 0, s>>>(pos64, T, N, box_internal[0], box_internal[1],
-                                        box_internal[2], Lx, Ly, Lz, nc[0], nc[1], nc[2], cell_of,
-                                        rank_of, count);
+                                        box_internal[2], Lx, Ly, Lz, box_internal[6],
+                                        box_internal[7], box_internal[8], tric ? 1 : 0, nc[0],
+                                        nc[1], nc[2], cell_of, rank_of, count);
     k_cell_scan<<<(unsigned)T, NT, 0, s>>>(count, start, ncell);
     if (spos && sidt)
         k_cell_scatter<<<blocks, NT, 0, s>>>(pos64, types8, T, N, NP, ncell, box_internal[0],

@@ -19,9 +19,23 @@
 // per chunk of CH records, two chunk buffers per warp, completion tracked by
 // one mbarrier per buffer.  Cells reached across the box boundary are the
 // periodic image of the cell: after the copy lands, the warp moves the
-// chunk's records to that image (x += s fl32(L), one FP32 rounding, the
-// block kernel's arithmetic), so the pair arithmetic and its certified error
-// bound (gofr_capi.cu, error_bound_cells) are the block kernel's.
+// chunk's records to that image (x += fl32 of the lattice vector, one FP32
+// rounding per axis; orthorhombic: s fl32(L), the block kernel's
+// arithmetic), so the pair arithmetic and its certified error bound
+// (gofr_capi.cu, error_bound_cells) are the block kernel's.
+//
+// Triclinic boxes (upper-triangular cell vectors a, b, c) use the same
+// kernel.  The reference's minimum image (z, then y, then x) leaves every
+// component within half the box edge, so its image of a pair is the one
+// lattice translate inside the axis-aligned box [-L/2, L/2]^3, and a pair it
+// counts (distance < rmax < L/2) has exactly one image within rmax.  Cells
+// are therefore an axis-aligned grid of the cell's axis-aligned fundamental
+// domain, atoms reduced into it by the lattice; a layer reached across a z
+// face is the image +-c, shifted in y and x by the tilts, and a row reached
+// across a y face the image +-b, shifted in x: each layer's rows and each
+// row's cells start a fraction of a cell off, which host tables give (one
+// more cell where the shift is not whole), together with the FP32 lattice
+// vector of each image.
 //
 // Warps never wait for one another inside a work item (lag, origin, part of
 // the warp blocks): they pull warp blocks from a shared counter, stream
@@ -90,12 +104,10 @@ __device__ __forceinline__ f2 pair2s(f2 xi, f2 yi, f2 zi, f2 xj, f2 yj, f2 zj)
     return d2;
 }
 
-__device__ __forceinline__ int wrapi(int a, int n)
-{
-    a %= n;
-    return a < 0 ? a + n : a;
-}
-__device__ __forceinline__ int image_of(int c, int n) { return c < 0 ? -1 : (c >= n ? 1 : 0); }
+// floor(a / n) for n > 0
+__device__ __forceinline__ int floordiv(int a, int n) { return a >= 0 ? a / n : -((n - 1 - a) / n); }
+
+constexpr unsigned SEG_BEGIN = 0x1ffffffu;  // a segment's begin; its image index above bit 25
 
 // Orders this thread's generic-proxy shared-memory accesses before later
 // async-proxy (bulk copy) writes to the same buffer.
@@ -110,7 +122,8 @@ struct WarpArea {
     uint2 slots[SLOTS][32];      // candidates {d2 bits, r << 30 | type << 24 | atom id of j}
     uint4 q[QW];                 // FP64 recheck queue {ia, ja, channel, 0}
     unsigned iv[4][32];          // type << 24 | atom id of the first atoms (R <= 4)
-    int2 seg[2 * MAXROWS];       // sorted ranges of the neighbourhood rows (two halves each)
+    int2 seg[2 * MAXROWS];       // sorted ranges of the neighbourhood rows (two halves each):
+                                 // {begin | image << 25, end}
     uint64_t bar[2];             // one mbarrier per chunk buffer
     int n[2];                    // records in each buffer
     int code[2];                 // image of each buffer's records
@@ -141,6 +154,8 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
     unsigned short *const chtab = reinterpret_cast<unsigned short *>(hist + HCOPY * hist_cap);
     __shared__ int s_next, s_abort;
     __shared__ unsigned long long s_pairs;  // pairs evaluated in the current item
+    __shared__ float4 s_shift[CELLW_NSHIFT];
+    __shared__ int2 s_ny[3], s_nx[15];
 
     const PairLaunch &P = C.pair;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -151,7 +166,6 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
     const float hi_f = P.hi_f;
     const int ncx = C.nc[0], ncy = C.nc[1], ncz = C.nc[2];
     const int ncell = ncx * ncy * ncz;
-    const int m = C.reach;
     const int nwx = C.nw[0], nwy = C.nw[1], nwz = C.nw[2];
     const int nwb = nwx * nwy * nwz;
     const long long NP = P.NP;
@@ -160,6 +174,9 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
     for (int c = 0; c < HCOPY; ++c)
         for (int i = tid; i < hlen; i += NT) hist[c * hist_cap + i] = 0u;
     for (int i = tid; i < P.ntypes * P.ntypes; i += NT) chtab[i] = P.chtab[i];
+    for (int i = tid; i < CELLW_NSHIFT; i += NT) s_shift[i] = C.shift[i];
+    if (tid < 3) s_ny[tid] = make_int2(C.ny_lo[tid], C.ny_hi[tid]);
+    if (tid < 15) s_nx[tid] = make_int2(C.nx_lo[tid], C.nx_hi[tid]);
     if (lane == 0) {
         mbar_init(&A.bar[0], 1);
         mbar_init(&A.bar[1], 1);
@@ -172,12 +189,6 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
     unsigned ph0 = 0u, ph1 = 0u;      // mbarrier phases of the two buffers
     bool dead = false;                // a bounded wait of this warp ran out
     unsigned long long n_cand = 0, n_rech = 0, n_eval = 0;
-    float L32[3];
-    {
-        const Box32 b = P.box32[0];  // the box is the same in every frame
-#pragma unroll
-        for (int a = 0; a < 3; ++a) L32[a] = b.L[a];
-    }
 
     for (long long g = blockIdx.x; g < P.n_items; g += gridDim.x) {
         // item = (lag, origin, part): lag slowest
@@ -200,6 +211,13 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
         }
         __syncthreads();
 
+        // the reference's d2 of a pair in FP64 (its minimum image for the box kind)
+        auto ref_d2_box = [&](const double *xi64, const double *xj64, const double *box) {
+            return P.tric ? ref_d2<true>(xi64[0], xi64[1], xi64[2], xj64[0], xj64[1], xj64[2],
+                                         box, P.err)
+                          : ref_d2<false>(xi64[0], xi64[1], xi64[2], xj64[0], xj64[1], xj64[2],
+                                          box, P.err);
+        };
         // Bins every slot of this warp's lanes (each lane its own, FLUSH_ILP
         // per round), then empties them.
         int cnt = 0;
@@ -250,9 +268,7 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                         } else {
                             const double *xi64 = P.pos64 + (fo * P.N + ia[u]) * 3;
                             const double *xj64 = P.pos64 + (fl * P.N + ja[u]) * 3;
-                            const double d2d = ref_d2<false>(xi64[0], xi64[1], xi64[2], xj64[0],
-                                                              xj64[1], xj64[2], P.box64 + fo * 9,
-                                                              P.err);
+                            const double d2d = ref_d2_box(xi64, xj64, P.box64 + fo * 9);
                             const int bb = ref_bin(d2d, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
                             if (bb >= 0) atomicAdd(whist + ch[u] * P.nbin + bb, 1u);
                         }
@@ -271,8 +287,7 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                 const uint4 e = A.q[q];
                 const double *xi64 = P.pos64 + (fo * P.N + (int)e.x) * 3;
                 const double *xj64 = P.pos64 + (fl * P.N + (int)e.y) * 3;
-                const double d2d = ref_d2<false>(xi64[0], xi64[1], xi64[2], xj64[0], xj64[1],
-                                                 xj64[2], P.box64 + fo * 9, P.err);
+                const double d2d = ref_d2_box(xi64, xj64, P.box64 + fo * 9);
                 const int bb = ref_bin(d2d, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
                 if (bb >= 0) atomicAdd(whist + (int)e.z * P.nbin + bb, 1u);
             }
@@ -308,46 +323,67 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
             }
             const int n_i = __shfl_sync(0xffffffffu, ipre, 31);
             if (n_i == 0) continue;
-            // the neighbourhood: rows (y, z) in [cy0 - m, cy0 + cny + m) x
-            // [cz0 - m, cz0 + cnz + m), each the x cells [cx0 - m, cx0 + cnx + m)
-            // in one or two sorted ranges (two when the row wraps the box)
-            const int jny = cny + 2 * m, jnz = cnz + 2 * m, jnx = cnx + 2 * m;
-            const int nrows = jny * jnz;
+            // the neighbourhood: layers uz (image sz), in each the rows uy
+            // (image sy), each row the cells ux in one or two sorted ranges
+            // (two when the row wraps the box: images sx and sx + 1); the
+            // layer's row slots beyond its own rows stay empty
+            const int jny = cny + C.ny_span;
+            const int nrows = (cnz + C.nz_hi - C.nz_lo + 1) * jny;
             for (int rr = lane; rr < nrows; rr += 32) {
-                const int uy = cy0 - m + rr % jny, uz = cz0 - m + rr / jny;
-                const int base = (wrapi(uz, ncz) * ncy + wrapi(uy, ncy)) * ncx;
-                const int a = wrapi(cx0 - m, ncx), b = a + jnx;
-                if (b <= ncx) {
-                    A.seg[2 * rr] = make_int2(st_l[base + a], st_l[base + b]);
-                    A.seg[2 * rr + 1] = make_int2(0, 0);
-                } else {
-                    A.seg[2 * rr] = make_int2(st_l[base + a], st_l[base + ncx]);
-                    A.seg[2 * rr + 1] = make_int2(st_l[base], st_l[base + b - ncx]);
+                const int lz = rr / jny, k = rr - lz * jny;
+                const int uz = cz0 + C.nz_lo + lz;
+                const int sz = floordiv(uz, ncz), cz = uz - sz * ncz;
+                int2 s0 = make_int2(0, 0), s1 = make_int2(0, 0);
+                // the host keeps every image reached inside the tables and every
+                // row within one wrap of the box; a row outside them is reported
+                // and left empty (no access outside the tables or the frame)
+                bool ok = sz >= -1 && sz <= 1;
+                const int2 yr = ok ? s_ny[sz + 1] : make_int2(0, -1 - cny);
+                if (k <= cny + yr.y - yr.x) {
+                    const int uy = cy0 + yr.x + k;
+                    const int sy = floordiv(uy, ncy), cy = uy - sy * ncy;
+                    ok = sy >= -2 && sy <= 2;
+                    const int2 xr = ok ? s_nx[(sz + 1) * 5 + sy + 2] : make_int2(0, 0);
+                    const int ux = cx0 + xr.x, len = cnx + xr.y - xr.x + 1;
+                    const int sx = floordiv(ux, ncx), a = ux - sx * ncx, b = a + len;
+                    ok = ok && sx >= -2 && len >= 0 && len <= ncx && (b <= ncx ? sx <= 2 : sx <= 1);
+                    if (ok) {
+                        const int base = (cz * ncy + cy) * ncx;
+                        const unsigned code =
+                            (unsigned)((sx + 2) + 5 * (sy + 2) + 25 * (sz + 1)) << 25;
+                        if (b <= ncx) {
+                            s0 = make_int2((int)((unsigned)st_l[base + a] | code), st_l[base + b]);
+                        } else {
+                            s0 = make_int2((int)((unsigned)st_l[base + a] | code),
+                                           st_l[base + ncx]);
+                            s1 = make_int2((int)((unsigned)st_l[base] | (code + (1u << 25))),
+                                           st_l[base + b - ncx]);
+                        }
+                    }
                 }
+                if (!ok) atomicOr(P.err, ERRW_BOUNDS);
+                A.seg[2 * rr] = s0;
+                A.seg[2 * rr + 1] = s1;
             }
             __syncwarp();
             int n_j = 0;
-            for (int s = lane; s < 2 * nrows; s += 32) n_j += A.seg[s].y - A.seg[s].x;
+            for (int s = lane; s < 2 * nrows; s += 32)
+                n_j += A.seg[s].y - (int)((unsigned)A.seg[s].x & SEG_BEGIN);
             n_j = __reduce_add_sync(0xffffffffu, n_j);
-            const int sx0 = image_of(cx0 - m, ncx);
-            // image code of segment (row, half): (sx + 1) | (sy + 1) << 2 | (sz + 1) << 4
-            auto seg_code = [&](int rr, int h) {
-                const int uy = cy0 - m + rr % jny, uz = cz0 - m + rr / jny;
-                return (sx0 + h + 1) | (image_of(uy, ncy) + 1) << 2 | (image_of(uz, ncz) + 1) << 4;
-            };
             // Advances w to the next non-empty piece and (lane 0) copies it into
             // buffer b; returns false at the end of the neighbourhood.
             auto issue = [&](Walk &w, int b) -> bool {
                 while (w.row < nrows) {
                     const int2 sg = A.seg[2 * w.row + w.half];
-                    const int len = sg.y - sg.x;
+                    const int beg = (int)((unsigned)sg.x & SEG_BEGIN);
+                    const int len = sg.y - beg;
                     if (w.off < len) {
                         const int n = min(CH, len - w.off);
                         if (lane == 0) {
                             A.n[b] = n;
-                            A.code[b] = seg_code(w.row, w.half);
+                            A.code[b] = (int)((unsigned)sg.x >> 25);
                             mbar_arrive_expect_tx(&A.bar[b], (unsigned)(n * 16));
-                            bulk_g2s(&A.buf[b][0], rec_l + sg.x + w.off, (unsigned)(n * 16),
+                            bulk_g2s(&A.buf[b][0], rec_l + beg + w.off, (unsigned)(n * 16),
                                      &A.bar[b]);
                         }
                         w.off += n;
@@ -416,14 +452,14 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                     const int n = A.n[b];
                     const int code = A.code[b];
                     float4 *const bufp = A.buf[b];
-                    if (code != 21) {  // 21: image (0, 0, 0)
-                        const int s0 = (code & 3) - 1, s1 = ((code >> 2) & 3) - 1,
-                                  s2 = ((code >> 4) & 3) - 1;
+                    if (code != CELLW_SHIFT0) {  // image (0, 0, 0): nothing to move
+                        // a zero component adds exactly nothing (x + 0 = x)
+                        const float4 sh = s_shift[code];
                         for (int e = lane; e < n; e += 32) {
                             float4 v = bufp[e];
-                            if (s0) v.x = __fadd_rn(v.x, s0 > 0 ? L32[0] : -L32[0]);
-                            if (s1) v.y = __fadd_rn(v.y, s1 > 0 ? L32[1] : -L32[1]);
-                            if (s2) v.z = __fadd_rn(v.z, s2 > 0 ? L32[2] : -L32[2]);
+                            v.x = __fadd_rn(v.x, sh.x);
+                            v.y = __fadd_rn(v.y, sh.y);
+                            v.z = __fadd_rn(v.z, sh.z);
                             bufp[e] = v;
                         }
                     }
@@ -519,26 +555,36 @@ int cellw_warp_atoms(int r) { return 32 * r; }
 
 // Sorted AoS copy of every frame: {x, y, z, type << 24 | id} with the block
 // kernel's coordinates (w = x - n L, n = floor((x - xlo) / L), one FMA in
-// FP64, then fl32(fl64(w - c)), c the box centre).
+// FP64, then fl32(fl64(w - c)), c the box centre); triclinic: w the lattice
+// reduction of wrap_tric64, the same FP32 rounding about the centre.
 __global__ void k_cell_scatter_w(const double *__restrict__ pos64,
                                  const unsigned char *__restrict__ types8, size_t T, size_t N,
                                  size_t NP, int ncell, double xlo, double ylo, double zlo,
-                                 double Lx, double Ly, double Lz, double cx, double cy, double cz,
+                                 double Lx, double Ly, double Lz, double xy, double xz, double yz,
+                                 int tric, double cx, double cy, double cz,
                                  const int *__restrict__ cell_of, const int *__restrict__ rank_of,
                                  const int *__restrict__ start, float4 *__restrict__ wpos)
 {
     const double lo[3] = {xlo, ylo, zlo}, L[3] = {Lx, Ly, Lz}, c[3] = {cx, cy, cz};
+    const double tilt[3] = {xy, xz, yz};
     for (size_t g = blockIdx.x * (size_t)blockDim.x + threadIdx.x; g < T * N;
          g += (size_t)gridDim.x * blockDim.x) {
         const size_t f = g / N, a = g - f * N;
         const size_t d = (size_t)start[f * (size_t)(ncell + 1) + cell_of[g]] + rank_of[g];
         const double *p = pos64 + g * 3;
         float v[3];
+        if (tric) {
+            double w[3];
+            wrap_tric64(p, lo, L, tilt, w);
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            const double n = floor(__ddiv_rn(__dsub_rn(p[k], lo[k]), L[k]));
-            const double w = __fma_rn(-n, L[k], p[k]);
-            v[k] = __double2float_rn(__dsub_rn(w, c[k]));
+            for (int k = 0; k < 3; ++k) v[k] = __double2float_rn(__dsub_rn(w[k], c[k]));
+        } else {
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const double n = floor(__ddiv_rn(__dsub_rn(p[k], lo[k]), L[k]));
+                const double w = __fma_rn(-n, L[k], p[k]);
+                v[k] = __double2float_rn(__dsub_rn(w, c[k]));
+            }
         }
         wpos[f * NP + d] =
             make_float4(v[0], v[1], v[2], __uint_as_float(((unsigned)types8[a] << 24) | (unsigned)a));
@@ -547,8 +593,8 @@ __global__ void k_cell_scatter_w(const double *__restrict__ pos64,
 
 int launch_cell_scatter_w(const double *pos64, const unsigned char *types8, size_t T, size_t N,
                           const double *box_internal, const double *centre, const int *nc,
-                          const int *cell_of, const int *rank_of, const int *start, float4 *wpos,
-                          cudaStream_t s)
+                          bool tric, const int *cell_of, const int *rank_of, const int *start,
+                          float4 *wpos, cudaStream_t s)
 {
     const int ncell = nc[0] * nc[1] * nc[2];
     const size_t NP = padded_natoms(N);
@@ -560,8 +606,9 @@ int launch_cell_scatter_w(const double *pos64, const unsigned char *types8, size
     const double Lx = 2.0 * box_internal[3], Ly = 2.0 * box_internal[4], Lz = 2.0 * box_internal[5];
     k_cell_scatter_w<<<blocks, 256, 0, s>>>(pos64, types8, T, N, NP, ncell, box_internal[0],
                                             box_internal[1], box_internal[2], Lx, Ly, Lz,
-                                            centre[0], centre[1], centre[2], cell_of, rank_of,
-                                            start, wpos);
+                                            box_internal[6], box_internal[7], box_internal[8],
+                                            tric ? 1 : 0, centre[0], centre[1], centre[2],
+                                            cell_of, rank_of, start, wpos);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 

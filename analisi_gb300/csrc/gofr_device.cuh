@@ -178,4 +178,25 @@ __device__ __forceinline__ int ref_bin(double d2, double rmin, double dr, double
     return ((unsigned)idx < (unsigned)nbin) ? idx : -1;
 }
 
+// Lattice translate of p into the axis-aligned cell [lo, lo + L) of an
+// upper-triangular box (cell vectors a = (Lx, 0, 0), b = (xy, Ly, 0),
+// c = (xz, yz, Lz); tilt = {xy, xz, yz}), in FP64: the z count from one
+// quotient and floor, the z, y and x components moved by FMAs, then y, then
+// x.  Each FMA rounds once, so w differs from p - (nz c + ny b + nx a) by at
+// most 2^-53 (|y1| + |w_y|) in y and 2^-53 (|x1| + |x2| + |w_x|) in x.  A
+// quotient that rounds across an integer leaves w just outside the cell.
+__device__ __forceinline__ void wrap_tric64(const double p[3], const double lo[3],
+                                            const double L[3], const double tilt[3], double w[3])
+{
+    const double nz = floor(__ddiv_rn(__dsub_rn(p[2], lo[2]), L[2]));
+    w[2] = __fma_rn(-nz, L[2], p[2]);
+    const double y1 = __fma_rn(-nz, tilt[2], p[1]);
+    const double x1 = __fma_rn(-nz, tilt[1], p[0]);
+    const double ny = floor(__ddiv_rn(__dsub_rn(y1, lo[1]), L[1]));
+    w[1] = __fma_rn(-ny, L[1], y1);
+    const double x2 = __fma_rn(-ny, tilt[0], x1);
+    const double nx = floor(__ddiv_rn(__dsub_rn(x2, lo[0]), L[0]));
+    w[0] = __fma_rn(-nx, L[0], x2);
+}
+
 }  // namespace gofr

@@ -12,7 +12,8 @@ enum : unsigned {
     ERRW_WAIT_TIMEOUT = 1u,   // a bounded mbarrier wait ran out
     ERRW_WRAP_LOOP = 2u,      // the FP64 iterative minimum image exceeded its iteration cap
     ERRW_QUEUE = 4u,          // a work queue overflowed its capacity
-    ERRW_BOUNDS = 8u,         // a debug bounds check failed (GOFR_DEBUG_BOUNDS builds only)
+    ERRW_BOUNDS = 8u,         // a bounds check failed (GOFR_CHECK in GOFR_DEBUG_BOUNDS builds;
+                              // the warp-streamed kernel's neighbourhood tables always)
     ERRW_HIST_OVERFLOW = 16u  // an item could have overflowed a u32 shared bin (run discarded)
 };
 
@@ -94,7 +95,22 @@ struct CellLaunch {
 // One launch of the warp-streamed cell-list kernel (gofr_cellw.cu): items
 // are (lag, origin, part), pair.n_items = n_lags * n_orig * parts; each warp
 // takes blocks of w[0] x w[1] x w[2] cells of the part's range.
-constexpr int CELLW_MAX_ROWS = 64;  // neighbourhood rows (w_y + 2 reach)(w_z + 2 reach)
+//
+// Cells are an axis-aligned grid of the box [lo, lo + L) (triclinic: the
+// upper-triangular cell's axis-aligned fundamental domain).  A warp block's
+// neighbourhood is given relative to the block, per lattice image
+// (sx, sy, sz) of the cells reached: layers uz in [cz0 + nz_lo, cz0 + cnz +
+// nz_hi] (image sz = floor(uz / ncz)); in a layer of image sz, rows uy in
+// [cy0 + ny_lo[sz+1], cy0 + cny + ny_hi[sz+1]] (image sy); in a row of images
+// (sy, sz), cells ux in [cx0 + nx_lo[k], cx0 + cnx + nx_hi[k]], k = (sz + 1) 5 +
+// sy + 2 (image sx).  Orthorhombic boxes have lo = -reach, hi = reach - 1
+// everywhere; a triclinic layer or row is shifted by the tilts, so its range
+// starts a fraction of a cell off and may take one cell more.  shift[]
+// holds the FP32 lattice vector of each image, index (sx + 2) + 5 (sy + 2) +
+// 25 (sz + 1).
+constexpr int CELLW_MAX_ROWS = 64;  // neighbourhood rows of a warp block (all its layers)
+constexpr int CELLW_NSHIFT = 75;    // images sx, sy in -2..2, sz in -1..1
+constexpr int CELLW_SHIFT0 = 37;    // index of the image (0, 0, 0)
 struct CellwLaunch {
     PairLaunch pair;
     const int *start;              // [T][ncell+1] sorted-record offset of each cell
@@ -107,13 +123,21 @@ struct CellwLaunch {
     int parts;                     // parts of the warp blocks per (lag, origin)
     int cta_warps;                 // warps per CTA: 8 (two CTAs per SM) or 16 (one)
     int hcopy;                     // copies of the shared histogram (privatisation depth: 1, 2)
+    int nz_lo, nz_hi;              // neighbourhood layers (see above)
+    int ny_lo[3], ny_hi[3];        // rows, per layer image sz + 1
+    int nx_lo[15], nx_hi[15];      // cells, per row images (sz + 1) 5 + sy + 2
+    int ny_span;                   // max over sz of ny_hi - ny_lo + 1
+    float4 shift[CELLW_NSHIFT];    // FP32 lattice vector {x, y, z, 0} of each image
 };
 int cellw_smem_bytes(int nch, int nbin, int ntypes, int cta_warps = 8, int hcopy = 1);
 int cellw_warp_atoms(int r);
+// box_internal {xlo, ylo, zlo, lx/2, ly/2, lz/2, xy, xz, yz}; tric: the
+// coordinates are reduced into the axis-aligned cell by the lattice (z, then
+// y, then x), else per axis.
 int launch_cell_scatter_w(const double *pos64, const unsigned char *types8, size_t T, size_t N,
                           const double *box_internal, const double *centre, const int *nc,
-                          const int *cell_of, const int *rank_of, const int *start, float4 *wpos,
-                          cudaStream_t s);
+                          bool tric, const int *cell_of, const int *rank_of, const int *start,
+                          float4 *wpos, cudaStream_t s);
 int launch_cellw_pairs(const CellwLaunch &C, int num_sms, cudaStream_t s);
 
 // FP64 normalisation of window counts on the device (gofr_norm.cu).
@@ -185,9 +209,10 @@ int launch_neigh_sort(const NeighLaunch &L, int num_sms, cudaStream_t s);
 
 // Cell assignment and per-frame cell starts (and, with spos/sidt non-null,
 // the block kernel's SoA sorted frames); cell_of and rank_of are left for
-// launch_cell_scatter_w.
+// launch_cell_scatter_w.  tric: cells of the coordinates reduced into the
+// axis-aligned cell by the lattice (spos/sidt must then be null).
 int launch_cell_build(const double *pos64, const unsigned char *types8, size_t T, size_t N,
-                      const double *box_internal, const double *centre, const int *nc,
+                      const double *box_internal, const double *centre, const int *nc, bool tric,
                       int *cell_of, int *rank_of, int *count, int *start, float *spos,
                       unsigned *sidt, cudaStream_t s);
 // One trajectory's cell-list items in one launch.

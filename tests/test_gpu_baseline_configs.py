@@ -79,13 +79,13 @@ def test_c2_16k_atoms_default_plan_all_pairs_and_fp64(gpu_engine, oracle_mod):
 def test_c3_32k_atoms_triclinic(gpu_engine, oracle_mod):
     """32768 atoms in the triclinic cell a=(L,0,0), b=(0.3L,L,0),
     c=(0.2L,0.1L,L), L=70, 500 bins on [0, 15]: origins 0 and 500, lags
-    {0, 1, 50}, default plan and plain FP64."""
+    {0, 1, 50}, through the default plan (the warp-streamed cell-list kernel
+    on tilted cells), the all-pairs FP32 kernel and plain FP64."""
     w = workloads.c3()
     gpu_engine.set_frames(w["positions"], w["boxes"], w["type_ids"], w["ntypes"], triclinic=True)
     samples = [(o, lag) for o in (0, 500) for lag in (1, 50)]
-    used = _check_samples(gpu_engine, oracle_mod, w, samples, ["auto", "f64"])
-    assert used["f64"] == {2}
-    assert used["auto"] <= {1, 3}
+    used = _check_samples(gpu_engine, oracle_mod, w, samples, ["auto", "cellw", "f32", "f64"])
+    assert used == {"auto": {5}, "cellw": {5}, "f32": {1}, "f64": {2}}
 
 
 def test_c5_131k_atoms_cells_against_fp64_all_pairs(gpu_engine, oracle_mod):

@@ -26,7 +26,9 @@ def _ref(oracle_mod, w, p):
 
 @pytest.mark.parametrize("kernel,tric,L,rmax", [("f32", False, 18.0, 5.0), ("f32", True, 14.0, 5.0),
                                                  ("f32", False, 6.0, 4.5),  # wrap check
-                                                 ("f64", True, 14.0, 5.0), ("cell", False, 26.0, 5.0)])
+                                                 ("f64", True, 14.0, 5.0), ("cell", False, 26.0, 5.0),
+                                                 ("cellw", False, 26.0, 5.0),
+                                                 ("cellw", True, 26.0, 5.0)])
 def test_debug_build_parity_without_check_failures(debug_lib, oracle_mod, kernel, tric, L, rmax):
     from analisi_gb300 import engine
     w = workloads.small_case(95, 1500 if L > 10 else 120, 8, L, 0.2, [900, 600] if L > 10 else [70, 50],
