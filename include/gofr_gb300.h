@@ -78,11 +78,15 @@ enum gofr_kernel {
                                     runs; AUTO takes a remembered choice for its key
                                     (ANALISI_GB300_TUNE_LOG: a file for every timing) */
     GOFR_KERNEL_CELL_WARP = 5    /* warp-streamed cell-list FP32 + recheck kernel: each warp
-                                    streams the neighbourhood of its own small block of cells
-                                    (error if not eligible: the cell-list conditions and at
-                                    most 64 types); AUTO takes it wherever it would take the
-                                    block cell-list form.  ANALISI_GB300_CELLW_PLAN=
-                                    "reach,r,wx,wy,wz" pins its configuration */
+                                    streams the neighbourhood of its own small block of cells;
+                                    orthorhombic and triclinic boxes (error if not eligible:
+                                    the cell-list conditions, at most 64 types, and tilts
+                                    that keep the images a block reaches within two box
+                                    edges).  AUTO takes it wherever it would take the block
+                                    cell-list form, and for a triclinic box when it
+                                    evaluates under half of the pairs.
+                                    ANALISI_GB300_CELLW_PLAN="reach,r,wx,wy,wz" pins its
+                                    configuration */
 };
 
 /* Parameters of one Gofrt::calculate (lib/include/gofrt.h:37-45 constructor
