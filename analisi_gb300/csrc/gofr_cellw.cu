@@ -41,11 +41,15 @@
 // the warp blocks): they pull warp blocks from a shared counter, stream
 // their own neighbourhoods and add their candidates to the CTA's shared
 // histogram; the CTA synchronises only at the end of the item, to add the
-// histogram to the counts.  Candidates (FP32 d2 <= hi_f) go to per-lane
-// slots carrying d2 and the neighbour's own type and id, so slots outlive
-// the chunk buffers and are binned (the block kernel's certified window
-// test, predicated shared-memory reductions) only when some lane's slots are
-// nearly full or the warp's first atoms change.
+// histogram to the counts.  Candidates (FP32 d2 <= hi_f) are compacted into
+// a dense per-warp queue as they are found (one ballot per record and first
+// atom group: each candidate lane writes at the warp's count plus the
+// candidates of the lanes below it); an entry names the first atom and the
+// record of the current chunk buffer, 16 bits.  The queue is binned 32
+// entries at a time, every lane busy: when it is nearly full and at the end
+// of each chunk (before the buffer is refilled), d2 recomputed with the
+// pair loop's arithmetic (the same value), then the block kernel's
+// certified window test and predicated shared-memory reductions.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -57,11 +61,11 @@ namespace cellw {
 
 constexpr int CH = 128;        // neighbour records per chunk buffer
 constexpr int CHP = CH + 4;    // + room for NaN records padding a chunk to a multiple of 4
-constexpr int SLOTS = 16;
+constexpr int CQ = 512;        // candidate queue entries of a warp
+constexpr int CQ_ROOM = 4 * 32; // entries one first-atom group of one step can add
 constexpr int QW = 32;         // FP64 recheck queue of a warp
 constexpr int MAXROWS = CELLW_MAX_ROWS;  // neighbourhood rows of a warp block
-constexpr int FLUSH_ILP = 2;
-static_assert(SLOTS % FLUSH_ILP == 0, "a flush round reads rows q0 .. q0 + FLUSH_ILP - 1 < SLOTS");
+static_assert(CH + 4 <= 256, "a queue entry names a record of the chunk buffer in 8 bits");
 
 typedef unsigned long long f2;
 __device__ __forceinline__ f2 f2pk(float a, float b)
@@ -109,6 +113,14 @@ __device__ __forceinline__ int floordiv(int a, int n) { return a >= 0 ? a / n : 
 
 constexpr unsigned SEG_BEGIN = 0x1ffffffu;  // a segment's begin; its image index above bit 25
 
+// Record k of a chunk buffer whose records are interleaved in pairs (unit
+// k / 2 = {x0, x1, y0, y1, z0, z1, w0, w1}).
+__device__ __forceinline__ float4 unit_record(const float4 *buf, unsigned k)
+{
+    const float *p = reinterpret_cast<const float *>(buf) + (k >> 1) * 8 + (k & 1u);
+    return make_float4(p[0], p[2], p[4], p[6]);
+}
+
 // Orders this thread's generic-proxy shared-memory accesses before later
 // async-proxy (bulk copy) writes to the same buffer.
 __device__ __forceinline__ void fence_proxy_async_smem()
@@ -119,9 +131,9 @@ __device__ __forceinline__ void fence_proxy_async_smem()
 // Shared memory of one warp.
 struct WarpArea {
     float4 buf[2][CHP];          // chunk buffers (bulk-copy destinations, 16-byte aligned)
-    uint2 slots[SLOTS][32];      // candidates {d2 bits, r << 30 | type << 24 | atom id of j}
+    float4 fa[4 * 32];           // first atoms of the pass {x, y, z, type << 24 | id}, q = 32 r + lane
+    unsigned short cq[CQ];       // candidate queue: q << 8 | record of the current chunk buffer
     uint4 q[QW];                 // FP64 recheck queue {ia, ja, channel, 0}
-    unsigned iv[4][32];          // type << 24 | atom id of the first atoms (R <= 4)
     int2 seg[2 * MAXROWS];       // sorted ranges of the neighbourhood rows (two halves each):
                                  // {begin | image << 25, end}
     uint64_t bar[2];             // one mbarrier per chunk buffer
@@ -144,9 +156,7 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                                                                         int win_cap, int hist_cap)
 {
     constexpr int NT = NWARP * 32;
-    // first atoms between two checks of the slot counts (one warp vote each)
-    constexpr int VG = R <= 3 ? R : 2;
-    static_assert(4 * VG <= SLOTS - 4, "slots for the candidates between two checks");
+    static_assert(32 * R <= 256, "a queue entry names a first atom in 8 bits");
     extern __shared__ __align__(128) unsigned char smem[];
     WarpArea *const areas = reinterpret_cast<WarpArea *>(smem);
     float2 *const win = reinterpret_cast<float2 *>(areas + NWARP);
@@ -159,6 +169,7 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
 
     const PairLaunch &P = C.pair;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned lt = (1u << lane) - 1u;  // the lanes below this one
     WarpArea &A = areas[warp];
     const int hlen = P.nch * P.nbin;
     unsigned *const whist = hist + (warp * HCOPY / NWARP) * hist_cap;  // this warp's copy
@@ -218,66 +229,67 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                           : ref_d2<false>(xi64[0], xi64[1], xi64[2], xj64[0], xj64[1], xj64[2],
                                           box, P.err);
         };
-        // Bins every slot of this warp's lanes (each lane its own, FLUSH_ILP
-        // per round), then empties them.
-        int cnt = 0;
-        auto flush_slots = [&]() {
-            const int maxc = __reduce_max_sync(0xffffffffu, (unsigned)cnt);
-            for (int q0 = 0; q0 < maxc; q0 += FLUSH_ILP) {
-                bool ok[FLUSH_ILP], need[FLUSH_ILP];
-                int ch[FLUSH_ILP], bi[FLUSH_ILP], ia[FLUSH_ILP], ja[FLUSH_ILP];
-#pragma unroll
-                for (int u = 0; u < FLUSH_ILP; ++u) {
-                    const bool v = q0 + u < cnt;
-                    // rows < SLOTS (q0 even, SLOTS even): load, then select
-                    const uint2 e = A.slots[q0 + u][lane];
-                    const float d2 = __uint_as_float(v ? e.x : 0x7f800000u);
-                    const unsigned meta = v ? e.y : 0u;
-                    const unsigned iv = A.iv[meta >> 30][lane];
-                    const int t_i = (int)(iv >> 24), t_j = (int)((meta >> 24) & 63u);
-                    ia[u] = (int)(iv & 0xffffffu);
-                    ja[u] = (int)(meta & 0xffffffu);
-                    ch[u] = chtab[t_i * P.ntypes + t_j] + (ia[u] == ja[u] ? half_ch : 0);
-                    const int b_ = __float2int_rd(
-                        __fmul_rn(__fsub_rn(sqrt_guess(d2), P.rmin_f), P.inv_dr_f));
-                    bi[u] = min(max(b_, 0), P.nbin - 1);
-                    const float2 w = win[bi[u]];
-                    const bool test = v && d2 >= P.lo_f;
-                    const bool inw = d2 >= w.x && d2 <= w.y;
-                    ok[u] = test && inw;
-                    need[u] = test && !inw;
-                }
-#pragma unroll
-                for (int u = 0; u < FLUSH_ILP; ++u)
-                    red_shared_add1_if(smem_u32(whist + ch[u] * P.nbin + bi[u]),
-                                       ok[u] && GOFR_CHECK(ch[u] >= 0 && ch[u] < P.nch &&
-                                                               bi[u] >= 0 && bi[u] < P.nbin,
-                                                           P.err));
-                bool any_need = false;
-#pragma unroll
-                for (int u = 0; u < FLUSH_ILP; ++u) any_need |= need[u];
-                if (__any_sync(0xffffffffu, any_need)) {
-#pragma unroll
-                    for (int u = 0; u < FLUSH_ILP; ++u) {
-                        if (!need[u]) continue;
-                        ++n_rech;
-                        const int slot = atomicAdd(&A.qn, 1);
-                        if (slot < QW) {
-                            A.q[slot] = make_uint4((unsigned)ia[u], (unsigned)ja[u],
-                                                   (unsigned)ch[u], 0u);
-                        } else {
-                            const double *xi64 = P.pos64 + (fo * P.N + ia[u]) * 3;
-                            const double *xj64 = P.pos64 + (fl * P.N + ja[u]) * 3;
-                            const double d2d = ref_d2_box(xi64, xj64, P.box64 + fo * 9);
-                            const int bb = ref_bin(d2d, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
-                            if (bb >= 0) atomicAdd(whist + ch[u] * P.nbin + bb, 1u);
-                        }
+        // Bins the warp's queued candidates 32 at a time.  An entry's FP32 d2
+        // is recomputed from the first atom and the chunk buffer's record
+        // with the pair loop's operations (one difference per axis, a
+        // multiply, two FMAs: the same value); pairs outside their bin's
+        // certified window are flagged per round and recomputed in FP64
+        // after the rounds.
+        int cn = 0;  // entries in the queue (the same in every lane)
+        auto flush_q = [&](const float4 *bufp) {
+            __syncwarp();  // every lane's entries and first atoms visible
+            unsigned needm = 0u;  // rounds whose entry of this lane goes to the recheck
+            for (int g0 = 0; g0 < cn; g0 += 32) {
+                const bool v = g0 + lane < cn;
+                const unsigned e = v ? (unsigned)A.cq[g0 + lane] : 0u;
+                const float4 fi = A.fa[e >> 8];
+                const float4 fj = unit_record(bufp, e & 0xffu);
+                const float dx = __fsub_rn(fi.x, fj.x), dy = __fsub_rn(fi.y, fj.y),
+                            dz = __fsub_rn(fi.z, fj.z);
+                float d2 = __fmul_rn(dx, dx);
+                d2 = __fmaf_rn(dy, dy, d2);
+                d2 = __fmaf_rn(dz, dz, d2);
+                const unsigned iv = __float_as_uint(fi.w), jv = __float_as_uint(fj.w);
+                const int ch = chtab[(int)(iv >> 24) * P.ntypes + (int)((jv >> 24) & 63u)] +
+                               (((iv ^ jv) & 0xffffffu) == 0u ? half_ch : 0);
+                const int b_ = __float2int_rd(
+                    __fmul_rn(__fsub_rn(sqrt_guess(d2), P.rmin_f), P.inv_dr_f));
+                const int bi = min(max(b_, 0), P.nbin - 1);
+                const float2 w = win[bi];
+                const bool test = v && d2 >= P.lo_f;
+                const bool inw = d2 >= w.x && d2 <= w.y;
+                red_shared_add1_if(smem_u32(whist + ch * P.nbin + bi),
+                                   test && inw &&
+                                       GOFR_CHECK(ch >= 0 && ch < P.nch && bi >= 0 && bi < P.nbin,
+                                                  P.err));
+                needm |= (test && !inw) ? 1u << (g0 >> 5) : 0u;
+            }
+            if (__any_sync(0xffffffffu, needm != 0u)) {
+                while (needm) {
+                    const int it = __ffs(needm) - 1;
+                    needm &= needm - 1u;
+                    const unsigned e = A.cq[it * 32 + lane];
+                    const unsigned iv = __float_as_uint(A.fa[e >> 8].w),
+                                   jv = __float_as_uint(unit_record(bufp, e & 0xffu).w);
+                    const int ia = (int)(iv & 0xffffffu), ja = (int)(jv & 0xffffffu);
+                    const int ch = chtab[(int)(iv >> 24) * P.ntypes + (int)((jv >> 24) & 63u)] +
+                                   (ia == ja ? half_ch : 0);
+                    ++n_rech;
+                    const int slot = atomicAdd(&A.qn, 1);
+                    if (slot < QW) {
+                        A.q[slot] = make_uint4((unsigned)ia, (unsigned)ja, (unsigned)ch, 0u);
+                    } else {
+                        const double *xi64 = P.pos64 + (fo * P.N + ia) * 3;
+                        const double *xj64 = P.pos64 + (fl * P.N + ja) * 3;
+                        const double d2d = ref_d2_box(xi64, xj64, P.box64 + fo * 9);
+                        const int bb = ref_bin(d2d, P.rmin, P.dr, P.rmin2, P.rmax2, P.nbin);
+                        if (bb >= 0) atomicAdd(whist + ch * P.nbin + bb, 1u);
                     }
                 }
             }
-            n_cand += cnt;
-            cnt = 0;
-            __syncwarp();
+            if (lane == 0) n_cand += (unsigned)cn;
+            cn = 0;
+            __syncwarp();  // every lane done with the entries before they are rewritten
         };
         // Recomputes the warp's queued pairs in exact FP64 (reference arithmetic).
         auto drain_queue = [&]() {
@@ -417,7 +429,7 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                     } else {
                         x = y = z = __int_as_float(0x7fc00000);
                     }
-                    A.iv[r][lane] = iv;
+                    A.fa[32 * r + lane] = make_float4(x, y, z, __uint_as_float(iv));
                     xi[r] = f2pk(x, x); yi[r] = f2pk(y, y); zi[r] = f2pk(z, z);
                 }
                 if (lane == 0) {
@@ -452,31 +464,35 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                     const int n = A.n[b];
                     const int code = A.code[b];
                     float4 *const bufp = A.buf[b];
-                    if (code != CELLW_SHIFT0) {  // image (0, 0, 0): nothing to move
-                        // a zero component adds exactly nothing (x + 0 = x)
-                        const float4 sh = s_shift[code];
-                        for (int e = lane; e < n; e += 32) {
-                            float4 v = bufp[e];
-                            v.x = __fadd_rn(v.x, sh.x);
-                            v.y = __fadd_rn(v.y, sh.y);
-                            v.z = __fadd_rn(v.z, sh.z);
-                            bufp[e] = v;
-                        }
-                    }
                     if (lane < ((n + 3) & ~3) - n)  // no atom: NaN never passes d2 <= hi_f
                         bufp[n + lane] = make_float4(__int_as_float(0x7fc00000),
                                                      __int_as_float(0x7fc00000),
                                                      __int_as_float(0x7fc00000),
                                                      __uint_as_float(0xffffffffu));
                     __syncwarp();
+                    // records moved to the chunk's image and interleaved in pairs, in
+                    // place: unit u (32 B) = {x0, x1, y0, y1, z0, z1, w0, w1} of records
+                    // 2u and 2u + 1, so each coordinate pair loads as one f32x2 operand
+                    // (image (0, 0, 0) adds zeros: x + 0 = x)
+                    {
+                        const float4 sh = s_shift[code];
+                        const int nu = ((n + 3) & ~3) >> 1;
+                        for (int u = lane; u < nu; u += 32) {
+                            const float4 r0 = bufp[2 * u], r1 = bufp[2 * u + 1];
+                            bufp[2 * u] = make_float4(__fadd_rn(r0.x, sh.x), __fadd_rn(r1.x, sh.x),
+                                                      __fadd_rn(r0.y, sh.y), __fadd_rn(r1.y, sh.y));
+                            bufp[2 * u + 1] = make_float4(__fadd_rn(r0.z, sh.z),
+                                                          __fadd_rn(r1.z, sh.z), r0.w, r1.w);
+                        }
+                    }
+                    __syncwarp();
+                    const ulonglong2 *const bq = reinterpret_cast<const ulonglong2 *>(bufp);
 
                     for (int jj = 0; jj < n; jj += 4) {
-                        const float4 a0 = bufp[jj], a1 = bufp[jj + 1], a2 = bufp[jj + 2],
-                                     a3 = bufp[jj + 3];
-                        const f2 xa = f2pk(a0.x, a1.x), ya = f2pk(a0.y, a1.y), za = f2pk(a0.z, a1.z);
-                        const f2 xb = f2pk(a2.x, a3.x), yb = f2pk(a2.y, a3.y), zb = f2pk(a2.z, a3.z);
-                        const unsigned m0 = __float_as_uint(a0.w), m1 = __float_as_uint(a1.w),
-                                       m2 = __float_as_uint(a2.w), m3 = __float_as_uint(a3.w);
+                        // units jj / 2 and jj / 2 + 1: {x, y} pairs, then {z, w} pairs
+                        const ulonglong2 ua = bq[jj], ub = bq[jj + 2];
+                        const f2 xa = ua.x, ya = ua.y, za = bq[jj + 1].x;
+                        const f2 xb = ub.x, yb = ub.y, zb = bq[jj + 3].x;
 #pragma unroll
                         for (int r = 0; r < R; ++r) {
                             const f2 da = pair2s(xi[r], yi[r], zi[r], xa, ya, za);
@@ -484,24 +500,33 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                             float d0, d1, d2v, d3;
                             f2up(da, d0, d1);
                             f2up(db, d2v, d3);
-                            const unsigned rm = (unsigned)r << 30;
-                            if (d0 <= hi_f) { A.slots[cnt][lane] = make_uint2(__float_as_uint(d0), m0 | rm); ++cnt; }
-                            if (d1 <= hi_f) { A.slots[cnt][lane] = make_uint2(__float_as_uint(d1), m1 | rm); ++cnt; }
-                            if (d2v <= hi_f) { A.slots[cnt][lane] = make_uint2(__float_as_uint(d2v), m2 | rm); ++cnt; }
-                            if (d3 <= hi_f) { A.slots[cnt][lane] = make_uint2(__float_as_uint(d3), m3 | rm); ++cnt; }
-                            if (!GOFR_CHECK(cnt <= SLOTS, P.err)) cnt = SLOTS;
-                            // room for the next VG first atoms' four candidates each
-                            if ((r + 1) % VG == 0 || r == R - 1)
-                                if (__any_sync(0xffffffffu, cnt > SLOTS - 4 * VG)) flush_slots();
+                            // entries q << 8 | record, compacted by one ballot per record
+                            const unsigned eb = ((unsigned)(32 * r) + (unsigned)lane) << 8 | (unsigned)jj;
+                            const bool p0 = d0 <= hi_f, p1 = d1 <= hi_f, p2 = d2v <= hi_f,
+                                       p3 = d3 <= hi_f;
+                            const unsigned b0 = __ballot_sync(0xffffffffu, p0),
+                                           b1 = __ballot_sync(0xffffffffu, p1),
+                                           b2 = __ballot_sync(0xffffffffu, p2),
+                                           b3 = __ballot_sync(0xffffffffu, p3);
+                            const int c1 = cn + __popc(b0), c2 = c1 + __popc(b1),
+                                      c3 = c2 + __popc(b2);
+                            if (p0) A.cq[cn + __popc(b0 & lt)] = (unsigned short)eb;
+                            if (p1) A.cq[c1 + __popc(b1 & lt)] = (unsigned short)(eb + 1u);
+                            if (p2) A.cq[c2 + __popc(b2 & lt)] = (unsigned short)(eb + 2u);
+                            if (p3) A.cq[c3 + __popc(b3 & lt)] = (unsigned short)(eb + 3u);
+                            cn = c3 + __popc(b3);
+                            if (!GOFR_CHECK(cn <= CQ, P.err)) cn = CQ;
+                            // room for the next group's entries
+                            if (cn > CQ - CQ_ROOM) flush_q(bufp);
                         }
                     }
+                    // the entries name records of this buffer: bin them before it is refilled
+                    if (cn > 0) flush_q(bufp);
                     fence_proxy_async_smem();
                     __syncwarp();  // every lane done with buffer b
                     if (b) have1 = issue(w, 1);
                     else have0 = issue(w, 0);
                 }
-                // the slots refer to this pass's first atoms
-                if (__any_sync(0xffffffffu, cnt > 0)) flush_slots();
                 if (A.qn > QW / 2) drain_queue();
             }
         }
