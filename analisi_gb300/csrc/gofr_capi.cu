@@ -1024,12 +1024,13 @@ struct CellwCand {
 };
 
 // Every configuration, cheapest first.  The cost counts, over all warp
-// blocks, the first-atom lane slots a block pays for (its atoms with room for
-// two standard deviations of density fluctuation, rounded up to passes of
-// 32 r) times its neighbourhood's atoms, plus a fixed overhead per staged
-// chunk (a row of the neighbourhood, in one or two pieces), relative to N^2.
-// Triclinic neighbourhoods take the widest row and cell ranges of their
-// geometry (one more than the orthorhombic 2 reach where a tilt shifts them).
+// blocks, the block's first atoms times the record slots of its
+// neighbourhood's chunks (rows packed 128 records to a chunk, at most 8
+// pieces each, so short rows fill chunks less), plus a fixed overhead per
+// chunk streamed (one per batch of 64 first atoms; atoms with room for two
+// standard deviations of density fluctuation), relative to N^2.  Triclinic
+// neighbourhoods take the widest row and cell ranges of their geometry (one
+// more than the orthorhombic 2 reach where a tilt shifts them).
 std::vector<CellwCand> cellw_candidates(const TrajDev &t, const gofr_params &p)
 {
     std::vector<CellwCand> all;
@@ -1058,23 +1059,26 @@ std::vector<CellwCand> cellw_candidates(const TrajDev &t, const gofr_params &p)
                     const double nbhd = rows * row_atoms;
                     const double blocks = (double)((nc[0] + wx - 1) / wx) *
                                           ((nc[1] + wy - 1) / wy) * ((nc[2] + wz - 1) / wz);
-                    for (int r = 2; r <= 4; ++r) {
-                        const int TI = cellw_warp_atoms(r);
-                        const double passes =
-                            std::ceil(std::max(atoms + 2.0 * std::sqrt(atoms), 1.0) / TI);
-                        // a chunk costs about 24 neighbour records of work beyond its own
-                        const double chunks =
-                            rows * (1.0 + std::floor(row_atoms / 128.0)) + 0.3 * rows;
-                        CellwCand c;
-                        c.reach = m;
-                        c.r = r;
-                        for (int k = 0; k < 3; ++k) c.nc[k] = nc[k];
-                        c.w = {{wx, wy, wz}};
-                        c.fraction = rows * (wx + g.nx_span) / ncell;
-                        c.cost = blocks * passes * TI * (nbhd + 24.0 * chunks) /
-                                 ((double)t.N * t.N);
-                        all.push_back(c);
-                    }
+                    const double chr = cellw_chunk_records();
+                    // a row wrapping the box is two pieces
+                    const double pieces_per_row = 1.0 + (double)(wx + g.nx_span) / nc[0];
+                    const double per_chunk =
+                        std::min(chr, cellw_chunk_pieces() * row_atoms / pieces_per_row);
+                    const double chunks = std::ceil(nbhd / per_chunk) + 0.5;
+                    const double batches =
+                        std::ceil(std::max(atoms + 2.0 * std::sqrt(atoms), 1.0) /
+                                  cellw_batch_atoms());
+                    // a chunk's fixed work (wait, image moves, padding, the last
+                    // flush) is about that of six first atoms against its records
+                    CellwCand c;
+                    c.reach = m;
+                    c.r = 4;
+                    for (int k = 0; k < 3; ++k) c.nc[k] = nc[k];
+                    c.w = {{wx, wy, wz}};
+                    c.fraction = rows * (wx + g.nx_span) / ncell;
+                    c.cost = blocks * (atoms + 6.0 * batches) * chunks * chr /
+                             ((double)t.N * t.N);
+                    all.push_back(c);
                 }
     }
     std::stable_sort(all.begin(), all.end(),

@@ -5,10 +5,18 @@
 // (gofr_cells.cu), the atoms of every frame are binned into cells of edge
 // >= rmax / reach and sorted by cell, so a pair the reference counts lies in
 // cells at most `reach` apart on every axis; here the unit of neighbourhood
-// is much smaller: each WARP owns a small block of cells (a few cells, about
-// 32 R first atoms) and streams only that block's own neighbourhood, so the
-// pairs evaluated per first atom shrink from the neighbourhood of a CTA-sized
-// block to the neighbourhood of a warp-sized one.
+// is much smaller: each WARP owns a small block of cells and streams only
+// that block's own neighbourhood, so the pairs evaluated per first atom
+// shrink from the neighbourhood of a CTA-sized block to the neighbourhood of
+// a warp-sized one.
+//
+// Lanes hold neighbours, not first atoms: a chunk buffer holds 128 records
+// of the neighbourhood (rows packed back to back, several per chunk when
+// they are short), each lane keeps four of them in registers as f32x2 pairs,
+// and the warp walks the block's first atoms one at a time, each broadcast
+// from shared memory, so no lane idles for want of a first atom whatever the
+// block's atom count (only the last chunk of a neighbourhood is partly
+// padding).
 //
 // Layout per frame (built once per upload and grid): records
 // {x, y, z, type << 24 | atom id} (float4, the coordinates wrapped into the
@@ -16,8 +24,9 @@
 // kernel's), sorted by cell, x fastest; cell start offsets.  A row of cells
 // of a neighbourhood is one contiguous run of 16-byte records, so a warp
 // stages it into shared memory with one 1-D bulk copy (TMA, cp.async.bulk)
-// per chunk of CH records, two chunk buffers per warp, completion tracked by
-// one mbarrier per buffer.  Cells reached across the box boundary are the
+// per piece (a row's run of records, or the part of it that fits), up to
+// MAXP pieces and CH records per chunk, two chunk buffers per warp,
+// completion tracked by one mbarrier per buffer.  Cells reached across the box boundary are the
 // periodic image of the cell: after the copy lands, the warp moves the
 // chunk's records to that image (x += fl32 of the lattice vector, one FP32
 // rounding per axis; orthorhombic: s fl32(L), the block kernel's
@@ -59,13 +68,15 @@
 namespace gofr {
 namespace cellw {
 
-constexpr int CH = 128;        // neighbour records per chunk buffer
-constexpr int CHP = CH + 4;    // + room for NaN records padding a chunk to a multiple of 4
+constexpr int CH = 128;        // neighbour records per chunk buffer: 4 per lane
+constexpr int MAXP = 8;        // pieces (bulk copies) per chunk
+constexpr int FA = 64;         // first atoms per batch
 constexpr int CQ = 512;        // candidate queue entries of a warp
 constexpr int CQ_ROOM = 4 * 32; // entries one first-atom group of one step can add
 constexpr int QW = 32;         // FP64 recheck queue of a warp
 constexpr int MAXROWS = CELLW_MAX_ROWS;  // neighbourhood rows of a warp block
-static_assert(CH + 4 <= 256, "a queue entry names a record of the chunk buffer in 8 bits");
+static_assert(CH == 4 * 32, "four records per lane");
+static_assert(CH <= 256 && FA <= 256, "a queue entry names a first atom and a record in 8 bits each");
 
 typedef unsigned long long f2;
 __device__ __forceinline__ f2 f2pk(float a, float b)
@@ -113,14 +124,6 @@ __device__ __forceinline__ int floordiv(int a, int n) { return a >= 0 ? a / n : 
 
 constexpr unsigned SEG_BEGIN = 0x1ffffffu;  // a segment's begin; its image index above bit 25
 
-// Record k of a chunk buffer whose records are interleaved in pairs (unit
-// k / 2 = {x0, x1, y0, y1, z0, z1, w0, w1}).
-__device__ __forceinline__ float4 unit_record(const float4 *buf, unsigned k)
-{
-    const float *p = reinterpret_cast<const float *>(buf) + (k >> 1) * 8 + (k & 1u);
-    return make_float4(p[0], p[2], p[4], p[6]);
-}
-
 // Orders this thread's generic-proxy shared-memory accesses before later
 // async-proxy (bulk copy) writes to the same buffer.
 __device__ __forceinline__ void fence_proxy_async_smem()
@@ -130,15 +133,17 @@ __device__ __forceinline__ void fence_proxy_async_smem()
 
 // Shared memory of one warp.
 struct WarpArea {
-    float4 buf[2][CHP];          // chunk buffers (bulk-copy destinations, 16-byte aligned)
-    float4 fa[4 * 32];           // first atoms of the pass {x, y, z, type << 24 | id}, q = 32 r + lane
-    unsigned short cq[CQ];       // candidate queue: q << 8 | record of the current chunk buffer
+    float4 buf[2][CH];           // chunk buffers (bulk-copy destinations, 16-byte aligned)
+    ulonglong2 fa[2 * FA];       // first atoms of the batch as f32x2 pairs:
+                                 // {(x, x), (y, y)}, {(z, z), (w, w)}, w = type << 24 | id
+    unsigned short cq[CQ];       // candidate queue: first atom << 8 | record of the current chunk
     uint4 q[QW];                 // FP64 recheck queue {ia, ja, channel, 0}
     int2 seg[2 * MAXROWS];       // sorted ranges of the neighbourhood rows (two halves each):
                                  // {begin | image << 25, end}
+    int4 pc[2][MAXP];            // pieces of each buffer {first record, source record, count, image}
     uint64_t bar[2];             // one mbarrier per chunk buffer
     int n[2];                    // records in each buffer
-    int code[2];                 // image of each buffer's records
+    int np[2];                   // pieces in each buffer
     int qn;                      // entries in q
     int pad[3];
 };
@@ -151,12 +156,11 @@ struct Walk {
 // NWARP warps per CTA (8: two CTAs per SM, 16: one), HCOPY copies of the
 // shared histogram (warp w adds to copy w HCOPY / NWARP: the privatisation
 // depth, fewer warps contending for each bin).
-template <int R, int NWARP, int HCOPY>
+template <int NWARP, int HCOPY>
 __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const CellwLaunch C,
                                                                         int win_cap, int hist_cap)
 {
     constexpr int NT = NWARP * 32;
-    static_assert(32 * R <= 256, "a queue entry names a first atom in 8 bits");
     extern __shared__ __align__(128) unsigned char smem[];
     WarpArea *const areas = reinterpret_cast<WarpArea *>(smem);
     float2 *const win = reinterpret_cast<float2 *>(areas + NWARP);
@@ -242,8 +246,9 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
             for (int g0 = 0; g0 < cn; g0 += 32) {
                 const bool v = g0 + lane < cn;
                 const unsigned e = v ? (unsigned)A.cq[g0 + lane] : 0u;
-                const float4 fi = A.fa[e >> 8];
-                const float4 fj = unit_record(bufp, e & 0xffu);
+                const float *const fp = reinterpret_cast<const float *>(A.fa) + 8 * (e >> 8);
+                const float4 fi = make_float4(fp[0], fp[2], fp[4], fp[6]);
+                const float4 fj = bufp[e & 0xffu];
                 const float dx = __fsub_rn(fi.x, fj.x), dy = __fsub_rn(fi.y, fj.y),
                             dz = __fsub_rn(fi.z, fj.z);
                 float d2 = __fmul_rn(dx, dx);
@@ -269,8 +274,9 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                     const int it = __ffs(needm) - 1;
                     needm &= needm - 1u;
                     const unsigned e = A.cq[it * 32 + lane];
-                    const unsigned iv = __float_as_uint(A.fa[e >> 8].w),
-                                   jv = __float_as_uint(unit_record(bufp, e & 0xffu).w);
+                    const unsigned iv =
+                                       __float_as_uint(reinterpret_cast<const float *>(A.fa)[8 * (e >> 8) + 6]),
+                                   jv = __float_as_uint(bufp[e & 0xffu].w);
                     const int ia = (int)(iv & 0xffffffu), ja = (int)(jv & 0xffffffu);
                     const int ch = chtab[(int)(iv >> 24) * P.ntypes + (int)((jv >> 24) & 63u)] +
                                    (ia == ja ? half_ch : 0);
@@ -382,64 +388,68 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
             for (int s = lane; s < 2 * nrows; s += 32)
                 n_j += A.seg[s].y - (int)((unsigned)A.seg[s].x & SEG_BEGIN);
             n_j = __reduce_add_sync(0xffffffffu, n_j);
-            // Advances w to the next non-empty piece and (lane 0) copies it into
-            // buffer b; returns false at the end of the neighbourhood.
+            // Fills buffer b with the next records of the neighbourhood: up to CH
+            // records from up to MAXP pieces (every lane walks the segments
+            // alike); lane 0 then expects their bytes on the buffer's mbarrier
+            // and issues one bulk copy per piece.  False at the end of the
+            // neighbourhood (nothing issued).
             auto issue = [&](Walk &w, int b) -> bool {
-                while (w.row < nrows) {
+                int filled = 0, np = 0;
+                while (w.row < nrows && filled < CH && np < MAXP) {
                     const int2 sg = A.seg[2 * w.row + w.half];
                     const int beg = (int)((unsigned)sg.x & SEG_BEGIN);
                     const int len = sg.y - beg;
                     if (w.off < len) {
-                        const int n = min(CH, len - w.off);
-                        if (lane == 0) {
-                            A.n[b] = n;
-                            A.code[b] = (int)((unsigned)sg.x >> 25);
-                            mbar_arrive_expect_tx(&A.bar[b], (unsigned)(n * 16));
-                            bulk_g2s(&A.buf[b][0], rec_l + beg + w.off, (unsigned)(n * 16),
-                                     &A.bar[b]);
-                        }
+                        const int n = min(CH - filled, len - w.off);
+                        if (lane == 0)
+                            A.pc[b][np] = make_int4(filled, beg + w.off, n,
+                                                    (int)((unsigned)sg.x >> 25));
+                        ++np;
+                        filled += n;
                         w.off += n;
-                        return true;
+                        continue;
                     }
                     w.off = 0;
                     if (++w.half == 2) { w.half = 0; ++w.row; }
                 }
-                return false;
+                if (filled == 0) return false;
+                if (lane == 0) {
+                    A.n[b] = filled;
+                    A.np[b] = np;
+                    mbar_arrive_expect_tx(&A.bar[b], (unsigned)(filled * 16));
+                    for (int p = 0; p < np; ++p) {
+                        const int4 pc = A.pc[b][p];
+                        bulk_g2s(&A.buf[b][pc.x], rec_l + pc.y, (unsigned)(pc.z * 16), &A.bar[b]);
+                    }
+                }
+                return true;
             };
 
-            for (int ibase = 0; ibase < n_i && !dead; ibase += 32 * R) {
-                // first atoms: r-group r holds atoms ibase + 32 r + lane
-                f2 xi[R], yi[R], zi[R];
-#pragma unroll
-                for (int r = 0; r < R; ++r) {
-                    const int q = ibase + 32 * r + lane;
-                    // row of atom q (every lane takes part in the shuffles)
-                    const int qq = min(q, n_i - 1);
+            for (int ibase = 0; ibase < n_i && !dead; ibase += FA) {
+                // first atoms ibase .. ibase + na - 1 of the block, as f32x2 pairs
+                const int na = min(FA, n_i - ibase);
+                for (int q0 = 0; q0 < na; q0 += 32) {
+                    const int q = q0 + lane;
+                    // row of atom ibase + q (every lane takes part in the shuffles)
+                    const int qq = min(ibase + q, n_i - 1);
                     int row = 0;
                     for (int rr = 0; rr < nir; ++rr)
                         row += (qq >= __shfl_sync(0xffffffffu, ipre, rr)) ? 1 : 0;
                     const int rb = __shfl_sync(0xffffffffu, ib, row);
                     const int rp = __shfl_sync(0xffffffffu, ipre - ilen, row);
-                    float x, y, z;
-                    unsigned iv = 0x00ffffffu;  // type 0, no atom
-                    if (q < n_i) {
-                        const float4 v = rec_o[rb + (q - rp)];
-                        x = v.x; y = v.y; z = v.z;
-                        iv = __float_as_uint(v.w);
-                    } else {
-                        x = y = z = __int_as_float(0x7fc00000);
+                    if (q < na) {
+                        const float4 v = rec_o[rb + (qq - rp)];
+                        A.fa[2 * q] = make_ulonglong2(f2pk(v.x, v.x), f2pk(v.y, v.y));
+                        A.fa[2 * q + 1] = make_ulonglong2(f2pk(v.z, v.z), f2pk(v.w, v.w));
                     }
-                    A.fa[32 * r + lane] = make_float4(x, y, z, __uint_as_float(iv));
-                    xi[r] = f2pk(x, x); yi[r] = f2pk(y, y); zi[r] = f2pk(z, z);
                 }
                 if (lane == 0) {
-                    const unsigned long long pe =
-                        (unsigned long long)min(32 * R, n_i - ibase) * (unsigned long long)n_j;
+                    const unsigned long long pe = (unsigned long long)na * (unsigned long long)n_j;
                     n_eval += pe;
                     atomicAdd(&s_pairs, pe);
                 }
-                // earlier generic accesses of both buffers (image moves, NaN
-                // tails, reads) before the bulk copies that refill them
+                // earlier generic accesses of both buffers (records moved to their
+                // image, padding, reads) before the bulk copies that refill them
                 fence_proxy_async_smem();
                 __syncwarp();
                 Walk w{0, 0, 0};
@@ -461,64 +471,64 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                         break;
                     }
                     if (b) ph1 ^= 1u; else ph0 ^= 1u;
-                    const int n = A.n[b];
-                    const int code = A.code[b];
+                    const int n = A.n[b], np = A.np[b];
                     float4 *const bufp = A.buf[b];
-                    if (lane < ((n + 3) & ~3) - n)  // no atom: NaN never passes d2 <= hi_f
-                        bufp[n + lane] = make_float4(__int_as_float(0x7fc00000),
-                                                     __int_as_float(0x7fc00000),
-                                                     __int_as_float(0x7fc00000),
-                                                     __uint_as_float(0xffffffffu));
-                    __syncwarp();
-                    // records moved to the chunk's image and interleaved in pairs, in
-                    // place: unit u (32 B) = {x0, x1, y0, y1, z0, z1, w0, w1} of records
-                    // 2u and 2u + 1, so each coordinate pair loads as one f32x2 operand
-                    // (image (0, 0, 0) adds zeros: x + 0 = x)
-                    {
-                        const float4 sh = s_shift[code];
-                        const int nu = ((n + 3) & ~3) >> 1;
-                        for (int u = lane; u < nu; u += 32) {
-                            const float4 r0 = bufp[2 * u], r1 = bufp[2 * u + 1];
-                            bufp[2 * u] = make_float4(__fadd_rn(r0.x, sh.x), __fadd_rn(r1.x, sh.x),
-                                                      __fadd_rn(r0.y, sh.y), __fadd_rn(r1.y, sh.y));
-                            bufp[2 * u + 1] = make_float4(__fadd_rn(r0.z, sh.z),
-                                                          __fadd_rn(r1.z, sh.z), r0.w, r1.w);
-                        }
-                    }
-                    __syncwarp();
-                    const ulonglong2 *const bq = reinterpret_cast<const ulonglong2 *>(bufp);
-
-                    for (int jj = 0; jj < n; jj += 4) {
-                        // units jj / 2 and jj / 2 + 1: {x, y} pairs, then {z, w} pairs
-                        const ulonglong2 ua = bq[jj], ub = bq[jj + 2];
-                        const f2 xa = ua.x, ya = ua.y, za = bq[jj + 1].x;
-                        const f2 xb = ub.x, yb = ub.y, zb = bq[jj + 3].x;
+                    // this lane's records 4 lane + t: moved to their piece's image
+                    // (image (0, 0, 0) adds zeros: x + 0 = x) and written back for
+                    // the binning; records past n are NaN (never a candidate)
+                    float rx[4], ry[4], rz[4];
 #pragma unroll
-                        for (int r = 0; r < R; ++r) {
-                            const f2 da = pair2s(xi[r], yi[r], zi[r], xa, ya, za);
-                            const f2 db = pair2s(xi[r], yi[r], zi[r], xb, yb, zb);
-                            float d0, d1, d2v, d3;
-                            f2up(da, d0, d1);
-                            f2up(db, d2v, d3);
-                            // entries q << 8 | record, compacted by one ballot per record
-                            const unsigned eb = ((unsigned)(32 * r) + (unsigned)lane) << 8 | (unsigned)jj;
-                            const bool p0 = d0 <= hi_f, p1 = d1 <= hi_f, p2 = d2v <= hi_f,
-                                       p3 = d3 <= hi_f;
-                            const unsigned b0 = __ballot_sync(0xffffffffu, p0),
-                                           b1 = __ballot_sync(0xffffffffu, p1),
-                                           b2 = __ballot_sync(0xffffffffu, p2),
-                                           b3 = __ballot_sync(0xffffffffu, p3);
-                            const int c1 = cn + __popc(b0), c2 = c1 + __popc(b1),
-                                      c3 = c2 + __popc(b2);
-                            if (p0) A.cq[cn + __popc(b0 & lt)] = (unsigned short)eb;
-                            if (p1) A.cq[c1 + __popc(b1 & lt)] = (unsigned short)(eb + 1u);
-                            if (p2) A.cq[c2 + __popc(b2 & lt)] = (unsigned short)(eb + 2u);
-                            if (p3) A.cq[c3 + __popc(b3 & lt)] = (unsigned short)(eb + 3u);
-                            cn = c3 + __popc(b3);
-                            if (!GOFR_CHECK(cn <= CQ, P.err)) cn = CQ;
-                            // room for the next group's entries
-                            if (cn > CQ - CQ_ROOM) flush_q(bufp);
+                    for (int t = 0; t < 4; ++t) {
+                        const int k = 4 * lane + t;
+                        float4 v = make_float4(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000),
+                                               __int_as_float(0x7fc00000),
+                                               __uint_as_float(0xffffffffu));
+                        if (k < n) {
+                            int code = A.pc[b][0].w;
+                            for (int p = 1; p < np; ++p) {
+                                const int4 pc = A.pc[b][p];
+                                if (pc.x <= k) code = pc.w;
+                            }
+                            const float4 sh = s_shift[code];
+                            v = bufp[k];
+                            v.x = __fadd_rn(v.x, sh.x);
+                            v.y = __fadd_rn(v.y, sh.y);
+                            v.z = __fadd_rn(v.z, sh.z);
                         }
+                        bufp[k] = v;
+                        rx[t] = v.x; ry[t] = v.y; rz[t] = v.z;
+                    }
+                    const f2 xa = f2pk(rx[0], rx[1]), ya = f2pk(ry[0], ry[1]), za = f2pk(rz[0], rz[1]);
+                    const f2 xb = f2pk(rx[2], rx[3]), yb = f2pk(ry[2], ry[3]), zb = f2pk(rz[2], rz[3]);
+                    __syncwarp();
+                    const unsigned eb0 = (unsigned)(4 * lane);
+                    for (int i = 0; i < na; ++i) {
+                        // first atom i (broadcast) against this lane's four records
+                        const ulonglong2 fxy = A.fa[2 * i];
+                        const f2 fz = A.fa[2 * i + 1].x;
+                        const f2 da = pair2s(fxy.x, fxy.y, fz, xa, ya, za);
+                        const f2 db = pair2s(fxy.x, fxy.y, fz, xb, yb, zb);
+                        float d0, d1, d2v, d3;
+                        f2up(da, d0, d1);
+                        f2up(db, d2v, d3);
+                        // entries i << 8 | record, compacted by one ballot per record slot
+                        const unsigned eb = (unsigned)i << 8 | eb0;
+                        const bool p0 = d0 <= hi_f, p1 = d1 <= hi_f, p2 = d2v <= hi_f,
+                                   p3 = d3 <= hi_f;
+                        const unsigned b0 = __ballot_sync(0xffffffffu, p0),
+                                       b1 = __ballot_sync(0xffffffffu, p1),
+                                       b2 = __ballot_sync(0xffffffffu, p2),
+                                       b3 = __ballot_sync(0xffffffffu, p3);
+                        const int c1 = cn + __popc(b0), c2 = c1 + __popc(b1),
+                                  c3 = c2 + __popc(b2);
+                        if (p0) A.cq[cn + __popc(b0 & lt)] = (unsigned short)eb;
+                        if (p1) A.cq[c1 + __popc(b1 & lt)] = (unsigned short)(eb + 1u);
+                        if (p2) A.cq[c2 + __popc(b2 & lt)] = (unsigned short)(eb + 2u);
+                        if (p3) A.cq[c3 + __popc(b3 & lt)] = (unsigned short)(eb + 3u);
+                        cn = c3 + __popc(b3);
+                        if (!GOFR_CHECK(cn <= CQ, P.err)) cn = CQ;
+                        // room for the next first atom's entries
+                        if (cn > CQ - CQ_ROOM) flush_q(bufp);
                     }
                     // the entries name records of this buffer: bin them before it is refilled
                     if (cn > 0) flush_q(bufp);
@@ -576,7 +586,9 @@ int cellw_smem_bytes(int nch, int nbin, int ntypes, int cta_warps, int hcopy)
     return (int)((b + 127) / 128 * 128);
 }
 
-int cellw_warp_atoms(int r) { return 32 * r; }
+int cellw_chunk_records() { return cellw::CH; }
+int cellw_batch_atoms() { return cellw::FA; }
+int cellw_chunk_pieces() { return cellw::MAXP; }
 
 // Sorted AoS copy of every frame: {x, y, z, type << 24 | id} with the block
 // kernel's coordinates (w = x - n L, n = floor((x - xlo) / L), one FMA in
@@ -637,12 +649,12 @@ int launch_cell_scatter_w(const double *pos64, const unsigned char *types8, size
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
 }
 
-template <int R, int NWARP, int HCOPY>
-static int launch_cellw_r(const CellwLaunch &C, int num_sms, cudaStream_t s)
+template <int NWARP, int HCOPY>
+static int launch_cellw_shape(const CellwLaunch &C, int num_sms, cudaStream_t s)
 {
     using namespace cellw;
     constexpr int NT = NWARP * 32;
-    auto kern = k_pairs_cellw<R, NWARP, HCOPY>;
+    auto kern = k_pairs_cellw<NWARP, HCOPY>;
     const int smem = cellw_smem_bytes(C.pair.nch, C.pair.nbin, C.pair.ntypes, NWARP, HCOPY);
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
         cudaSuccess)
@@ -655,17 +667,6 @@ static int launch_cellw_r(const CellwLaunch &C, int num_sms, cudaStream_t s)
     if (grid > C.pair.n_items) grid = C.pair.n_items;
     kern<<<(unsigned)grid, NT, smem, s>>>(C, C.pair.nbin, C.pair.nch * C.pair.nbin);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;
-}
-
-template <int NWARP, int HCOPY>
-static int launch_cellw_shape(const CellwLaunch &C, int num_sms, cudaStream_t s)
-{
-    switch (C.r) {
-    case 2: return launch_cellw_r<2, NWARP, HCOPY>(C, num_sms, s);
-    case 3: return launch_cellw_r<3, NWARP, HCOPY>(C, num_sms, s);
-    case 4: return launch_cellw_r<4, NWARP, HCOPY>(C, num_sms, s);
-    default: return -3;
-    }
 }
 
 int launch_cellw_pairs(const CellwLaunch &C, int num_sms, cudaStream_t s)

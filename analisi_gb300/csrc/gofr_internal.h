@@ -119,7 +119,7 @@ struct CellwLaunch {
     int w[3];                      // cells per warp block per axis
     int nw[3];                     // warp blocks per axis
     int reach;                     // neighbour cells per side
-    int r;                         // first atoms per lane (2, 3 or 4)
+    int r;                         // records per lane (4; kept in plans and tuner keys)
     int parts;                     // parts of the warp blocks per (lag, origin)
     int cta_warps;                 // warps per CTA: 8 (two CTAs per SM) or 16 (one)
     int hcopy;                     // copies of the shared histogram (privatisation depth: 1, 2)
@@ -130,7 +130,9 @@ struct CellwLaunch {
     float4 shift[CELLW_NSHIFT];    // FP32 lattice vector {x, y, z, 0} of each image
 };
 int cellw_smem_bytes(int nch, int nbin, int ntypes, int cta_warps = 8, int hcopy = 1);
-int cellw_warp_atoms(int r);
+int cellw_chunk_records();  // neighbour records per chunk (4 per lane)
+int cellw_batch_atoms();    // first atoms per batch (each batch streams the neighbourhood)
+int cellw_chunk_pieces();   // bulk copies per chunk at most
 // box_internal {xlo, ylo, zlo, lx/2, ly/2, lz/2, xy, xz, yz}; tric: the
 // coordinates are reduced into the axis-aligned cell by the lattice (z, then
 // y, then x), else per axis.

@@ -1,8 +1,8 @@
 """Warp-streamed cell-list kernel (GOFR_KERNEL_CELL_WARP): each warp streams
 the neighbourhood of its own small block of cells through 1-D bulk copies.
-Counts must equal the oracle's for every configuration: reach 1, 2 and 3, 2
-to 4 first atoms per lane, warp blocks whose neighbourhood wraps the box on
-every axis, several passes of first atoms per block, shifted and non-cubic
+Counts must equal the oracle's for every configuration: reach 1, 2 and 3,
+warp blocks whose neighbourhood wraps the box on every axis, several batches
+of first atoms per block, chunks packed from several rows, shifted and non-cubic
 boxes, unwrapped coordinates far outside the box, and thousands of FP64
 rechecks (a warp's recheck queue overflowing)."""
 import numpy as np
@@ -31,8 +31,10 @@ def _ref(oracle_mod, w):
 
 
 # "reach,r,wx,wy,wz" through ANALISI_GB300_CELLW_PLAN (None: the planner's
-# choice); (1,2,1,1,1) with few first atoms per lane makes several passes
-PLANS = [None, "1,2,1,1,1", "1,4,2,2,1", "2,3,1,2,2", "2,2,3,1,1", "2,4,2,2,2", "3,3,2,2,2"]
+# choice; r is the 4 records a lane holds); blocks of 2 x 2 x 1 and 2 x 2 x 2
+# cells of reach 1 hold more than one batch of 64 first atoms
+PLANS = [None, "1,4,1,1,1", "1,4,2,2,1", "2,4,1,2,2", "2,4,3,1,1", "2,4,2,2,2", "3,4,2,2,2",
+         "1,4,2,2,2"]
 
 
 @pytest.mark.parametrize("plan", PLANS, ids=[str(p) for p in PLANS])
@@ -55,7 +57,7 @@ def test_cellw_matches_oracle(gpu_engine, oracle_mod, case, plan, monkeypatch):
     np.testing.assert_array_equal(got, ref)
 
 
-@pytest.mark.parametrize("plan", [None, "1,3,1,1,1", "2,2,2,1,2"])
+@pytest.mark.parametrize("plan", [None, "1,4,1,1,1", "2,4,2,1,2"])
 def test_cellw_far_unwrapped_coordinates(gpu_engine, oracle_mod, plan, monkeypatch):
     """Atoms several box lengths outside a box that is not at the origin."""
     if plan is None:
@@ -77,7 +79,7 @@ def test_cellw_far_unwrapped_coordinates(gpu_engine, oracle_mod, plan, monkeypat
     np.testing.assert_array_equal(got, ref)
 
 
-@pytest.mark.parametrize("plan", ["2,3,2,2,2", "1,4,1,1,1"])
+@pytest.mark.parametrize("plan", ["2,4,2,2,2", "1,4,1,1,1"])
 def test_cellw_many_rechecks(gpu_engine, oracle_mod, plan, monkeypatch):
     """Copies of every atom on bin thresholds: thousands of FP64 rechecks per
     item, far more than a warp's queue holds between drains."""
@@ -182,7 +184,7 @@ def test_every_cta_size_and_histogram_depth_is_exact(built_engine, oracle_mod, t
     # the warp-streamed planner's first choice for this job, with this shape
     from analisi_gb300 import engine  # noqa: F401
     with open(cache, "w") as f:
-        f.write(f"{key} 2 2 2 1 1 2 {shape}\n")
+        f.write(f"{key} 2 2 4 1 1 2 {shape}\n")
     b = _child("auto", {"ANALISI_GB300_TUNE_CACHE": cache})
     assert first["sum"] == want["sum"]
     assert b["kernel_used"] == 5

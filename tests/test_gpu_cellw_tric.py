@@ -60,7 +60,7 @@ CASES = [
 ]
 # "reach,r,wx,wy,wz" through ANALISI_GB300_CELLW_PLAN (None: the planner's
 # choice; a plan the planner does not list for a case falls back to its choice)
-PLANS = [None, "1,2,1,1,1", "2,3,1,2,2", "2,4,2,1,1", "3,3,2,2,2", "3,2,1,1,1"]
+PLANS = [None, "1,4,1,1,1", "2,4,1,2,2", "2,4,2,1,1", "3,4,2,2,2", "3,4,1,1,1"]
 
 
 def _ref(oracle_mod, w):
