@@ -136,6 +136,7 @@ struct WarpArea {
     float4 buf[2][CH];           // chunk buffers (bulk-copy destinations, 16-byte aligned)
     ulonglong2 fa[2 * FA];       // first atoms of the batch as f32x2 pairs:
                                  // {(x, x), (y, y)}, {(z, z), (w, w)}, w = type << 24 | id
+    float4 fi[FA];               // the same first atoms {x, y, z, w} (read by the binning)
     unsigned short cq[CQ];       // candidate queue: first atom << 8 | record of the current chunk
     uint4 q[QW];                 // FP64 recheck queue {ia, ja, channel, 0}
     int2 seg[2 * MAXROWS];       // sorted ranges of the neighbourhood rows (two halves each):
@@ -246,8 +247,7 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
             for (int g0 = 0; g0 < cn; g0 += 32) {
                 const bool v = g0 + lane < cn;
                 const unsigned e = v ? (unsigned)A.cq[g0 + lane] : 0u;
-                const float *const fp = reinterpret_cast<const float *>(A.fa) + 8 * (e >> 8);
-                const float4 fi = make_float4(fp[0], fp[2], fp[4], fp[6]);
+                const float4 fi = A.fi[e >> 8];
                 const float4 fj = bufp[e & 0xffu];
                 const float dx = __fsub_rn(fi.x, fj.x), dy = __fsub_rn(fi.y, fj.y),
                             dz = __fsub_rn(fi.z, fj.z);
@@ -274,8 +274,7 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                     const int it = __ffs(needm) - 1;
                     needm &= needm - 1u;
                     const unsigned e = A.cq[it * 32 + lane];
-                    const unsigned iv =
-                                       __float_as_uint(reinterpret_cast<const float *>(A.fa)[8 * (e >> 8) + 6]),
+                    const unsigned iv = __float_as_uint(A.fi[e >> 8].w),
                                    jv = __float_as_uint(bufp[e & 0xffu].w);
                     const int ia = (int)(iv & 0xffffffu), ja = (int)(jv & 0xffffffu);
                     const int ch = chtab[(int)(iv >> 24) * P.ntypes + (int)((jv >> 24) & 63u)] +
@@ -441,6 +440,7 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                         const float4 v = rec_o[rb + (qq - rp)];
                         A.fa[2 * q] = make_ulonglong2(f2pk(v.x, v.x), f2pk(v.y, v.y));
                         A.fa[2 * q + 1] = make_ulonglong2(f2pk(v.z, v.z), f2pk(v.w, v.w));
+                        A.fi[q] = v;
                     }
                 }
                 if (lane == 0) {
@@ -473,13 +473,14 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                     if (b) ph1 ^= 1u; else ph0 ^= 1u;
                     const int n = A.n[b], np = A.np[b];
                     float4 *const bufp = A.buf[b];
-                    // this lane's records 4 lane + t: moved to their piece's image
+                    // this lane's records lane + 32 t (consecutive lanes, consecutive
+                    // records: no bank conflict): moved to their piece's image
                     // (image (0, 0, 0) adds zeros: x + 0 = x) and written back for
                     // the binning; records past n are NaN (never a candidate)
                     float rx[4], ry[4], rz[4];
 #pragma unroll
                     for (int t = 0; t < 4; ++t) {
-                        const int k = 4 * lane + t;
+                        const int k = lane + 32 * t;
                         float4 v = make_float4(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000),
                                                __int_as_float(0x7fc00000),
                                                __uint_as_float(0xffffffffu));
@@ -501,7 +502,7 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                     const f2 xa = f2pk(rx[0], rx[1]), ya = f2pk(ry[0], ry[1]), za = f2pk(rz[0], rz[1]);
                     const f2 xb = f2pk(rx[2], rx[3]), yb = f2pk(ry[2], ry[3]), zb = f2pk(rz[2], rz[3]);
                     __syncwarp();
-                    const unsigned eb0 = (unsigned)(4 * lane);
+                    const unsigned eb0 = (unsigned)lane;
                     for (int i = 0; i < na; ++i) {
                         // first atom i (broadcast) against this lane's four records
                         const ulonglong2 fxy = A.fa[2 * i];
@@ -522,9 +523,9 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                         const int c1 = cn + __popc(b0), c2 = c1 + __popc(b1),
                                   c3 = c2 + __popc(b2);
                         if (p0) A.cq[cn + __popc(b0 & lt)] = (unsigned short)eb;
-                        if (p1) A.cq[c1 + __popc(b1 & lt)] = (unsigned short)(eb + 1u);
-                        if (p2) A.cq[c2 + __popc(b2 & lt)] = (unsigned short)(eb + 2u);
-                        if (p3) A.cq[c3 + __popc(b3 & lt)] = (unsigned short)(eb + 3u);
+                        if (p1) A.cq[c1 + __popc(b1 & lt)] = (unsigned short)(eb + 32u);
+                        if (p2) A.cq[c2 + __popc(b2 & lt)] = (unsigned short)(eb + 64u);
+                        if (p3) A.cq[c3 + __popc(b3 & lt)] = (unsigned short)(eb + 96u);
                         cn = c3 + __popc(b3);
                         if (!GOFR_CHECK(cn <= CQ, P.err)) cn = CQ;
                         // room for the next first atom's entries
