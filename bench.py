@@ -649,8 +649,9 @@ def run_gpu(args):
             "notes": "achieved = 16 FP32 lane operations (one FADD/FMUL/FFMA = 1) x every "
                      "ordered pair of the reference loop (N^2 per origin and lag) / mean kernel "
                      "time: the all-pairs unit of the metric.  The cell-list kernel evaluates "
-                     "only the pairs of neighbouring cells at 7 operations each (images "
-                     "shifted once per tile element); frac_evaluated_pairs is that issue rate "
+                     "only the pairs of neighbouring cells at 7 operations each (three "
+                     "differences, a multiply, two FMAs, the candidate test; neighbours moved "
+                     "to their image once per chunk); frac_evaluated_pairs is that issue rate "
                      "against the same peak.  Candidate binning is counted in neither.  "
                      "traffic = ncu dram bytes per launch (profiles/)",
             "frac_evaluated_pairs": round(achieved_eval / peak, 4),
