@@ -1036,9 +1036,11 @@ std::vector<CellwCand> cellw_candidates(const TrajDev &t, const gofr_params &p)
     std::vector<CellwCand> all;
     // slots carry the neighbour's type in 6 bits
     if (!cell_eligible(t, p, true) || t.ntypes > 64) return all;
-    if (cellw_smem_bytes((int)(t.ntypes * (t.ntypes + 1)), (int)p.nbin, (int)t.ntypes) >
-        110 * 1024)
-        return all;  // two CTAs per SM, or not at all
+    // one CTA of 16 warps per SM or two of 8, or not at all
+    const int nch = (int)(t.ntypes * (t.ntypes + 1));
+    if (cellw_smem_bytes(nch, (int)p.nbin, (int)t.ntypes, 16, 1) > 220 * 1024 &&
+        cellw_smem_bytes(nch, (int)p.nbin, (int)t.ntypes, 8, 1) > 110 * 1024)
+        return all;
     for (int m = 1; m <= 3; ++m) {
         int nc[3];
         CellwGeom g;

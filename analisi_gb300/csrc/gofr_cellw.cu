@@ -71,11 +71,12 @@ namespace cellw {
 constexpr int CH = 128;        // neighbour records per chunk buffer: 4 per lane
 constexpr int MAXP = 8;        // pieces (bulk copies) per chunk
 constexpr int FA = 64;         // first atoms per batch
-constexpr int CQ = 512;        // candidate queue entries of a warp
+constexpr int CQ = 1024;       // candidate queue entries of a warp
 constexpr int CQ_ROOM = 4 * 32; // entries one first-atom group of one step can add
 constexpr int QW = 32;         // FP64 recheck queue of a warp
 constexpr int MAXROWS = CELLW_MAX_ROWS;  // neighbourhood rows of a warp block
 static_assert(CH == 4 * 32, "four records per lane");
+static_assert(CQ / 32 <= 32, "one bit per binning round in a 32-bit recheck mask");
 static_assert(CH <= 256 && FA <= 256, "a queue entry names a first atom and a record in 8 bits each");
 
 typedef unsigned long long f2;
@@ -257,9 +258,11 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                 const unsigned iv = __float_as_uint(fi.w), jv = __float_as_uint(fj.w);
                 const int ch = chtab[(int)(iv >> 24) * P.ntypes + (int)((jv >> 24) & 63u)] +
                                (((iv ^ jv) & 0xffffffu) == 0u ? half_ch : 0);
+                // bin guess (the window test decides): (sqrt(d2) - rmin) / dr as one
+                // FMA, negative guesses clamped to the last bin (whose window fails)
                 const int b_ = __float2int_rd(
-                    __fmul_rn(__fsub_rn(sqrt_guess(d2), P.rmin_f), P.inv_dr_f));
-                const int bi = min(max(b_, 0), P.nbin - 1);
+                    __fmaf_rn(sqrt_guess(d2), P.inv_dr_f, -P.rmin_f * P.inv_dr_f));
+                const int bi = (int)min((unsigned)b_, (unsigned)(P.nbin - 1));
                 const float2 w = win[bi];
                 const bool test = v && d2 >= P.lo_f;
                 const bool inw = d2 >= w.x && d2 <= w.y;
