@@ -1088,8 +1088,9 @@ std::vector<CellwCand> cellw_candidates(const TrajDev &t, const gofr_params &p)
     return all;
 }
 
-// ANALISI_GB300_CELLW_PLAN="reach,r,wx,wy,wz" fixes the warp-streamed
-// configuration (reproducible timings); it must be one the planner accepts.
+// ANALISI_GB300_CELLW_PLAN="reach,4,wx,wy,wz" (4: the records a lane holds)
+// fixes the warp-streamed configuration (reproducible timings); it must be
+// one the planner accepts.
 bool cellw_choice(const TrajDev &t, const gofr_params &p, CellwCand &out)
 {
     const std::vector<CellwCand> all = cellw_candidates(t, p);
@@ -1153,9 +1154,11 @@ bool make_cellw_plan(const TrajDev &t, const gofr_params &p, Plan &pl, const Cel
 // AUTO takes the cell-list form when its modelled time is below this share of
 // the all-pairs kernel's (a margin for the model's error).
 constexpr double kCellAutoTime = 0.85;
-// ... and the warp-streamed form in a triclinic box when its modelled
-// evaluated pairs are below this share of the all-pairs kernel's.
-constexpr double kCellwTricAuto = 0.5;
+// ... and the warp-streamed form where the block form is not taken (a
+// triclinic box, or a box too small for the block form to pay) when its
+// modelled lane work is below this share of the all-pairs kernel's pairs (an
+// evaluated pair costs it about twice an all-pairs one).
+constexpr double kCellwAuto = 0.4;
 
 int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl,
               bool allow_cells = true)
@@ -1201,16 +1204,16 @@ int make_plan(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, Plan &pl,
     }
     // the warp-streamed form: on request, and for AUTO wherever the block
     // cell-list form was taken and the warp form is eligible (measured faster
-    // on every workload where both run), and for triclinic boxes (which the
-    // block form does not take) where its modelled cost is below
-    // kCellwTricAuto of the all-pairs pairs
+    // on every workload where both run), and elsewhere (triclinic boxes,
+    // boxes where the block form does not pay) when its modelled lane work is
+    // below kCellwAuto of the all-pairs pairs
     if (allow_cells && !pl.wrapcheck &&
-        (req == GOFR_KERNEL_CELL_WARP || (req == GOFR_KERNEL_AUTO && (pl.cells || t.tric)))) {
+        (req == GOFR_KERNEL_CELL_WARP || req == GOFR_KERNEL_AUTO)) {
         CellwCand c;
         Plan q = pl;
         q.cells = false;
         if (cellw_choice(t, p, c) &&
-            (req != GOFR_KERNEL_AUTO || pl.cells || c.cost < kCellwTricAuto) &&
+            (req != GOFR_KERNEL_AUTO || pl.cells || c.cost < kCellwAuto) &&
             make_cellw_plan(t, p, q, c))
             pl = q;
     }
@@ -1862,13 +1865,26 @@ int build_batch(gofr_ctx *ctx)
     std::vector<char> is_cell(ctx->trajs.size(), 0);
     for (size_t k = 0; k < ctx->trajs.size(); ++k) {
         const CellCand *c = best_of(k, B.cell_r);
+        gofr_params p = ctx->trajs[k].params;
+        p.nparts = 1;
         if (!c) {
-            B.allpairs_pairs += (unsigned long long)work[k];
+            // the warp-streamed form where the block form does not pay, as AUTO
+            // takes it for a single trajectory
+            CellwCand cw;
+            Plan q = plans[k];
+            q.cells = false;
+            p.kernel = GOFR_KERNEL_AUTO;
+            if (plans[k].kind == 0 && !plans[k].wrapcheck && !plans[k].empty &&
+                cellw_choice(ctx->trajs[k], p, cw) && cw.cost < kCellwAuto &&
+                make_cellw_plan(ctx->trajs[k], p, q, cw)) {
+                plans[k] = q;
+                is_cell[k] = 1;
+            } else {
+                B.allpairs_pairs += (unsigned long long)work[k];
+            }
             continue;
         }
         Plan q = plans[k];
-        gofr_params p = ctx->trajs[k].params;
-        p.nparts = 1;
         if (make_cell_plan(ctx->trajs[k], p, q, *c) &&
             cell_smem_bytes((int)shapes[k].nch, (int)p.nbin, (int)ctx->trajs[k].ntypes) <= 160 * 1024) {
             plans[k] = q;
@@ -1982,6 +1998,8 @@ int build_batch(gofr_ctx *ctx)
         Plan q = plans[k];
         q.cells = false;
         if (!(cellw_choice(t, p, cw) && make_cellw_plan(t, p, q, cw))) {
+            if (plans[k].cellw)  // planned for the warp form alone: no block plan to fall back on
+                return fail(ctx, GOFR_ERR_UNSUPPORTED, "trajectory %d: warp cell-list plan lost", k);
             block_members.push_back(k);
             continue;
         }
@@ -2000,7 +2018,7 @@ int build_batch(gofr_ctx *ctx)
         for (int a = 0; a < 3; ++a) { C.nc[a] = q.nc[a]; C.w[a] = q.wblk[a]; C.nw[a] = q.nw[a]; }
         C.reach = q.reach;
         C.r = q.cell_r;
-        C.cta_warps = 8;
+        C.cta_warps = q.cta_warps;  // as a single run of the member
         C.hcopy = 1;
         set_cellw_geometry(C, q.geom);
         wl.push_back({(unsigned long long)work[k], C});

@@ -69,9 +69,9 @@ enum gofr_kernel {
                                     by timing them on a sample of the job: the all-pairs
                                     kernel, the block cell-list kernel (cell size, block
                                     shape, first atoms per thread) and the warp-streamed
-                                    cell-list kernel (cell size, warp block shape, first
-                                    atoms per lane, CTA size 8 or 16 warps, one or two
-                                    copies of the shared histogram); the choice is
+                                    cell-list kernel (cell size, warp block shape, CTA
+                                    size 8 or 16 warps, one or two copies of the shared
+                                    histogram); the choice is
                                     remembered per key (log2 N, nbin, ntypes, box kind,
                                     cell grid) in the process and, when the environment
                                     variable ANALISI_GB300_TUNE_CACHE names a file, across
@@ -85,8 +85,8 @@ enum gofr_kernel {
                                     edges).  AUTO takes it wherever it would take the block
                                     cell-list form, and for a triclinic box when it
                                     evaluates under half of the pairs.
-                                    ANALISI_GB300_CELLW_PLAN="reach,r,wx,wy,wz" pins its
-                                    configuration */
+                                    ANALISI_GB300_CELLW_PLAN="reach,4,wx,wy,wz" pins its
+                                    configuration (4: the records a lane holds) */
 };
 
 /* Parameters of one Gofrt::calculate (lib/include/gofrt.h:37-45 constructor
