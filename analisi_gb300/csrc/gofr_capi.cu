@@ -1034,8 +1034,7 @@ struct CellwCand {
 std::vector<CellwCand> cellw_candidates(const TrajDev &t, const gofr_params &p)
 {
     std::vector<CellwCand> all;
-    // slots carry the neighbour's type in 6 bits
-    if (!cell_eligible(t, p, true) || t.ntypes > 64) return all;
+    if (!cell_eligible(t, p, true)) return all;
     // one CTA of 16 warps per SM or two of 8, or not at all
     const int nch = (int)(t.ntypes * (t.ntypes + 1));
     if (cellw_smem_bytes(nch, (int)p.nbin, (int)t.ntypes, 16, 1) > 220 * 1024 &&

@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                 d2 = __fmaf_rn(dy, dy, d2);
                 d2 = __fmaf_rn(dz, dz, d2);
                 const unsigned iv = __float_as_uint(fi.w), jv = __float_as_uint(fj.w);
-                const int ch = chtab[(int)(iv >> 24) * P.ntypes + (int)((jv >> 24) & 63u)] +
+                const int ch = chtab[(int)(iv >> 24) * P.ntypes + (int)(jv >> 24)] +
                                (((iv ^ jv) & 0xffffffu) == 0u ? half_ch : 0);
                 // bin guess (the window test decides): (sqrt(d2) - rmin) / dr as one
                 // FMA, negative guesses clamped to the last bin (whose window fails)
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                     const unsigned iv = __float_as_uint(A.fi[e >> 8].w),
                                    jv = __float_as_uint(bufp[e & 0xffu].w);
                     const int ia = (int)(iv & 0xffffffu), ja = (int)(jv & 0xffffffu);
-                    const int ch = chtab[(int)(iv >> 24) * P.ntypes + (int)((jv >> 24) & 63u)] +
+                    const int ch = chtab[(int)(iv >> 24) * P.ntypes + (int)(jv >> 24)] +
                                    (ia == ja ? half_ch : 0);
                     ++n_rech;
                     const int slot = atomicAdd(&A.qn, 1);

@@ -80,7 +80,8 @@ enum gofr_kernel {
     GOFR_KERNEL_CELL_WARP = 5    /* warp-streamed cell-list FP32 + recheck kernel: each warp
                                     streams the neighbourhood of its own small block of cells;
                                     orthorhombic and triclinic boxes (error if not eligible:
-                                    the cell-list conditions, at most 64 types, and tilts
+                                    the cell-list conditions, a histogram and channel
+                                    table that fit shared memory, and tilts
                                     that keep the images a block reaches within two box
                                     edges).  AUTO takes it wherever it would take the block
                                     cell-list form, and for a triclinic box when it
