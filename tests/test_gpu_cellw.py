@@ -195,7 +195,7 @@ def test_cellw_many_types(gpu_engine, oracle_mod):
     """66 types (4422 channels, one bin): the neighbour's type travels in the
     record's top byte, so the warp-streamed kernel takes any type count whose
     histogram and channel table fit shared memory; counts are the oracle's."""
-    counts = [60] * 65 + [3000 - 60 * 65]
+    counts = [40] * 65 + [3000 - 40 * 65]
     w = workloads.small_case(66, 3000, 5, 31.0, 0.2, counts, rmin=0.5, rmax=5.0, nbin=1,
                              tmax=2, skip=1, every=1, ntimesteps=3, primo=0)
     assert w["ntypes"] == 66
