@@ -245,11 +245,19 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
         auto flush_q = [&](const float4 *bufp) {
             __syncwarp();  // every lane's entries and first atoms visible
             unsigned needm = 0u;  // rounds whose entry of this lane goes to the recheck
+            // each round's entry, first atom and record are loaded a round ahead
+            // (a lane past the queue's end reads entry 0's: valid addresses, unused)
+            bool vn = lane < cn;
+            unsigned en = vn ? (unsigned)A.cq[lane] : 0u;
+            float4 fin = A.fi[en >> 8], fjn = bufp[en & 0xffu];
             for (int g0 = 0; g0 < cn; g0 += 32) {
-                const bool v = g0 + lane < cn;
-                const unsigned e = v ? (unsigned)A.cq[g0 + lane] : 0u;
-                const float4 fi = A.fi[e >> 8];
-                const float4 fj = bufp[e & 0xffu];
+                const bool v = vn;
+                const unsigned e = en;
+                const float4 fi = fin, fj = fjn;
+                vn = g0 + 32 + lane < cn;
+                en = vn ? (unsigned)A.cq[g0 + 32 + lane] : 0u;
+                fin = A.fi[en >> 8];
+                fjn = bufp[en & 0xffu];
                 const float dx = __fsub_rn(fi.x, fj.x), dy = __fsub_rn(fi.y, fj.y),
                             dz = __fsub_rn(fi.z, fj.z);
                 float d2 = __fmul_rn(dx, dx);
