@@ -26,12 +26,12 @@
 // stages it into shared memory with one 1-D bulk copy (TMA, cp.async.bulk)
 // per piece (a row's run of records, or the part of it that fits), up to
 // MAXP pieces and CH records per chunk, two chunk buffers per warp,
-// completion tracked by one mbarrier per buffer.  Cells reached across the box boundary are the
-// periodic image of the cell: after the copy lands, the warp moves the
-// chunk's records to that image (x += fl32 of the lattice vector, one FP32
-// rounding per axis; orthorhombic: s fl32(L), the block kernel's
-// arithmetic), so the pair arithmetic and its certified error bound
-// (gofr_capi.cu, error_bound_cells) are the block kernel's.
+// completion tracked by one mbarrier per buffer.  Cells reached across the
+// box boundary are the periodic image of the cell: after the copy lands,
+// each lane moves its records to their piece's image (x += fl32 of the
+// lattice vector, one FP32 rounding per axis; orthorhombic: s fl32(L), the
+// block kernel's arithmetic), so the pair arithmetic and its certified error
+// bound (gofr_capi.cu, error_bound_cells) are the block kernel's.
 //
 // Triclinic boxes (upper-triangular cell vectors a, b, c) use the same
 // kernel.  The reference's minimum image (z, then y, then x) leaves every
@@ -51,8 +51,8 @@
 // their own neighbourhoods and add their candidates to the CTA's shared
 // histogram; the CTA synchronises only at the end of the item, to add the
 // histogram to the counts.  Candidates (FP32 d2 <= hi_f) are compacted into
-// a dense per-warp queue as they are found (one ballot per record and first
-// atom group: each candidate lane writes at the warp's count plus the
+// a dense per-warp queue as they are found (one ballot per first atom and
+// record slot: each candidate lane writes at the warp's count plus the
 // candidates of the lanes below it); an entry names the first atom and the
 // record of the current chunk buffer, 16 bits.  The queue is binned 32
 // entries at a time, every lane busy: when it is nearly full and at the end
@@ -72,7 +72,7 @@ constexpr int CH = 128;        // neighbour records per chunk buffer: 4 per lane
 constexpr int MAXP = 8;        // pieces (bulk copies) per chunk
 constexpr int FA = 64;         // first atoms per batch
 constexpr int CQ = 1024;       // candidate queue entries of a warp
-constexpr int CQ_ROOM = 4 * 32; // entries one first-atom group of one step can add
+constexpr int CQ_ROOM = 4 * 32; // entries one first atom can add (4 records x 32 lanes)
 constexpr int QW = 32;         // FP64 recheck queue of a warp
 constexpr int MAXROWS = CELLW_MAX_ROWS;  // neighbourhood rows of a warp block
 static_assert(CH == 4 * 32, "four records per lane");
