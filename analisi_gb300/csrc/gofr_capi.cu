@@ -695,6 +695,67 @@ int shape_of(gofr_ctx *ctx, const TrajDev &t, const gofr_params &p, RunShape &rs
     return GOFR_OK;
 }
 
+// Coordinate extent of axis k, [mn, mx] over every frame: the centre the
+// FP32 copies are taken about and the bound M on |x - shift|.
+void set_extent(TrajDev &t, int k, double mn, double mx)
+{
+    t.shift[k] = 0.5 * mn + 0.5 * mx;
+    const double m = std::max(std::fabs(mx - t.shift[k]), std::fabs(t.shift[k] - mn));
+    t.M[k] = m * (1.0 + std::ldexp(1.0, -40)) + 1e-300;
+}
+
+// The frames' boxes (stride 6 or 9 doubles each, internal format) into
+// t.h_box (9 per frame, tilts zero when orthorhombic), their statistics t.bs,
+// t.box_constant and the FP32 boxes b32 (nframes of them); the message of
+// the first bad value, or "".
+std::string read_boxes(TrajDev &t, const double *boxes, size_t nframes, size_t stride,
+                       std::vector<Box32> &b32)
+{
+    char msg[160];
+    t.h_box.assign(nframes * 9, 0.0);
+    BoxStats &s = t.bs;
+    for (int k = 0; k < 3; ++k) {
+        s.Lmin[k] = INFINITY; s.Lmax[k] = 0; s.eL[k] = 0; s.tmax[k] = 0; s.eT[k] = 0;
+    }
+    s.lh_min = INFINITY;
+    for (size_t f = 0; f < nframes; ++f) {
+        const double *src = boxes + f * stride;
+        double *dst = &t.h_box[f * 9];
+        for (size_t q = 0; q < stride; ++q) {
+            if (!std::isfinite(src[q])) {
+                std::snprintf(msg, sizeof msg, "non-finite box value in frame %zu", f);
+                return msg;
+            }
+            dst[q] = src[q];
+        }
+        Box32 &bb = b32[f];
+        std::memset(&bb, 0, sizeof bb);
+        for (int k = 0; k < 3; ++k) {
+            double lh = dst[3 + k];
+            if (!(lh > 0.0)) {
+                std::snprintf(msg, sizeof msg,
+                              "box half edge %d of frame %zu is not positive (%g)", k, f, lh);
+                return msg;
+            }
+            double L = lh * 2.0;
+            s.Lmin[k] = std::min(s.Lmin[k], L);
+            s.Lmax[k] = std::max(s.Lmax[k], L);
+            s.lh_min = std::min(s.lh_min, lh);
+            bb.L[k] = (float)L;
+            bb.invL[k] = (float)(1.0 / L);
+            s.eL[k] = std::max(s.eL[k], std::fabs((double)bb.L[k] - L));
+            double tl = dst[6 + k];
+            bb.tilt[k] = (float)tl;
+            s.tmax[k] = std::max(s.tmax[k], std::fabs(tl));
+            s.eT[k] = std::max(s.eT[k], std::fabs((double)bb.tilt[k] - tl));
+        }
+    }
+    t.box_constant = true;
+    for (size_t f = 1; f < nframes && t.box_constant; ++f)
+        t.box_constant = std::memcmp(&t.h_box[f * 9], &t.h_box[0], 9 * sizeof(double)) == 0;
+    return "";
+}
+
 // Upload one trajectory into t (device buffers owned by t).
 int upload_traj(gofr_ctx *ctx, TrajDev &t, const double *positions, const double *boxes,
                 int box_kind, const int *type_ids, unsigned ntypes, size_t natoms, size_t nframes)
@@ -715,44 +776,11 @@ int upload_traj(gofr_ctx *ctx, TrajDev &t, const double *positions, const double
     t.ntypes = ntypes;
     t.tric = box_kind == GOFR_BOX_TRICLINIC;
     const size_t stride = t.tric ? 9 : 6;
-    t.h_box.assign(nframes * 9, 0.0);
-    BoxStats &s = t.bs;
-    for (int k = 0; k < 3; ++k) {
-        s.Lmin[k] = INFINITY; s.Lmax[k] = 0; s.eL[k] = 0; s.tmax[k] = 0; s.eT[k] = 0;
-    }
-    s.lh_min = INFINITY;
     std::vector<Box32> b32(nframes);
-    for (size_t f = 0; f < nframes; ++f) {
-        const double *src = boxes + f * stride;
-        double *dst = &t.h_box[f * 9];
-        for (size_t q = 0; q < stride; ++q) {
-            if (!std::isfinite(src[q]))
-                return fail(ctx, GOFR_ERR_ARG, "non-finite box value in frame %zu", f);
-            dst[q] = src[q];
-        }
-        Box32 &bb = b32[f];
-        std::memset(&bb, 0, sizeof bb);
-        for (int k = 0; k < 3; ++k) {
-            double lh = dst[3 + k];
-            if (!(lh > 0.0))
-                return fail(ctx, GOFR_ERR_ARG,
-                            "box half edge %d of frame %zu is not positive (%g)", k, f, lh);
-            double L = lh * 2.0;
-            s.Lmin[k] = std::min(s.Lmin[k], L);
-            s.Lmax[k] = std::max(s.Lmax[k], L);
-            s.lh_min = std::min(s.lh_min, lh);
-            bb.L[k] = (float)L;
-            bb.invL[k] = (float)(1.0 / L);
-            s.eL[k] = std::max(s.eL[k], std::fabs((double)bb.L[k] - L));
-            double tl = dst[6 + k];
-            bb.tilt[k] = (float)tl;
-            s.tmax[k] = std::max(s.tmax[k], std::fabs(tl));
-            s.eT[k] = std::max(s.eT[k], std::fabs((double)bb.tilt[k] - tl));
-        }
+    {
+        const std::string msg = read_boxes(t, boxes, nframes, stride, b32);
+        if (!msg.empty()) return fail(ctx, GOFR_ERR_ARG, "%s", msg.c_str());
     }
-    t.box_constant = true;
-    for (size_t f = 1; f < nframes && t.box_constant; ++f)
-        t.box_constant = std::memcmp(&t.h_box[f * 9], &t.h_box[0], 9 * sizeof(double)) == 0;
     free_traj(t);
     const size_t n3 = nframes * natoms * 3;
     CK(dev_malloc(&t.pos64, n3 * sizeof(double)));
@@ -810,9 +838,7 @@ int upload_traj(gofr_ctx *ctx, TrajDev &t, const double *positions, const double
             mn = std::min(mn, mm[b * 6 + k]);
             mx = std::max(mx, mm[b * 6 + 3 + k]);
         }
-        t.shift[k] = 0.5 * mn + 0.5 * mx;
-        double m = std::max(std::fabs(mx - t.shift[k]), std::fabs(t.shift[k] - mn));
-        t.M[k] = m * (1.0 + std::ldexp(1.0, -40)) + 1e-300;
+        set_extent(t, k, mn, mx);
     }
     ++ctx->launches;
     if (launch_convert(t.pos64, t.types, nframes, natoms, t.shift[0], t.shift[1], t.shift[2],
@@ -2694,6 +2720,42 @@ int gofr_bin_thresholds(double rmin, double rmax, unsigned nbin, double *th)
     if (!regular_bins(rmin, rmax, nbin)) return GOFR_ERR_UNSUPPORTED;
     BinMap bm(rmin, rmax, nbin);
     thresholds(bm, th);
+    return GOFR_OK;
+}
+
+int gofr_cellw_tables(const double *box, int box_kind, const double *coord_min,
+                      const double *coord_max, double rmax, const int *nc, int *tables,
+                      float *shifts)
+{
+    if (!box || !coord_min || !coord_max || !nc || !tables) return GOFR_ERR_ARG;
+    if (box_kind != GOFR_BOX_ORTHO && box_kind != GOFR_BOX_TRICLINIC) return GOFR_ERR_ARG;
+    if (!(rmax > 0.0) || !std::isfinite(rmax)) return GOFR_ERR_ARG;
+    TrajDev t;
+    t.T = 1;
+    t.N = 1;
+    t.tric = box_kind == GOFR_BOX_TRICLINIC;
+    std::vector<Box32> b32(1);
+    if (!read_boxes(t, box, 1, t.tric ? 9 : 6, b32).empty()) return GOFR_ERR_ARG;
+    for (int k = 0; k < 3; ++k) {
+        if (!(coord_min[k] <= coord_max[k]) || !std::isfinite(coord_min[k]) ||
+            !std::isfinite(coord_max[k]) || nc[k] < 1)
+            return GOFR_ERR_ARG;
+        set_extent(t, k, coord_min[k], coord_max[k]);
+    }
+    gofr_params p{};
+    p.rmax = rmax;
+    CellwGeom g;
+    if (!cellw_geometry(t, p, nc, g)) return GOFR_ERR_UNSUPPORTED;
+    tables[0] = g.nz_lo;
+    tables[1] = g.nz_hi;
+    for (int k = 0; k < 3; ++k) { tables[2 + k] = g.ny_lo[k]; tables[5 + k] = g.ny_hi[k]; }
+    for (int k = 0; k < 15; ++k) { tables[8 + k] = g.nx_lo[k]; tables[23 + k] = g.nx_hi[k]; }
+    if (shifts)
+        for (int k = 0; k < CELLW_NSHIFT; ++k) {
+            shifts[3 * k] = g.shift[k].x;
+            shifts[3 * k + 1] = g.shift[k].y;
+            shifts[3 * k + 2] = g.shift[k].z;
+        }
     return GOFR_OK;
 }
 

@@ -29,7 +29,7 @@ EXPORTED = [
     "gofr_batch_output_layout", "gofr_batch_run", "gofr_measure_peaks",
     "gofr_run_f64_noalloc", "gofr_run_windows", "gofr_set_centres", "gofr_msd_output_size",
     "gofr_msd_run", "gofr_neigh_layout", "gofr_neigh_run", "gofr_run_normalized",
-    "gofr_run_streamed",
+    "gofr_run_streamed", "gofr_cellw_tables",
 ]
 
 
@@ -152,6 +152,8 @@ def load_library(path=None):
     L.gofr_counts_to_buffer.argtypes = [up, ctypes.c_size_t, ctypes.c_uint, ctypes.c_uint,
                                         ctypes.c_uint, dp]
     L.gofr_bin_thresholds.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_uint, dp]
+    L.gofr_cellw_tables.argtypes = [dp, ctypes.c_int, dp, dp, ctypes.c_double, ip, ip,
+                                    ctypes.POINTER(ctypes.c_float)]
     L.gofr_batch_set.argtypes = [vp, ctypes.POINTER(TrajDesc), ctypes.c_uint]
     L.gofr_batch_output_layout.argtypes = [vp, ctypes.c_uint, ctypes.POINTER(ctypes.c_size_t),
                                            ctypes.POINTER(ctypes.c_size_t)]
@@ -177,7 +179,8 @@ def load_library(path=None):
                  "gofr_run_device", "gofr_sync", "gofr_get_stats", "gofr_counts_to_buffer",
                  "gofr_bin_thresholds", "gofr_batch_set", "gofr_batch_output_layout",
                  "gofr_batch_run", "gofr_measure_peaks", "gofr_run_f64_noalloc",
-                 "gofr_run_windows", "gofr_run_normalized", "gofr_run_streamed"):
+                 "gofr_run_windows", "gofr_run_normalized", "gofr_run_streamed",
+                 "gofr_cellw_tables"):
         getattr(L, name).restype = ctypes.c_int
     if path is None:
         _lib = L
@@ -213,6 +216,33 @@ def bin_thresholds(rmin, rmax, nbin):
     if rc != GOFR_OK:
         raise GofrError(rc, "bin map not monotone for these parameters")
     return th
+
+
+def cellw_tables(box, triclinic, coord_min, coord_max, rmax, nc):
+    """Neighbourhood tables of the warp-streamed cell-list kernel for one box
+    (internal format), coordinate extent, rmax and grid (host code): a dict of
+    layer, row and cell ranges relative to a warp block, per lattice image,
+    and the FP32 image vectors [75][3]; None when the kernel refuses the box."""
+    L = load_library()
+    b = np.ascontiguousarray(box, dtype=np.float64)
+    lo = np.ascontiguousarray(coord_min, dtype=np.float64)
+    hi = np.ascontiguousarray(coord_max, dtype=np.float64)
+    n = np.ascontiguousarray(nc, dtype=np.int32)
+    t = np.zeros(38, dtype=np.int32)
+    sh = np.zeros((75, 3), dtype=np.float32)
+    rc = L.gofr_cellw_tables(_dp(b), BOX_TRICLINIC if triclinic else BOX_ORTHO, _dp(lo), _dp(hi),
+                             float(rmax), n.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                             t.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                             sh.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+    if rc == -7:  # GOFR_ERR_UNSUPPORTED
+        return None
+    if rc != GOFR_OK:
+        raise GofrError(rc, "invalid box, extent, rmax or grid")
+    return {"nz": (int(t[0]), int(t[1])),
+            "ny": {sz: (int(t[2 + sz + 1]), int(t[5 + sz + 1])) for sz in (-1, 0, 1)},
+            "nx": {(sz, sy): (int(t[8 + (sz + 1) * 5 + sy + 2]), int(t[23 + (sz + 1) * 5 + sy + 2]))
+                   for sz in (-1, 0, 1) for sy in range(-2, 3)},
+            "shift": sh}
 
 
 def counts_to_buffer(counts, ntimesteps, skip, nparts=0):

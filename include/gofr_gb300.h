@@ -238,6 +238,25 @@ int gofr_counts_to_buffer(const unsigned long long *counts, size_t n, unsigned n
  * (rmax <= rmin, non-finite values). */
 int gofr_bin_thresholds(double rmin, double rmax, unsigned nbin, double *th);
 
+/* Neighbourhood tables of the warp-streamed cell-list kernel (host only, no
+ * device work) for one box (internal format, 6 or 9 doubles), the
+ * coordinates' extent per axis [coord_min, coord_max], rmax and a cell grid
+ * nc[3]: the ranges a warp block of cells [c0, c0 + cn) reaches, relative to
+ * it, per lattice image.  tables (38 ints): layers uz in [cz0 + t[0],
+ * cz0 + cnz + t[1]]; in a layer of image sz (-1..1), rows uy in
+ * [cy0 + t[2 + sz + 1], cy0 + cny + t[5 + sz + 1]]; in a row of images
+ * (sy, sz), cells ux in [cx0 + t[8 + k], cx0 + cnx + t[23 + k]],
+ * k = (sz + 1) 5 + sy + 2 (images s = floor(u / nc)).  shifts (75 x 3
+ * floats, optional): the FP32 lattice vector of image (sx, sy, sz) at
+ * (sx + 2) + 5 (sy + 2) + 25 (sz + 1).  Returns GOFR_ERR_UNSUPPORTED when an
+ * image falls outside the table (the kernel then refuses the box).  No
+ * reference counterpart: the reference evaluates every pair
+ * (lib/src/gofrt.cpp:101-102); this exposes the cell-list geometry so that
+ * its completeness can be checked without a GPU. */
+int gofr_cellw_tables(const double *box, int box_kind, const double *coord_min,
+                      const double *coord_max, double rmax, const int *nc, int *tables,
+                      float *shifts);
+
 /* Measures, on `device`, the two peaks that bound the FP32 pair kernel: the
  * FP32 lane-operation rate (one FFMA = one operation, the unit of the kernel's
  * 16/19 operations per pair) and the shared-memory u32 atomic rate.  No
