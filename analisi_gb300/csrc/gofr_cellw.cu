@@ -12,8 +12,8 @@
 //
 // Lanes hold neighbours, not first atoms: a chunk buffer holds 128 records
 // of the neighbourhood (rows packed back to back, several per chunk when
-// they are short), each lane keeps four of them in registers as f32x2 pairs,
-// and the warp walks the block's first atoms one at a time, each broadcast
+// they are short), each lane keeps four of them in registers, and the warp
+// walks the block's first atoms one at a time, each broadcast
 // from shared memory, so no lane idles for want of a first atom whatever the
 // block's atom count (only the last chunk of a neighbourhood is partly
 // padding).
@@ -79,47 +79,6 @@ static_assert(CH == 4 * 32, "four records per lane");
 static_assert(CQ / 32 <= 32, "one bit per binning round in a 32-bit recheck mask");
 static_assert(CH <= 256 && FA <= 256, "a queue entry names a first atom and a record in 8 bits each");
 
-typedef unsigned long long f2;
-__device__ __forceinline__ f2 f2pk(float a, float b)
-{
-    f2 r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void f2up(f2 v, float &a, float &b)
-{
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
-}
-__device__ __forceinline__ f2 f2sub(f2 a, f2 b)
-{
-    f2 r;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 f2mul(f2 a, f2 b)
-{
-    f2 r;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-    return r;
-}
-__device__ __forceinline__ f2 f2fma(f2 a, f2 b, f2 c)
-{
-    f2 r;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-    return r;
-}
-
-// d2 of (i, j0) and (i, j1), second atoms already in the first atom's image:
-// three differences, one multiply, two FMAs, as f32x2 (the block kernel's).
-__device__ __forceinline__ f2 pair2s(f2 xi, f2 yi, f2 zi, f2 xj, f2 yj, f2 zj)
-{
-    const f2 dx = f2sub(xi, xj), dy = f2sub(yi, yj), dz = f2sub(zi, zj);
-    f2 d2 = f2mul(dx, dx);
-    d2 = f2fma(dy, dy, d2);
-    d2 = f2fma(dz, dz, d2);
-    return d2;
-}
-
 // floor(a / n) for n > 0
 __device__ __forceinline__ int floordiv(int a, int n) { return a >= 0 ? a / n : -((n - 1 - a) / n); }
 
@@ -135,9 +94,7 @@ __device__ __forceinline__ void fence_proxy_async_smem()
 // Shared memory of one warp.
 struct WarpArea {
     float4 buf[2][CH];           // chunk buffers (bulk-copy destinations, 16-byte aligned)
-    ulonglong2 fa[2 * FA];       // first atoms of the batch as f32x2 pairs:
-                                 // {(x, x), (y, y)}, {(z, z), (w, w)}, w = type << 24 | id
-    float4 fi[FA];               // the same first atoms {x, y, z, w} (read by the binning)
+    float4 fi[FA];               // first atoms of the batch {x, y, z, type << 24 | id}
     unsigned short cq[CQ];       // candidate queue: first atom << 8 | record of the current chunk
     uint4 q[QW];                 // FP64 recheck queue {ia, ja, channel, 0}
     int2 seg[2 * MAXROWS];       // sorted ranges of the neighbourhood rows (two halves each):
@@ -252,7 +209,6 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
             float4 fin = A.fi[en >> 8], fjn = bufp[en & 0xffu];
             for (int g0 = 0; g0 < cn; g0 += 32) {
                 const bool v = vn;
-                const unsigned e = en;
                 const float4 fi = fin, fj = fjn;
                 vn = g0 + 32 + lane < cn;
                 en = vn ? (unsigned)A.cq[g0 + 32 + lane] : 0u;
@@ -436,7 +392,7 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
             };
 
             for (int ibase = 0; ibase < n_i && !dead; ibase += FA) {
-                // first atoms ibase .. ibase + na - 1 of the block, as f32x2 pairs
+                // first atoms ibase .. ibase + na - 1 of the block
                 const int na = min(FA, n_i - ibase);
                 for (int q0 = 0; q0 < na; q0 += 32) {
                     const int q = q0 + lane;
@@ -447,12 +403,7 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                         row += (qq >= __shfl_sync(0xffffffffu, ipre, rr)) ? 1 : 0;
                     const int rb = __shfl_sync(0xffffffffu, ib, row);
                     const int rp = __shfl_sync(0xffffffffu, ipre - ilen, row);
-                    if (q < na) {
-                        const float4 v = rec_o[rb + (qq - rp)];
-                        A.fa[2 * q] = make_ulonglong2(f2pk(v.x, v.x), f2pk(v.y, v.y));
-                        A.fa[2 * q + 1] = make_ulonglong2(f2pk(v.z, v.z), f2pk(v.w, v.w));
-                        A.fi[q] = v;
-                    }
+                    if (q < na) A.fi[q] = rec_o[rb + (qq - rp)];
                 }
                 if (lane == 0) {
                     const unsigned long long pe = (unsigned long long)na * (unsigned long long)n_j;
@@ -510,19 +461,23 @@ __global__ void __launch_bounds__(NWARP * 32, 16 / NWARP) k_pairs_cellw(const Ce
                         bufp[k] = v;
                         rx[t] = v.x; ry[t] = v.y; rz[t] = v.z;
                     }
-                    const f2 xa = f2pk(rx[0], rx[1]), ya = f2pk(ry[0], ry[1]), za = f2pk(rz[0], rz[1]);
-                    const f2 xb = f2pk(rx[2], rx[3]), yb = f2pk(ry[2], ry[3]), zb = f2pk(rz[2], rz[3]);
                     __syncwarp();
                     const unsigned eb0 = (unsigned)lane;
                     for (int i = 0; i < na; ++i) {
                         // first atom i (broadcast) against this lane's four records
-                        const ulonglong2 fxy = A.fa[2 * i];
-                        const f2 fz = A.fa[2 * i + 1].x;
-                        const f2 da = pair2s(fxy.x, fxy.y, fz, xa, ya, za);
-                        const f2 db = pair2s(fxy.x, fxy.y, fz, xb, yb, zb);
-                        float d0, d1, d2v, d3;
-                        f2up(da, d0, d1);
-                        f2up(db, d2v, d3);
+                        const float4 fv = A.fi[i];
+                        float dd[4];
+#pragma unroll
+                        for (int t = 0; t < 4; ++t) {
+                            // one difference per axis, a multiply, two FMAs (the
+                            // binning recomputes d2 with the same operations)
+                            const float ex = __fsub_rn(fv.x, rx[t]), ey = __fsub_rn(fv.y, ry[t]),
+                                        ez = __fsub_rn(fv.z, rz[t]);
+                            float s2 = __fmul_rn(ex, ex);
+                            s2 = __fmaf_rn(ey, ey, s2);
+                            dd[t] = __fmaf_rn(ez, ez, s2);
+                        }
+                        const float d0 = dd[0], d1 = dd[1], d2v = dd[2], d3 = dd[3];
                         // entries i << 8 | record, compacted by one ballot per record slot
                         const unsigned eb = (unsigned)i << 8 | eb0;
                         const bool p0 = d0 <= hi_f, p1 = d1 <= hi_f, p2 = d2v <= hi_f,
