@@ -2723,6 +2723,46 @@ int gofr_bin_thresholds(double rmin, double rmax, unsigned nbin, double *th)
     return GOFR_OK;
 }
 
+int gofr_plan_query(const double *box, int box_kind, const double *coord_min,
+                    const double *coord_max, size_t natoms, unsigned ntypes,
+                    const gofr_params *p, int *out)
+{
+    if (!box || !coord_min || !coord_max || !p || !out) return GOFR_ERR_ARG;
+    if (box_kind != GOFR_BOX_ORTHO && box_kind != GOFR_BOX_TRICLINIC) return GOFR_ERR_ARG;
+    if (natoms == 0 || ntypes == 0 || ntypes > 255) return GOFR_ERR_ARG;
+    TrajDev t;
+    t.T = 1;
+    t.N = natoms;
+    t.ntypes = ntypes;
+    t.tric = box_kind == GOFR_BOX_TRICLINIC;
+    std::vector<Box32> b32(1);
+    if (!read_boxes(t, box, 1, t.tric ? 9 : 6, b32).empty()) return GOFR_ERR_ARG;
+    for (int k = 0; k < 3; ++k) {
+        if (!(coord_min[k] <= coord_max[k]) || !std::isfinite(coord_min[k]) ||
+            !std::isfinite(coord_max[k]))
+            return GOFR_ERR_ARG;
+        set_extent(t, k, coord_min[k], coord_max[k]);
+    }
+    gofr_ctx ctx;  // host state only: the planner touches no device
+    Plan pl;
+    const int rc = make_plan(&ctx, t, *p, pl);
+    for (int k = 0; k < 10; ++k) out[k] = 0;
+    if (rc) return rc;
+    out[0] = pl.kind == 1 ? GOFR_KERNEL_F64
+                          : (pl.cellw ? GOFR_KERNEL_CELL_WARP
+                                      : (pl.cells ? GOFR_KERNEL_CELL : GOFR_KERNEL_F32_RECHECK));
+    if (pl.cells) {
+        out[1] = pl.reach;
+        for (int k = 0; k < 3; ++k) {
+            out[2 + k] = pl.nc[k];
+            out[5 + k] = pl.cellw ? pl.wblk[k] : pl.blk[k];
+        }
+        out[8] = pl.cellw ? pl.cta_warps : 0;
+    }
+    out[9] = pl.wrapcheck ? 1 : 0;
+    return GOFR_OK;
+}
+
 int gofr_cellw_tables(const double *box, int box_kind, const double *coord_min,
                       const double *coord_max, double rmax, const int *nc, int *tables,
                       float *shifts)

@@ -29,7 +29,7 @@ EXPORTED = [
     "gofr_batch_output_layout", "gofr_batch_run", "gofr_measure_peaks",
     "gofr_run_f64_noalloc", "gofr_run_windows", "gofr_set_centres", "gofr_msd_output_size",
     "gofr_msd_run", "gofr_neigh_layout", "gofr_neigh_run", "gofr_run_normalized",
-    "gofr_run_streamed", "gofr_cellw_tables",
+    "gofr_run_streamed", "gofr_cellw_tables", "gofr_plan_query",
 ]
 
 
@@ -154,6 +154,8 @@ def load_library(path=None):
     L.gofr_bin_thresholds.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_uint, dp]
     L.gofr_cellw_tables.argtypes = [dp, ctypes.c_int, dp, dp, ctypes.c_double, ip, ip,
                                     ctypes.POINTER(ctypes.c_float)]
+    L.gofr_plan_query.argtypes = [dp, ctypes.c_int, dp, dp, ctypes.c_size_t, ctypes.c_uint,
+                                  ctypes.POINTER(Params), ip]
     L.gofr_batch_set.argtypes = [vp, ctypes.POINTER(TrajDesc), ctypes.c_uint]
     L.gofr_batch_output_layout.argtypes = [vp, ctypes.c_uint, ctypes.POINTER(ctypes.c_size_t),
                                            ctypes.POINTER(ctypes.c_size_t)]
@@ -180,7 +182,7 @@ def load_library(path=None):
                  "gofr_bin_thresholds", "gofr_batch_set", "gofr_batch_output_layout",
                  "gofr_batch_run", "gofr_measure_peaks", "gofr_run_f64_noalloc",
                  "gofr_run_windows", "gofr_run_normalized", "gofr_run_streamed",
-                 "gofr_cellw_tables"):
+                 "gofr_cellw_tables", "gofr_plan_query"):
         getattr(L, name).restype = ctypes.c_int
     if path is None:
         _lib = L
@@ -216,6 +218,25 @@ def bin_thresholds(rmin, rmax, nbin):
     if rc != GOFR_OK:
         raise GofrError(rc, "bin map not monotone for these parameters")
     return th
+
+
+def plan_query(box, triclinic, coord_min, coord_max, natoms, ntypes, params):
+    """The planner's choice for frames in one box (host code, no GPU, tuner
+    cache not consulted): a dict {kernel, reach, cells, block, cta_warps,
+    wrapcheck}; raises GofrError with gofr_run's status when it would fail."""
+    L = load_library()
+    b = np.ascontiguousarray(box, dtype=np.float64)
+    lo = np.ascontiguousarray(coord_min, dtype=np.float64)
+    hi = np.ascontiguousarray(coord_max, dtype=np.float64)
+    out = np.zeros(10, dtype=np.int32)
+    rc = L.gofr_plan_query(_dp(b), BOX_TRICLINIC if triclinic else BOX_ORTHO, _dp(lo), _dp(hi),
+                           int(natoms), int(ntypes), ctypes.byref(params),
+                           out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+    if rc != GOFR_OK:
+        raise GofrError(rc, "the planner refuses these parameters")
+    return {"kernel": int(out[0]), "reach": int(out[1]), "cells": tuple(int(v) for v in out[2:5]),
+            "block": tuple(int(v) for v in out[5:8]), "cta_warps": int(out[8]),
+            "wrapcheck": bool(out[9])}
 
 
 def cellw_tables(box, triclinic, coord_min, coord_max, rmax, nc):

@@ -238,6 +238,22 @@ int gofr_counts_to_buffer(const unsigned long long *counts, size_t n, unsigned n
  * (rmax <= rmin, non-finite values). */
 int gofr_bin_thresholds(double rmin, double rmax, unsigned nbin, double *th);
 
+/* The plan gofr_run's planner takes (host only, no device, tuner cache not
+ * consulted) for frames in one box (internal format, the same in every
+ * frame) with coordinates within [coord_min, coord_max] per axis, natoms
+ * atoms of ntypes types and parameters p (p->kernel as for gofr_run).  out
+ * (10 ints): [0] the kernel (GOFR_KERNEL_F32_RECHECK, _F64, _CELL or
+ * _CELL_WARP), [1] the cell reach, [2..4] cells per axis, [5..7] the
+ * (warp) block of cells, [8] warps per CTA of the warp-streamed kernel, [9] 1
+ * when the all-pairs kernel needs its per-pair wrap check; cell fields 0 for
+ * the all-pairs kernels.  Returns the status gofr_run would (e.g.
+ * GOFR_ERR_UNSUPPORTED for a forced cell-list kernel the box cannot take).
+ * No reference counterpart (the reference has one pair loop,
+ * lib/src/gofrt.cpp:96-122): it shows the planner's choices without a GPU. */
+int gofr_plan_query(const double *box, int box_kind, const double *coord_min,
+                    const double *coord_max, size_t natoms, unsigned ntypes,
+                    const gofr_params *p, int *out);
+
 /* Neighbourhood tables of the warp-streamed cell-list kernel (host only, no
  * device work) for one box (internal format, 6 or 9 doubles), the
  * coordinates' extent per axis [coord_min, coord_max], rmax and a cell grid
