@@ -7,7 +7,10 @@
 //     length check, origins/lags grid, incr;
 //   * exact bin thresholds in d2 space (gofr_bin_thresholds) and the certified
 //     FP32 error bound that turns them into FP32 windows (certify());
-//   * kernel selection, launches, counts back to the caller;
+//   * kernel selection (the planner's cost models, the cell grids and the
+//     warp-streamed kernel's neighbourhood geometry, orthorhombic and
+//     triclinic, with their certified bounds; the autotuner), launches,
+//     counts back to the caller;
 //   * the reference's double result buffer from counts, including its exact
 //     per-thread fold (gofr_counts_to_buffer).
 #include <algorithm>
