@@ -2768,7 +2768,7 @@ int gofr_plan_query(const double *box, int box_kind, const double *coord_min,
 
 int gofr_cellw_tables(const double *box, int box_kind, const double *coord_min,
                       const double *coord_max, double rmax, const int *nc, int *tables,
-                      float *shifts)
+                      float *shifts, double *bound)
 {
     if (!box || !coord_min || !coord_max || !nc || !tables) return GOFR_ERR_ARG;
     if (box_kind != GOFR_BOX_ORTHO && box_kind != GOFR_BOX_TRICLINIC) return GOFR_ERR_ARG;
@@ -2799,6 +2799,10 @@ int gofr_cellw_tables(const double *box, int box_kind, const double *coord_min,
             shifts[3 * k + 1] = g.shift[k].y;
             shifts[3 * k + 2] = g.shift[k].z;
         }
+    if (bound) {
+        const Bound b = t.tric ? error_bound_cells_tric(t, g) : error_bound_cells(t);
+        for (int k = 0; k < 3; ++k) bound[k] = b.e[k];
+    }
     return GOFR_OK;
 }
 

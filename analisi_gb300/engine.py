@@ -153,7 +153,7 @@ def load_library(path=None):
                                         ctypes.c_uint, dp]
     L.gofr_bin_thresholds.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_uint, dp]
     L.gofr_cellw_tables.argtypes = [dp, ctypes.c_int, dp, dp, ctypes.c_double, ip, ip,
-                                    ctypes.POINTER(ctypes.c_float)]
+                                    ctypes.POINTER(ctypes.c_float), dp]
     L.gofr_plan_query.argtypes = [dp, ctypes.c_int, dp, dp, ctypes.c_size_t, ctypes.c_uint,
                                   ctypes.POINTER(Params), ip]
     L.gofr_batch_set.argtypes = [vp, ctypes.POINTER(TrajDesc), ctypes.c_uint]
@@ -243,7 +243,8 @@ def cellw_tables(box, triclinic, coord_min, coord_max, rmax, nc):
     """Neighbourhood tables of the warp-streamed cell-list kernel for one box
     (internal format), coordinate extent, rmax and grid (host code): a dict of
     layer, row and cell ranges relative to a warp block, per lattice image,
-    and the FP32 image vectors [75][3]; None when the kernel refuses the box."""
+    the FP32 image vectors [75][3] and the certified per-axis component error
+    of the kernel's FP32 differences; None when the kernel refuses the box."""
     L = load_library()
     b = np.ascontiguousarray(box, dtype=np.float64)
     lo = np.ascontiguousarray(coord_min, dtype=np.float64)
@@ -251,10 +252,11 @@ def cellw_tables(box, triclinic, coord_min, coord_max, rmax, nc):
     n = np.ascontiguousarray(nc, dtype=np.int32)
     t = np.zeros(38, dtype=np.int32)
     sh = np.zeros((75, 3), dtype=np.float32)
+    e = np.zeros(3)
     rc = L.gofr_cellw_tables(_dp(b), BOX_TRICLINIC if triclinic else BOX_ORTHO, _dp(lo), _dp(hi),
                              float(rmax), n.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
                              t.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
-                             sh.ctypes.data_as(ctypes.POINTER(ctypes.c_float)))
+                             sh.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), _dp(e))
     if rc == -7:  # GOFR_ERR_UNSUPPORTED
         return None
     if rc != GOFR_OK:
@@ -263,7 +265,7 @@ def cellw_tables(box, triclinic, coord_min, coord_max, rmax, nc):
             "ny": {sz: (int(t[2 + sz + 1]), int(t[5 + sz + 1])) for sz in (-1, 0, 1)},
             "nx": {(sz, sy): (int(t[8 + (sz + 1) * 5 + sy + 2]), int(t[23 + (sz + 1) * 5 + sy + 2]))
                    for sz in (-1, 0, 1) for sy in range(-2, 3)},
-            "shift": sh}
+            "shift": sh, "bound": e}
 
 
 def counts_to_buffer(counts, ntimesteps, skip, nparts=0):

@@ -264,14 +264,18 @@ int gofr_plan_query(const double *box, int box_kind, const double *coord_min,
  * (sy, sz), cells ux in [cx0 + t[8 + k], cx0 + cnx + t[23 + k]],
  * k = (sz + 1) 5 + sy + 2 (images s = floor(u / nc)).  shifts (75 x 3
  * floats, optional): the FP32 lattice vector of image (sx, sy, sz) at
- * (sx + 2) + 5 (sy + 2) + 25 (sz + 1).  Returns GOFR_ERR_UNSUPPORTED when an
+ * (sx + 2) + 5 (sy + 2) + 25 (sz + 1).  bound (3 doubles, optional): the
+ * certified per-axis error e_k of the kernel's FP32 difference components
+ * against the reference's FP64 ones, from which the windows follow
+ * (|d2_f32 - d2_ref| <= (2 sqrt(d2) |e| + 2 |e|^2 + 5.01 2^-24 d2)(1 + 2^-20)).
+ * Returns GOFR_ERR_UNSUPPORTED when an
  * image falls outside the table (the kernel then refuses the box).  No
  * reference counterpart: the reference evaluates every pair
  * (lib/src/gofrt.cpp:101-102); this exposes the cell-list geometry so that
  * its completeness can be checked without a GPU. */
 int gofr_cellw_tables(const double *box, int box_kind, const double *coord_min,
                       const double *coord_max, double rmax, const int *nc, int *tables,
-                      float *shifts);
+                      float *shifts, double *bound);
 
 /* Measures, on `device`, the two peaks that bound the FP32 pair kernel: the
  * FP32 lane-operation rate (one FFMA = one operation, the unit of the kernel's
